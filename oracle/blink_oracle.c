@@ -1,0 +1,465 @@
+/*
+ * CPU oracle for the BLINK dirty-imaging path: test infrastructure only (see blink_oracle.h).
+ * Reference citations are paths inside PaCER-BLINK-Project/imager.
+ *
+ * Built with -ffp-contract=off so that no multiply-add is fused: the reference's CPU build on
+ * x86-64 has no FMA, and the results must not depend on the host architecture.
+ */
+#include "blink_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+int bgo_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* src/pacer_imager.cpp:69-70 (also src/gpu/corrections_gpu.cpp:24-25). */
+void bgo_baseline_antennas(uint32_t baseline, uint32_t *a1, uint32_t *a2) {
+    uint32_t i = (uint32_t)(-0.5 + sqrt(0.25 + 2.0 * (double)baseline));
+    *a1 = i;
+    *a2 = baseline - ((i + 1) * i) / 2u;
+}
+
+/* src/pacer_imager.cpp:60-86 */
+void bgo_update_flags(int n_ant, const int *flagged_ants, int n_flagged, int *baseline_flags) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2;
+    for (int64_t b = 0; b < nb; ++b) {
+        uint32_t a1, a2;
+        bgo_baseline_antennas((uint32_t)b, &a1, &a2);
+        int listed = 0;
+        for (int k = 0; k < n_flagged; ++k) {
+            if (flagged_ants[k] == (int)a1 || flagged_ants[k] == (int)a2) { listed = 1; break; }
+        }
+        baseline_flags[b] = (listed || a1 == a2) ? 1 : 0;
+    }
+}
+
+/* src/antenna_positions.cpp:54-56 (pair from the triangular index), :81-89 (zenith branch). */
+void bgo_zenith_uvw(int n_ant, const double *x, const double *y, const double *z,
+                    float *u, float *v, float *w) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2;
+    for (int64_t b = 0; b < nb; ++b) {
+        uint32_t i, j;
+        bgo_baseline_antennas((uint32_t)b, &i, &j);
+        double uu = x[i] - x[j], vv = y[i] - y[j], ww = z[i] - z[j];
+        u[b] = (float)(-uu);
+        v[b] = (float)(-vv);
+        w[b] = (float)(-ww);
+    }
+}
+
+/* src/pacer_imager.cpp:213-221 */
+void bgo_uv_max(int n_baselines, const float *u, const float *v, const int *baseline_flags,
+                double *u_max, double *v_max) {
+    double um = -INFINITY, vm = -INFINITY;
+    for (int b = 0; b < n_baselines; ++b) {
+        if (baseline_flags[b] == 0) {
+            if (um < fabsf(u[b])) um = fabsf(u[b]);
+            if (vm < fabsf(v[b])) vm = fabsf(v[b]);
+        }
+    }
+    *u_max = um;
+    *v_max = vm;
+}
+
+/* src/pacer_imager.cpp:497-499: float oversampling factor promoted to double. */
+double bgo_delta_uv(float oversampling_factor, double uv_max, int n_pixels) {
+    return (double)oversampling_factor * uv_max / n_pixels;
+}
+
+/* src/pacer_imager.cpp:528-555 */
+double bgo_channel_frequency_hz(double frequency_resolution_mhz, int n_averaged_channels,
+                                double coarse_channel_bw_mhz, int coarse_channel,
+                                int fine_channel, int cotter_compatible) {
+    double fine_ch_bw = frequency_resolution_mhz * n_averaged_channels;
+    double coarse_ch_bw = coarse_channel_bw_mhz;
+    double centre = coarse_channel * coarse_ch_bw;
+    double f;
+    if (cotter_compatible)
+        f = centre - coarse_ch_bw / 2.00 + fine_ch_bw * fine_channel;
+    else
+        f = centre - coarse_ch_bw / 2.00 + fine_ch_bw * fine_channel + fine_ch_bw / 2.00;
+    return f * 1e6;
+}
+
+/* Rotation of one complex value by (cos, sin) in double, stored as float
+ * (src/corrections.cpp:26-33, src/gpu/corrections_gpu.cpp:62-69). */
+static inline void rotate_store(float *p, double c, double s) {
+    double re = p[0], im = p[1];
+    double re_prim = re * c - im * s;
+    double im_prim = im * c + re * s;
+    p[0] = (float)re_prim;
+    p[1] = (float)im_prim;
+}
+
+/* src/corrections.cpp:7-39 with w[baseline] as src/gpu/corrections_gpu.cpp:61. */
+void bgo_apply_geometric(float *vis, int n_intervals, int n_channels, int n_ant,
+                         const float *w, int n_uvw_sets, const double *freqs_hz) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int t = 0; t < n_intervals; ++t) {
+        for (int ch = 0; ch < n_channels; ++ch) {
+            const float *wt = w + (n_uvw_sets > 1 ? (int64_t)t * nb : 0);
+            float *rec = vis + (((int64_t)t * n_channels + ch) * nb) * 8;
+            for (int64_t b = 0; b < nb; ++b) {
+                double ww = wt[b];
+                double angle = 2.0 * M_PI * ww * freqs_hz[ch] / BGO_VEL_LIGHT;
+                double s = sin(angle), c = cos(angle);
+                for (int p = 0; p < 4; ++p) rotate_store(rec + b * 8 + 2 * p, c, s);
+            }
+        }
+    }
+}
+
+/* src/corrections.cpp:41-73 */
+void bgo_apply_cable(float *vis, int n_intervals, int n_channels, int n_ant,
+                     const double *cable_lengths, const double *freqs_hz) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int t = 0; t < n_intervals; ++t) {
+        for (int ch = 0; ch < n_channels; ++ch) {
+            float *rec = vis + (((int64_t)t * n_channels + ch) * nb) * 8;
+            for (int a1 = 0; a1 < n_ant; ++a1) {
+                for (int a2 = 0; a2 <= a1; ++a2) {
+                    int64_t b = (int64_t)a1 * (a1 + 1) / 2 + a2;
+                    double d = cable_lengths[a2] - cable_lengths[a1];
+                    double angle = -2.0 * M_PI * d * freqs_hz[ch] / BGO_VEL_LIGHT;
+                    double s = sin(angle), c = cos(angle);
+                    for (int p = 0; p < 4; ++p) rotate_store(rec + b * 8 + 2 * p, c, s);
+                }
+            }
+        }
+    }
+}
+
+/* src/gpu/gridding_gpu.cpp:18-21 */
+static inline int64_t wrap_index(int64_t i, int side) { return i >= 0 ? i % side : side + i; }
+
+/* src/gpu/gridding_gpu.cpp:24-54.  A rounded pixel coordinate of magnitude 2^30 or more
+ * (far outside any grid) is reported as -1 instead of overflowing the int conversion. */
+int64_t bgo_cell_index(float u, float v, double delta_u, double delta_v, double wavelength,
+                       double min_uv, int n_pixels, int uv_sign) {
+    double ul = (double)u / wavelength;
+    double vl = (double)v / wavelength;
+    double dist = sqrt(ul * ul + vl * vl);
+    if (!(dist > min_uv)) return -1;
+    double up = round(ul / delta_u);
+    double vp = round(vl / delta_v);
+    if (!(fabs(up) < 1073741824.0) || !(fabs(vp) < 1073741824.0)) return -1;
+    int64_t ui = wrap_index((int64_t)(uv_sign * up), n_pixels);
+    int64_t vi = wrap_index((int64_t)(uv_sign * vp), n_pixels);
+    return (int64_t)n_pixels * vi + ui;
+}
+
+/* Polarisation selection, src/pacer_imager.cpp:301-325. */
+static inline void select_pol(const float *rec, int pol, float *re, float *im) {
+    if (pol == BGO_POL_XX) {
+        *re = rec[0]; *im = rec[1];
+    } else if (pol == BGO_POL_YY) {
+        *re = rec[6]; *im = rec[7];
+    } else if (pol == BGO_POL_V) {
+        /* (0 + 0.5i) * (xy - yx) */
+        float dr = rec[2] - rec[4], di = rec[3] - rec[5];
+        *re = 0.0f * dr - 0.5f * di;
+        *im = 0.0f * di + 0.5f * dr;
+    } else {
+        *re = (rec[0] + rec[6]) / 2.0f;
+        *im = (rec[1] + rec[7]) / 2.0f;
+    }
+}
+
+static int64_t grid_one_image(const float *rec0, int64_t nb, const float *u, const float *v,
+                              const int *flags, double wavelength, double du, double dv, int n,
+                              double min_uv, int pol, int uniform, float *grid, float *counter) {
+    const int64_t npix = (int64_t)n * n;
+    int64_t gridded = 0;
+    memset(grid, 0, sizeof(float) * 2 * npix);
+    memset(counter, 0, sizeof(float) * npix);
+    for (int64_t b = 0; b < nb; ++b) {
+        if (flags[b]) continue; /* :299 */
+        float re, im;
+        select_pol(rec0 + b * 8, pol, &re, &im);
+        if (isnan(re) || isnan(im)) continue;                          /* :327 */
+        if (!(fabsf(re) < BGO_MAX_VIS && fabsf(im) < BGO_MAX_VIS)) continue; /* :329 */
+        int64_t pos = bgo_cell_index(u[b], v[b], du, dv, wavelength, min_uv, n, +1);
+        if (pos >= 0 && pos < npix) {
+            grid[2 * pos] = grid[2 * pos] + re;
+            grid[2 * pos + 1] = grid[2 * pos + 1] + im;
+            counter[pos] += 1.0f;
+            ++gridded;
+        }
+        int64_t pos2 = bgo_cell_index(u[b], v[b], du, dv, wavelength, min_uv, n, -1);
+        if (pos2 >= 0 && pos2 < npix) {
+            grid[2 * pos2] = grid[2 * pos2] + re;
+            grid[2 * pos2 + 1] = grid[2 * pos2 + 1] - im;
+            counter[pos2] += 1.0f;
+            ++gridded;
+        }
+    }
+    if (uniform) { /* :421-428, empty cells become 0/0 as in the reference */
+        for (int64_t i = 0; i < npix; ++i) {
+            grid[2 * i] = grid[2 * i] / counter[i];
+            grid[2 * i + 1] = grid[2 * i + 1] / counter[i];
+        }
+    }
+    return gridded;
+}
+
+/* src/pacer_imager.cpp:250-432 */
+int64_t bgo_gridding(const float *vis, int n_intervals, int n_channels, int n_ant,
+                     const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                     const double *freqs_hz, double delta_u, double delta_v, int n_pixels,
+                     double min_uv, int pol, int uniform, float *grids, float *counters) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2;
+    const int64_t npix = (int64_t)n_pixels * n_pixels;
+    int64_t total = 0;
+#pragma omp parallel for collapse(2) schedule(static) reduction(+ : total)
+    for (int t = 0; t < n_intervals; ++t) {
+        for (int ch = 0; ch < n_channels; ++ch) {
+            int64_t img = (int64_t)t * n_channels + ch;
+            int64_t set = n_uvw_sets > 1 ? t : 0;
+            double wavelength = BGO_VEL_LIGHT / freqs_hz[ch]; /* :289 */
+            total += grid_one_image(vis + img * nb * 8, nb, u + set * nb, v + set * nb,
+                                    baseline_flags, wavelength, delta_u, delta_v, n_pixels,
+                                    min_uv, pol, uniform, grids + img * npix * 2,
+                                    counters + img * npix);
+        }
+    }
+    return total;
+}
+
+/* ------------------------------------------------------------------------------------------
+ * Inverse DFT of our own: iterative radix-2 (Cooley-Tukey, decimation in time with bit
+ * reversal) for powers of two, direct O(n^2) summation otherwise.  Twiddles exp(+2*pi*i*k/n)
+ * are computed in double from cos/sin.  Generated for double and float arithmetic.
+ * ------------------------------------------------------------------------------------------ */
+static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+#define DEFINE_FFT(T, SUF)                                                                       \
+    static void twiddles_##SUF(T *tw, int n) {                                                 \
+        for (int k = 0; k < n; ++k) {                                                          \
+            double a = 2.0 * M_PI * (double)k / (double)n;                                     \
+            tw[2 * k] = (T)cos(a);                                                             \
+            tw[2 * k + 1] = (T)sin(a);                                                         \
+        }                                                                                      \
+    }                                                                                          \
+    /* in-place inverse transform of n complex values at x[j*stride] */                        \
+    static void fft1_##SUF(T *x, int n, int64_t stride, T *buf, const T *tw) {                 \
+        for (int j = 0; j < n; ++j) {                                                          \
+            buf[2 * j] = x[2 * j * stride];                                                    \
+            buf[2 * j + 1] = x[2 * j * stride + 1];                                            \
+        }                                                                                      \
+        if (is_pow2(n)) {                                                                      \
+            for (int i = 1, j = 0; i < n; ++i) {                                               \
+                int bit = n >> 1;                                                              \
+                for (; j & bit; bit >>= 1) j ^= bit;                                           \
+                j ^= bit;                                                                      \
+                if (i < j) {                                                                   \
+                    T r = buf[2 * i], m = buf[2 * i + 1];                                      \
+                    buf[2 * i] = buf[2 * j]; buf[2 * i + 1] = buf[2 * j + 1];                  \
+                    buf[2 * j] = r; buf[2 * j + 1] = m;                                        \
+                }                                                                              \
+            }                                                                                  \
+            for (int len = 2; len <= n; len <<= 1) {                                           \
+                int half = len >> 1, step = n / len;                                           \
+                for (int s = 0; s < n; s += len) {                                             \
+                    for (int k = 0; k < half; ++k) {                                           \
+                        T wr = tw[2 * k * step], wi = tw[2 * k * step + 1];                    \
+                        T *a = buf + 2 * (s + k), *b = buf + 2 * (s + k + half);               \
+                        T br = b[0] * wr - b[1] * wi, bi = b[0] * wi + b[1] * wr;              \
+                        b[0] = a[0] - br; b[1] = a[1] - bi;                                    \
+                        a[0] = a[0] + br; a[1] = a[1] + bi;                                    \
+                    }                                                                          \
+                }                                                                              \
+            }                                                                                  \
+            for (int j = 0; j < n; ++j) {                                                      \
+                x[2 * j * stride] = buf[2 * j];                                                \
+                x[2 * j * stride + 1] = buf[2 * j + 1];                                        \
+            }                                                                                  \
+        } else {                                                                               \
+            for (int k = 0; k < n; ++k) {                                                      \
+                T sr = 0, si = 0;                                                              \
+                for (int j = 0; j < n; ++j) {                                                  \
+                    int64_t m = ((int64_t)j * k) % n;                                          \
+                    T wr = tw[2 * m], wi = tw[2 * m + 1];                                      \
+                    sr += buf[2 * j] * wr - buf[2 * j + 1] * wi;                               \
+                    si += buf[2 * j] * wi + buf[2 * j + 1] * wr;                               \
+                }                                                                              \
+                x[2 * k * stride] = sr;                                                        \
+                x[2 * k * stride + 1] = si;                                                    \
+            }                                                                                  \
+        }                                                                                      \
+    }                                                                                          \
+    /* in-place 2D inverse transform of one n x n image (rows, then columns) */                \
+    static void fft2_inplace_##SUF(T *img, int n, const T *tw, T *buf) {                       \
+        for (int r = 0; r < n; ++r) fft1_##SUF(img + (int64_t)2 * r * n, n, 1, buf, tw);       \
+        for (int c = 0; c < n; ++c) fft1_##SUF(img + 2 * c, n, n, buf, tw);                   \
+    }
+
+DEFINE_FFT(double, f64)
+DEFINE_FFT(float, f32)
+
+void bgo_fft2_inverse_f64(const double *in, double *out, int n, int n_images) {
+    const int64_t npix = (int64_t)n * n;
+    double *tw = (double *)malloc(sizeof(double) * 2 * n);
+    twiddles_f64(tw, n);
+    memcpy(out, in, sizeof(double) * 2 * npix * n_images);
+#pragma omp parallel
+    {
+        double *buf = (double *)malloc(sizeof(double) * 2 * n);
+#pragma omp for schedule(static)
+        for (int i = 0; i < n_images; ++i) fft2_inplace_f64(out + 2 * npix * i, n, tw, buf);
+        free(buf);
+    }
+    free(tw);
+}
+
+/* One image's 2D transform split over threads (rows, then columns), for batches smaller than
+ * the thread count. */
+static void fft2_parallel_f32(float *img, int n, const float *tw) {
+#pragma omp parallel
+    {
+        float *buf = (float *)malloc(sizeof(float) * 2 * n);
+#pragma omp for schedule(static)
+        for (int r = 0; r < n; ++r) fft1_f32(img + (int64_t)2 * r * n, n, 1, buf, tw);
+#pragma omp for schedule(static)
+        for (int c = 0; c < n; ++c) fft1_f32(img + 2 * c, n, n, buf, tw);
+        free(buf);
+    }
+}
+
+void bgo_fft2_inverse_f32(const float *in, float *out, int n, int n_images) {
+    const int64_t npix = (int64_t)n * n;
+    float *tw = (float *)malloc(sizeof(float) * 2 * n);
+    twiddles_f32(tw, n);
+    memcpy(out, in, sizeof(float) * 2 * npix * n_images);
+    if (n_images < bgo_max_threads()) {
+        for (int i = 0; i < n_images; ++i) fft2_parallel_f32(out + 2 * npix * i, n, tw);
+    } else {
+#pragma omp parallel
+        {
+            float *buf = (float *)malloc(sizeof(float) * 2 * n);
+#pragma omp for schedule(static)
+            for (int i = 0; i < n_images; ++i) fft2_inplace_f32(out + 2 * npix * i, n, tw, buf);
+            free(buf);
+        }
+    }
+    free(tw);
+}
+
+/* src/pacer_imager.cpp:30-35 */
+static inline int calc_fft_shift(int pos, int side) {
+    int is_odd = side % 2;
+    return (pos + side / 2 + is_odd) % side;
+}
+
+#define DEFINE_SHIFT(T, SUF)                                                                     \
+    void bgo_fft_shift_##SUF(T *image, int xs, int ys) {                                         \
+        for (int y = 0; y < ys; ++y) {                                                           \
+            for (int x = 0; x < xs / 2; ++x) {                                                   \
+                int64_t src = (int64_t)y * xs + x;                                               \
+                int64_t dst = (int64_t)y * xs + calc_fft_shift(x, xs);                           \
+                T r = image[2 * src], i = image[2 * src + 1];                                    \
+                image[2 * src] = image[2 * dst]; image[2 * src + 1] = image[2 * dst + 1];        \
+                image[2 * dst] = r; image[2 * dst + 1] = i;                                      \
+            }                                                                                    \
+        }                                                                                        \
+        for (int y = 0; y < ys / 2; ++y) {                                                       \
+            for (int x = 0; x < xs; ++x) {                                                       \
+                int64_t src = (int64_t)y * xs + x;                                               \
+                int64_t dst = (int64_t)calc_fft_shift(y, ys) * xs + x;                           \
+                T r = image[2 * src], i = image[2 * src + 1];                                    \
+                image[2 * src] = image[2 * dst]; image[2 * src + 1] = image[2 * dst + 1];        \
+                image[2 * dst] = r; image[2 * dst + 1] = i;                                      \
+            }                                                                                    \
+        }                                                                                        \
+    }
+
+DEFINE_SHIFT(double, f64)
+DEFINE_SHIFT(float, f32)
+
+/* src/pacer_imager.cpp:134-208 in FP64: FFT, multiply by 1/sum(counter), shift. */
+void bgo_image_f64(const float *grids, const float *counters, int n, int n_images,
+                   double *images) {
+    const int64_t npix = (int64_t)n * n;
+    double *tw = (double *)malloc(sizeof(double) * 2 * n);
+    twiddles_f64(tw, n);
+#pragma omp parallel
+    {
+        double *buf = (double *)malloc(sizeof(double) * 2 * n);
+#pragma omp for schedule(static)
+        for (int i = 0; i < n_images; ++i) {
+            double *img = images + 2 * npix * i;
+            const float *g = grids + 2 * npix * i;
+            for (int64_t k = 0; k < 2 * npix; ++k) img[k] = g[k];
+            fft2_inplace_f64(img, n, tw, buf);
+            double sum = 0.0;
+            const float *c = counters + npix * i;
+            for (int64_t k = 0; k < npix; ++k) sum += c[k];
+            double fnorm = 1.00 / sum;
+            for (int64_t k = 0; k < 2 * npix; ++k) img[k] *= fnorm;
+            bgo_fft_shift_f64(img, n, n);
+        }
+        free(buf);
+    }
+    free(tw);
+}
+
+/* Reference CPU run() in FP32: gridding (:250-432), FFT (:150-152), normalise by
+ * (float)(1/sum) (:171-178) and shift (:179). */
+void bgo_run_f32(const float *vis, int n_intervals, int n_channels, int n_ant,
+                 const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                 const double *freqs_hz, double delta_u, double delta_v, int n_pixels,
+                 double min_uv, int pol, float *grids, float *counters, float *images) {
+    const int n_images = n_intervals * n_channels;
+    const int64_t npix = (int64_t)n_pixels * n_pixels;
+    bgo_gridding(vis, n_intervals, n_channels, n_ant, u, v, n_uvw_sets, baseline_flags, freqs_hz,
+                 delta_u, delta_v, n_pixels, min_uv, pol, 0, grids, counters);
+    bgo_fft2_inverse_f32(grids, images, n_pixels, n_images);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n_images; ++i) {
+        double sum = 0.0;
+        const float *c = counters + npix * i;
+        for (int64_t k = 0; k < npix; ++k) sum += c[k];
+        float fnorm = (float)(1.00 / sum);
+        float *img = images + 2 * npix * i;
+        for (int64_t k = 0; k < 2 * npix; ++k) img[k] *= fnorm;
+        bgo_fft_shift_f32(img, n_pixels, n_pixels);
+    }
+}
+
+/* src/gpu/gpu_utils.cpp:19-71 (per-image sum); double accumulation makes it exact for the
+ * integer-valued counters it is used on. */
+void bgo_vector_sum(const float *data, int64_t image_size, int n_images, double *sums) {
+    for (int i = 0; i < n_images; ++i) {
+        double s = 0.0;
+        for (int64_t k = 0; k < image_size; ++k) s += data[(int64_t)i * image_size + k];
+        sums[i] = s;
+    }
+}
+
+/* src/gpu/gpu_utils.cpp:143-150: running complex sum over images, then divide by count. */
+void bgo_image_average(const float *images, int64_t image_size, int n_images, float *out) {
+    for (int64_t k = 0; k < image_size; ++k) {
+        float r = images[2 * k], m = images[2 * k + 1];
+        for (int i = 1; i < n_images; ++i) {
+            r += images[2 * (k + (int64_t)i * image_size)];
+            m += images[2 * (k + (int64_t)i * image_size) + 1];
+        }
+        out[2 * k] = r / (float)n_images;
+        out[2 * k + 1] = m / (float)n_images;
+    }
+}

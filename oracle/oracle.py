@@ -1,0 +1,236 @@
+"""ctypes wrapper of the CPU oracle (oracle/blink_oracle.c) -- test infrastructure only.
+
+The oracle restates the reference imager's CPU path (PaCER-BLINK-Project/imager,
+src/pacer_imager.cpp, src/corrections.cpp) in C.  Only tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` import this module, and only as the checker.
+
+``ref_library()`` loads the reference's own CPU sources compiled here against the stand-ins in
+``oracle/ref_shim`` (``make -C oracle ref``), when that build exists.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libblink_oracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libpacer_ref.so")
+REF_SRC = "/root/reference/src"
+
+POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+_lib = None
+_ref = None
+
+
+def build(ref: bool = False) -> None:
+    """Compile the oracle (and, when the reference checkout exists and ref is set, the
+    reference CPU build)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref and os.path.isdir(REF_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def library():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        lib = C.CDLL(LIB_PATH)
+        i64, i32, dbl, flt = C.c_int64, C.c_int, C.c_double, C.c_float
+        sig = {
+            "bgo_update_flags": (None, [i32, _i32p, i32, _i32p]),
+            "bgo_zenith_uvw": (None, [i32, _f64p, _f64p, _f64p, _f32p, _f32p, _f32p]),
+            "bgo_uv_max": (None, [i32, _f32p, _f32p, _i32p, C.POINTER(dbl), C.POINTER(dbl)]),
+            "bgo_delta_uv": (dbl, [flt, dbl, i32]),
+            "bgo_channel_frequency_hz": (dbl, [dbl, i32, dbl, i32, i32, i32]),
+            "bgo_apply_geometric": (None, [_f32p, i32, i32, i32, _f32p, i32, _f64p]),
+            "bgo_apply_cable": (None, [_f32p, i32, i32, i32, _f64p, _f64p]),
+            "bgo_cell_index": (i64, [flt, flt, dbl, dbl, dbl, dbl, i32, i32]),
+            "bgo_gridding": (i64, [_f32p, i32, i32, i32, _f32p, _f32p, i32, _i32p, _f64p, dbl,
+                                   dbl, i32, dbl, i32, i32, _f32p, _f32p]),
+            "bgo_fft2_inverse_f64": (None, [_f64p, _f64p, i32, i32]),
+            "bgo_fft2_inverse_f32": (None, [_f32p, _f32p, i32, i32]),
+            "bgo_fft_shift_f32": (None, [_f32p, i32, i32]),
+            "bgo_fft_shift_f64": (None, [_f64p, i32, i32]),
+            "bgo_image_f64": (None, [_f32p, _f32p, i32, i32, _f64p]),
+            "bgo_run_f32": (None, [_f32p, i32, i32, i32, _f32p, _f32p, i32, _i32p, _f64p, dbl,
+                                   dbl, i32, dbl, i32, _f32p, _f32p, _f32p]),
+            "bgo_vector_sum": (None, [_f32p, i64, i32, _f64p]),
+            "bgo_image_average": (None, [_f32p, i64, i32, _f32p]),
+            "bgo_max_threads": (i32, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def ref_library():
+    """The reference's own CPU code (built here against ref_shim), or None when absent."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        lib = C.CDLL(REF_PATH)
+        i32, dbl, flt = C.c_int, C.c_double, C.c_float
+        lib.ref_apply_geometric_cpu.argtypes = [_f32p, i32, i32, i32, _f32p, _f64p]
+        lib.ref_apply_cable_cpu.argtypes = [_f32p, i32, i32, i32, _f64p, _f64p]
+        lib.ref_fft_shift.argtypes = [_f32p, i32, i32]
+        lib.ref_fft_shift.restype = None
+        lib.ref_run.argtypes = [_f32p, i32, i32, i32, _f32p, _f32p, _f32p, _f64p, _i32p, i32,
+                                dbl, i32, dbl, i32, dbl, i32, flt, dbl, i32, C.c_char_p, i32,
+                                i32, _f32p, _f32p, _f32p, _f32p, _f64p]
+        _ref = lib
+    return _ref
+
+
+# ---------------------------------------------------------------------------------------------
+# numpy-level helpers
+# ---------------------------------------------------------------------------------------------
+def n_baselines(n_ant: int) -> int:
+    return n_ant * (n_ant + 1) // 2
+
+
+def update_flags(n_ant, flagged_ants=()):
+    fl = np.zeros(n_baselines(n_ant), np.int32)
+    fa = np.ascontiguousarray(np.asarray(list(flagged_ants) or [0], np.int32))
+    library().bgo_update_flags(n_ant, fa, len(flagged_ants), fl)
+    return fl
+
+
+def zenith_uvw(x, y, z):
+    x, y, z = (np.ascontiguousarray(a, np.float64) for a in (x, y, z))
+    nb = n_baselines(len(x))
+    u, v, w = (np.zeros(nb, np.float32) for _ in range(3))
+    library().bgo_zenith_uvw(len(x), x, y, z, u, v, w)
+    return u, v, w
+
+
+def uv_max(u, v, flags):
+    """max |u|, |v| over unflagged baselines of every UVW set in u, v ([sets][B] or [B])."""
+    u = np.ascontiguousarray(u, np.float32).reshape(-1)
+    v = np.ascontiguousarray(v, np.float32).reshape(-1)
+    fl = np.ascontiguousarray(np.tile(np.asarray(flags, np.int32), len(u) // len(flags)))
+    um, vm = C.c_double(), C.c_double()
+    library().bgo_uv_max(len(u), u, v, fl, C.byref(um), C.byref(vm))
+    return um.value, vm.value
+
+
+def delta_uv(osf, uvmax, n_pixels):
+    return library().bgo_delta_uv(osf, uvmax, n_pixels)
+
+
+def apply_geometric(vis, w, freqs, n_uvw_sets=1):
+    """In place on a float32 array [T][C][B][4][2]."""
+    T, Cn, nb = vis.shape[:3]
+    n_ant = int(round((-1 + np.sqrt(1 + 8 * nb)) / 2))
+    library().bgo_apply_geometric(vis.reshape(-1), T, Cn, n_ant, np.ascontiguousarray(w, np.float32),
+                                  n_uvw_sets, np.ascontiguousarray(freqs, np.float64))
+
+
+def apply_cable(vis, cable, freqs):
+    T, Cn, nb = vis.shape[:3]
+    n_ant = len(cable)
+    library().bgo_apply_cable(vis.reshape(-1), T, Cn, n_ant, np.ascontiguousarray(cable, np.float64),
+                              np.ascontiguousarray(freqs, np.float64))
+
+
+def cell_index(u, v, du, dv, wavelength, min_uv, n_pixels, sign):
+    return library().bgo_cell_index(u, v, du, dv, wavelength, min_uv, n_pixels, sign)
+
+
+def gridding(vis, u, v, flags, freqs, du, dv, n_pixels, min_uv=-1000.0, pol="XX", uniform=False,
+             n_uvw_sets=1):
+    T, Cn, nb = vis.shape[:3]
+    n_ant = int(round((-1 + np.sqrt(1 + 8 * nb)) / 2))
+    grids = np.zeros((T, Cn, n_pixels, n_pixels, 2), np.float32)
+    counters = np.zeros((T, Cn, n_pixels, n_pixels), np.float32)
+    n = library().bgo_gridding(np.ascontiguousarray(vis, np.float32).reshape(-1), T, Cn, n_ant,
+                               np.ascontiguousarray(u, np.float32), np.ascontiguousarray(v, np.float32),
+                               n_uvw_sets, np.ascontiguousarray(flags, np.int32),
+                               np.ascontiguousarray(freqs, np.float64), du, dv, n_pixels, min_uv,
+                               POL[pol], int(uniform), grids.reshape(-1), counters.reshape(-1))
+    return grids, counters, n
+
+
+def fft2_inverse_f64(x):
+    """x complex128 [..., N, N] -> unnormalised inverse 2D DFT."""
+    n = x.shape[-1]
+    a = np.ascontiguousarray(x, np.complex128)
+    out = np.empty_like(a)
+    library().bgo_fft2_inverse_f64(a.view(np.float64).reshape(-1), out.view(np.float64).reshape(-1),
+                                   n, a.size // (n * n))
+    return out
+
+
+def fft_shift(img):
+    """fftshift of a complex64 [ny, nx] image by the reference's half swaps (returns a copy)."""
+    a = np.ascontiguousarray(img, np.complex64).copy()
+    library().bgo_fft_shift_f32(a.view(np.float32).reshape(-1), a.shape[1], a.shape[0])
+    return a
+
+
+def image_f64(grids, counters):
+    """grids float32 [..., N, N, 2], counters [..., N, N] -> complex128 images [..., N, N]."""
+    n = counters.shape[-1]
+    n_images = counters.size // (n * n)
+    out = np.empty(counters.shape, np.complex128)
+    library().bgo_image_f64(np.ascontiguousarray(grids, np.float32).reshape(-1),
+                            np.ascontiguousarray(counters, np.float32).reshape(-1), n, n_images,
+                            out.view(np.float64).reshape(-1))
+    return out
+
+
+def run_f32(vis, u, v, flags, freqs, du, dv, n_pixels, min_uv=-1000.0, pol="XX", n_uvw_sets=1):
+    T, Cn, nb = vis.shape[:3]
+    n_ant = int(round((-1 + np.sqrt(1 + 8 * nb)) / 2))
+    grids = np.zeros((T, Cn, n_pixels, n_pixels, 2), np.float32)
+    counters = np.zeros((T, Cn, n_pixels, n_pixels), np.float32)
+    images = np.zeros((T, Cn, n_pixels, n_pixels, 2), np.float32)
+    library().bgo_run_f32(np.ascontiguousarray(vis, np.float32).reshape(-1), T, Cn, n_ant,
+                          np.ascontiguousarray(u, np.float32), np.ascontiguousarray(v, np.float32),
+                          n_uvw_sets, np.ascontiguousarray(flags, np.int32),
+                          np.ascontiguousarray(freqs, np.float64), du, dv, n_pixels, min_uv, POL[pol],
+                          grids.reshape(-1), counters.reshape(-1), images.reshape(-1))
+    return images.view(np.complex64)[..., 0]
+
+
+def vector_sum(data, image_size, n_images):
+    out = np.zeros(n_images, np.float64)
+    library().bgo_vector_sum(np.ascontiguousarray(data, np.float32).reshape(-1), image_size, n_images, out)
+    return out
+
+
+def image_average(images):
+    """complex64 [n, ...] -> complex64 mean image."""
+    a = np.ascontiguousarray(images, np.complex64)
+    n = a.shape[0]
+    size = a[0].size
+    out = np.zeros(a.shape[1:], np.complex64)
+    library().bgo_image_average(a.view(np.float32).reshape(-1), size, n, out.view(np.float32).reshape(-1))
+    return out
+
+
+def full_pipeline(vis_raw, u, v, w, cable, flags, freqs, n_pixels, osf=2.0, min_uv=-1000.0,
+                  pol="XX", n_uvw_sets=1, apply_geom=True, apply_cable_corr=True):
+    """Reference run(): corrections, delta_u from u_max, gridding, FP64 images.
+    Returns (corrected vis, grids, counters, images complex128, (du, dv))."""
+    vis = np.array(vis_raw, np.float32, copy=True)
+    if apply_geom:
+        apply_geometric(vis, w, freqs, n_uvw_sets)
+    if apply_cable_corr:
+        apply_cable(vis, cable, freqs)
+    umax, vmax = uv_max(u, v, flags)
+    du, dv = delta_uv(osf, umax, n_pixels), delta_uv(osf, vmax, n_pixels)
+    grids, counters, _ = gridding(vis, u, v, flags, freqs, du, dv, n_pixels, min_uv, pol,
+                                  n_uvw_sets=n_uvw_sets)
+    images = image_f64(grids, counters)
+    return vis, grids, counters, images, (du, dv)
