@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 BLINK dirty-imaging path; prints one JSON line on rank 0.
+
+Workload (one step): a block of 256 antennas (32,896 baselines incl. autos), 64 channels over
+150-180 MHz x 10 intervals of 1 s with Earth-rotated zenith UVW, complex64 4-pol
+visibilities (673 MB), imaged to 640 dirty images of 512x512 (pol XX, oversampling 2, natural
+weighting): geometric + cable corrections, nearest-neighbour gridding, inverse 2D FFT,
+fftshift and normalisation.  Inputs are seeded synthetic data with that shape (no public data
+set exists for this path).
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+`--impl reference` times the reference's CPU imaging path (the C restatement in oracle/, run
+with every host thread) on bounded samples of the same workload.  Under torchrun each rank
+images its own block (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "images/s & vis/s: mixed-precision batched vs plain FP32 GPU at ≤1e-4 rel err"
+WORKLOAD = ("256 antennas in a 35 m disk (32896 baselines incl. autos), 64 channels 150-180 MHz x "
+            "10 intervals (1 s, Earth-rotated zenith UVW), complex64 4-pol visibilities -> 640 dirty "
+            "images 512x512, pol XX, osf 2, natural weighting: geometric+cable corrections, "
+            "nearest-neighbour gridding, inverse 2D FFT, fftshift + 1/sum(w)")
+HBM_PEAK_FALLBACK = 6800.0
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_PEAK_FALLBACK, "fallback"
+
+
+# ------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples every 100 ms; lines are kept for the GPU whose UUID matches."""
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, uuid: str):
+        self.samples = []
+        self.proc = None
+        self.uuid = uuid.lower().replace("gpu-", "") if uuid else ""
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            uid = parts[0].lower().replace("gpu-", "")
+            if self.uuid and uid != self.uuid:
+                continue
+            if not self.uuid:
+                self.uuid = uid
+            try:
+                self.samples.append((time.monotonic(), float(parts[1]), float(parts[2]), parts[4:8]))
+            except ValueError:
+                pass
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        inside = [s for s in self.samples if t0 <= s[0] <= t1]
+        basis = "timed region"
+        if len(inside) < 3:
+            inside = self.samples
+            basis = "whole run (timed region shorter than the sampling period)"
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "basis": "nvidia-smi unavailable"}
+        reasons = sorted({self.NAMES[i] for s in inside for i, r in enumerate(s[3]) if r.lower() == "active"})
+        return {"sm_mhz": statistics.median(s[1] for s in inside), "sm_max_mhz": max(s[2] for s in inside),
+                "reasons": reasons, "samples": len(inside), "basis": basis}
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baseline: the reference CPU path restated in oracle/ (OpenMP, every host thread)
+# ------------------------------------------------------------------------------------------
+def cpu_sample_rate(obs, n_channels_sample: int, seconds: float, steps: int = 0):
+    """Images/s of the CPU path on interval 0 x the first n channels: corrections, gridding,
+    FFT (FP32), normalise, shift.  Repeats until `seconds` or for `steps` repetitions."""
+    from oracle import oracle as O
+    O.build()
+    vis0 = np.ascontiguousarray(obs.vis_f32()[:1, :n_channels_sample])
+    u, v, w = obs.u[:1], obs.v[:1], obs.w[:1]
+    freqs = obs.freqs[:n_channels_sample]
+    umax, vmax = O.uv_max(obs.u, obs.v, obs.flags)
+    du, dv = O.delta_uv(2.0, umax, obs.n_pixels), O.delta_uv(2.0, vmax, obs.n_pixels)
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        vis = vis0.copy()
+        O.apply_geometric(vis, w, freqs)
+        O.apply_cable(vis, obs.cable, freqs)
+        O.run_f32(vis, u, v, obs.flags, freqs, du, dv, obs.n_pixels, -1000.0, "XX")
+        times.append(time.perf_counter() - t0)
+        if steps and len(times) >= steps:
+            break
+        if not steps and time.perf_counter() - t_start >= seconds:
+            break
+    return n_channels_sample / statistics.median(times), times, O.library().bgo_max_threads()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from imager_gb300 import synth
+    obs = synth.config2(device="cpu", n_intervals=1)
+    n_sample = 16
+    from oracle import oracle as O
+    O.build()
+    # warm-up steps, then K timed steps (each a bounded 16-image sample of the workload)
+    cpu_sample_rate(obs, n_sample, 0.0, steps=max(1, args.warmup))
+    rate, times, threads = cpu_sample_rate(obs, n_sample, 0.0, steps=args.steps)
+    ms = 1000.0 * statistics.mean(times)
+    out = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "images/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded; shapes of the workload)",
+           "config": {"workload": WORKLOAD, "images_per_step": n_sample},
+           "cpu_baseline": {"value": rate, "unit": "images/s", "cores": threads, "kind": "port",
+                            "sample": f"{n_sample} images (interval 0, channels 0-{n_sample - 1}) per step: "
+                                      "corrections, gridding, FP32 FFT, normalise, shift"},
+           "e2e": {"value": rate, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "reference CPU path restated in C (oracle/); the reference's own build needs astroio, "
+                   "FFTW, cfitsio and msfitslib, absent on this box"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from imager_gb300 import capi, synth
+    from imager_gb300.imager import APPLY_CABLE, APPLY_GEOMETRIC, Imager
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    capi.lib(build_if_missing=True)
+    obs = synth.config2(device="cuda")
+    T, Cn, B = obs.vis.shape[:3]
+    N = obs.n_pixels
+    n_images = T * Cn
+    vis_np = obs.vis_f32()
+    vis = torch.from_numpy(vis_np).cuda()
+    out = torch.empty((T, Cn, N, N), dtype=torch.complex64, device="cuda")
+    im = Imager(N, 2.0, "XX", -1000.0, max_images_per_wave=args.wave)
+    im.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+    im.set_frequencies(obs.freqs)
+    flags = APPLY_GEOMETRIC | APPLY_CABLE
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        im.image(vis, flags=flags, out=out)
+    torch.cuda.synchronize()
+    sums = im.weight_sums(n_images)
+    gridded_vis = int(sums.sum()) // 2  # each gridded visibility lands at two cells
+
+    props = torch.cuda.get_device_properties(local_rank)
+    uuid = str(getattr(props, "uuid", "") or "")
+    clocks = ClockSampler(uuid if len(uuid.replace("GPU-", "")) == 36 else "")
+    clocks.start()
+    time.sleep(0.3)
+    im.set_stage_timing(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.monotonic()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        im.image(vis, flags=flags, out=out)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t1 = time.monotonic()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    stages = im.stage_times()
+    im.set_stage_timing(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the host-buffer entry point: pinned input, pinned output
+    vis_h = torch.from_numpy(vis_np).pin_memory()
+    out_h = torch.empty((T, Cn, N, N), dtype=torch.complex64).pin_memory()
+    e2e_steps = max(3, min(args.steps, 20))
+    im.image_host(vis_h, flags=flags, out=out_h)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for _ in range(e2e_steps):
+        im.image_host(vis_h, flags=flags, out=out_h)
+    e2e_s = (time.perf_counter() - t2) / e2e_steps
+    t3 = time.monotonic()
+    clocks.stop()
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return 0
+
+    # parity spot check of the timed output: three images against the FP64 oracle
+    from oracle import oracle as O
+    O.build()
+    du, dv, _, _ = im.uv_cell
+    corr = np.ascontiguousarray(vis_np[[0, 9]][:, [0, 63]])
+    O.apply_geometric(corr, np.ascontiguousarray(obs.w[[0, 9]]), obs.freqs[[0, 63]], n_uvw_sets=2)
+    O.apply_cable(corr, obs.cable, obs.freqs[[0, 63]])
+    errs = []
+    for k, (t, c) in enumerate(((0, 0), (9, 63))):
+        g, cnt, _ = O.gridding(corr[k:k + 1, k:k + 1], obs.u[t:t + 1], obs.v[t:t + 1], obs.flags,
+                               obs.freqs[c:c + 1], du, dv, N)
+        ref = O.image_f64(g, cnt)[0, 0]
+        got = out[t, c].cpu().numpy().astype(np.complex128)
+        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+
+    images_per_s = world * n_images * args.steps / (ms / 1000.0)
+    hbm_peak, peak_kind = measured_peaks()
+    # algorithmic bytes per image of each stage
+    alg = {"gridding": B * 32 + 8 * N * N, "fft_rows": 16 * N * N, "fft_cols": 16 * N * N}
+    stage_info = {}
+    for k, (tot_ms, launches) in stages.items():
+        if launches:
+            per_launch_ms = tot_ms / launches
+            imgs_per_launch = n_images * args.steps / launches
+            gbs = alg[k] * imgs_per_launch / (per_launch_ms / 1000.0) / 1e9
+            stage_info[k] = {"ms_per_launch": per_launch_ms, "launches": launches,
+                             "images_per_launch": imgs_per_launch, "achieved_gbs": gbs,
+                             "share": tot_ms / max(sum(v[0] for v in stages.values()), 1e-12)}
+    dom = max(stage_info, key=lambda k: stage_info[k]["share"])
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            tr = json.load(f)
+        if dom in tr.get("bytes_per_image", {}):
+            traffic = tr["bytes_per_image"][dom] * stage_info[dom]["images_per_launch"]
+    except Exception:
+        traffic = None
+    roof = {"kernel": dom, "bound": "hbm", "achieved": stage_info[dom]["achieved_gbs"], "peak": hbm_peak,
+            "unit": "GB/s", "frac": stage_info[dom]["achieved_gbs"] / hbm_peak,
+            "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "traffic": traffic,
+            "algorithmic_bytes_per_image": alg[dom]}
+
+    cpu_rate, cpu_times, cpu_threads = cpu_sample_rate(obs, 16, args.cpu_seconds)
+    h2d = vis_np.nbytes
+    d2h = n_images * N * N * 8
+    line = {
+        "metric": METRIC, "value": images_per_s, "unit": "images/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; shapes and distributions of the workload)",
+        "config": {"workload": WORKLOAD, "images_per_step": n_images, "n_pixels": N, "baselines": B,
+                   "wave_images": args.wave or "auto",
+                   "l2": "inputs (673 MB visibilities) and outputs (1.34 GB images) larger than L2 (129 MB)",
+                   "parallelism": "one block per GPU, no collective" if world > 1 else "single GPU"},
+        "vis_per_s": world * gridded_vis * args.steps / (ms / 1000.0),
+        "e2e": {"value": world * n_images / e2e_s, "unit": "images/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "api": "bgi_image_host (pinned host buffers)"},
+        "roofline": roof,
+        "stages": stage_info,
+        "cpu_baseline": {"value": cpu_rate, "unit": "images/s", "cores": cpu_threads, "kind": "port",
+                         "sample": f"16 images (interval 0, channels 0-15) per repetition, "
+                                   f"{len(cpu_times)} repetitions: corrections, gridding, FP32 FFT, "
+                                   "normalise, shift (oracle/ restatement, OpenMP)"},
+        "clocks": clocks.summary(t0, t3),
+        "gpu_launches": sum(v[1] for v in stages.values()),
+        "parity_sample_rel_l2": max(errs),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--wave", type=int, default=0, help="images per launch wave (0 = auto)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

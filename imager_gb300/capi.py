@@ -1,0 +1,98 @@
+"""ctypes binding of the C ABI in include/blink_imager_gb300.h.
+
+The library is built in tree (``python -m imager_gb300.build``) to
+``imager_gb300/_lib/libblink_imager_gb300.so``.  Loading fails loudly when it is missing: there
+is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+from . import build as _build
+
+HEADER = os.path.join(_build.ROOT, "include", "blink_imager_gb300.h")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_STATE = 0, -1, -2, -3, -4, -5
+POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
+COUNTERS_FIRST_INTERVAL, COUNTERS_PER_IMAGE = 0, 1
+APPLY_GEOMETRIC, APPLY_CABLE = 0x1, 0x2
+
+
+class BgiError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("n_pixels", C.c_int), ("oversampling_factor", C.c_float), ("pol", C.c_int),
+                ("min_uv", C.c_double), ("max_images_per_wave", C.c_int), ("device", C.c_int)]
+
+
+_vp, _i, _i64, _d, _f, _u = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_float, C.c_uint
+_SIGNATURES = {
+    "bgi_last_error": (C.c_char_p, []),
+    "bgi_version": (_i, []),
+    "bgi_apply_geometric_corrections_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _vp]),
+    "bgi_apply_cable_lengths_corrections_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp]),
+    "bgi_gridding_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _vp, _d, _d, _i, _d, _i, _i,
+                              _vp, _vp, _vp]),
+    "bgi_fft_inverse_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
+    "bgi_fft_shift_and_norm_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp]),
+    "bgi_vector_sum_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
+    "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
+    "bgi_create": (_i, [C.POINTER(Config), C.POINTER(_vp)]),
+    "bgi_destroy": (_i, [_vp]),
+    "bgi_set_array": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "bgi_set_frequencies": (_i, [_vp, _i, _vp]),
+    "bgi_get_uv_cell": (_i, [_vp, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
+    "bgi_image": (_i, [_vp, _vp, _i, _u, _vp, _vp]),
+    "bgi_image_host": (_i, [_vp, _vp, _i, _u, _vp, _vp]),
+    "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
+    "bgi_set_stage_timing": (_i, [_vp, _i]),
+    "bgi_get_stage_times": (_i, [_vp, C.POINTER(_d), C.POINTER(_i64)]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def lib(build_if_missing: bool = False):
+    """The loaded C library.  Raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise RuntimeError(f"{path} is missing: run `python -m imager_gb300.build` "
+                                   "(the imaging path has no CPU fallback)")
+            _build.build()
+        L = C.CDLL(path)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def header_functions():
+    """Names of every function the public header declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bgi_\w+)\s*\(", text)))
+
+
+def check(status: int) -> None:
+    if status != OK:
+        msg = lib().bgi_last_error()
+        raise BgiError(status, msg.decode() if msg else "")
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))

@@ -1,0 +1,505 @@
+// C ABI of the BLINK GB300 imaging path (include/blink_imager_gb300.h).
+//
+// Free functions mirror the reference's GPU entry points (src/gpu/*.h) on device pointers.
+// The imager handle mirrors CPacerImagerHip's resident members (src/gpu/pacer_imager_hip.h:14-27)
+// and runs the fused path: per wave of images, one gridding launch (corrections fused), one
+// row-FFT launch (which also re-zeroes the grid scratch) and one column-FFT launch (fftshift
+// and 1/sum(weights) fused into its stores).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bgi_internal.h"
+
+namespace bgi {
+
+static thread_local std::string g_last_error;
+
+int set_error(int status, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return BGI_OK;
+    return set_error(e == cudaErrorMemoryAllocation ? BGI_ERR_ALLOC : BGI_ERR_CUDA, "%s: %s (%s)",
+                     what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what); }
+
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace bgi
+
+using namespace bgi;
+
+#define BGI_TRY(expr)              \
+    do {                           \
+        int _st = (expr);          \
+        if (_st != BGI_OK) return _st; \
+    } while (0)
+
+namespace {
+
+cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Visibility records are read and written as 16-byte vectors.
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+long long baselines_of(int n_ant) { return (long long)n_ant * (n_ant + 1) / 2; }
+
+template <class T>
+int dev_alloc(T **p, size_t count, const char *what) {
+    *p = nullptr;
+    if (count == 0) return BGI_OK;
+    return check_cuda(cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count), what);
+}
+
+template <class T>
+void dev_free(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// grow-only device buffer
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t cap = 0;
+    int ensure(size_t count, const char *what, bool *fresh = nullptr) {
+        if (fresh) *fresh = false;
+        if (count <= cap) return BGI_OK;
+        dev_free(ptr);
+        cap = 0;
+        BGI_TRY(dev_alloc(&ptr, count, what));
+        cap = count;
+        if (fresh) *fresh = true;
+        return BGI_OK;
+    }
+    void release() {
+        dev_free(ptr);
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct bgi_imager {
+    bgi_config cfg{};
+    int n_ant = 0, n_uvw_sets = 0, n_channels = 0;
+    long long n_baselines = 0;
+    double u_max = 0, v_max = 0, delta_u = 0, delta_v = 0;
+    float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
+    double *d_dl = nullptr;
+    int *d_flags = nullptr;
+    double *d_freqs = nullptr;
+    DevBuf<float2> grid;          // wave scratch: images x N*N
+    DevBuf<unsigned int> wsum;    // per-image weight counts of the last call
+    DevBuf<float> io_vis, io_img; // device staging of bgi_image_host
+    bool grid_dirty = false;
+    int last_images = 0;
+    // stage timing: event quads (before gridding, after gridding, after rows, after cols)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+
+    int next_event(cudaEvent_t *e) {
+        if (ev_used == ev_pool.size()) {
+            cudaEvent_t ne;
+            BGI_TRY(check_cuda(cudaEventCreate(&ne), "stage timing event"));
+            ev_pool.push_back(ne);
+        }
+        *e = ev_pool[ev_used++];
+        return BGI_OK;
+    }
+    int mark(cudaStream_t s) {
+        if (!timing) return BGI_OK;
+        cudaEvent_t e;
+        BGI_TRY(next_event(&e));
+        return check_cuda(cudaEventRecord(e, s), "stage timing record");
+    }
+
+    int activate() const {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (cur != cfg.device) return check_cuda(cudaSetDevice(cfg.device), "cudaSetDevice");
+        return BGI_OK;
+    }
+    void release_array() {
+        dev_free(d_u);
+        dev_free(d_v);
+        dev_free(d_w);
+        dev_free(d_dl);
+        dev_free(d_flags);
+    }
+};
+
+extern "C" {
+
+const char *bgi_last_error(void) { return g_last_error.c_str(); }
+
+int bgi_version(void) { return 100 * BGI_VERSION_MAJOR + BGI_VERSION_MINOR; }
+
+// ------------------------------------------------------------------------------------------
+// Free functions
+// ------------------------------------------------------------------------------------------
+int bgi_apply_geometric_corrections_gpu(float *vis, int n_ant, int n_channels, int n_intervals,
+                                        const float *w, int n_uvw_sets, const double *freqs_hz,
+                                        void *stream) {
+    if (!vis || !w || !freqs_hz || n_ant < 1 || n_channels < 1 || n_intervals < 0)
+        return set_error(BGI_ERR_INVALID, "apply_geometric_corrections: bad arguments");
+    if (n_uvw_sets != 1 && n_uvw_sets != n_intervals)
+        return set_error(BGI_ERR_INVALID, "apply_geometric_corrections: n_uvw_sets must be 1 or n_intervals");
+    if (!aligned16(vis)) return set_error(BGI_ERR_INVALID, "apply_geometric_corrections: vis must be 16-byte aligned");
+    return launch_geometric(vis, n_ant, n_channels, n_intervals, w, n_uvw_sets, freqs_hz,
+                            as_stream(stream));
+}
+
+int bgi_apply_cable_lengths_corrections_gpu(float *vis, int n_ant, int n_channels,
+                                            int n_intervals, const double *cable_lengths,
+                                            const double *freqs_hz, void *stream) {
+    if (!vis || !cable_lengths || !freqs_hz || n_ant < 1 || n_channels < 1 || n_intervals < 0)
+        return set_error(BGI_ERR_INVALID, "apply_cable_lengths_corrections: bad arguments");
+    if (!aligned16(vis)) return set_error(BGI_ERR_INVALID, "apply_cable_lengths_corrections: vis must be 16-byte aligned");
+    return launch_cable(vis, n_ant, n_channels, n_intervals, cable_lengths, freqs_hz,
+                        as_stream(stream));
+}
+
+int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
+                     const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                     const float *antenna_weights, const double *freqs_hz, double delta_u,
+                     double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
+                     float *counters, float *grids, void *stream) {
+    (void)antenna_weights;
+    if (!vis || !u || !v || !baseline_flags || !freqs_hz || !grids || n_ant < 1 ||
+        n_channels < 1 || n_intervals < 0 || n_pixels < 1 || n_pixels > 46340)
+        return set_error(BGI_ERR_INVALID, "gridding: bad arguments");
+    if (pol < BGI_POL_XX || pol > BGI_POL_V) return set_error(BGI_ERR_INVALID, "gridding: bad pol %d", pol);
+    if (n_uvw_sets != 1 && n_uvw_sets != n_intervals)
+        return set_error(BGI_ERR_INVALID, "gridding: n_uvw_sets must be 1 or n_intervals");
+    if (counters && counter_mode != BGI_COUNTERS_FIRST_INTERVAL && counter_mode != BGI_COUNTERS_PER_IMAGE)
+        return set_error(BGI_ERR_INVALID, "gridding: bad counter_mode %d", counter_mode);
+    if (!(delta_u > 0) || !(delta_v > 0)) return set_error(BGI_ERR_INVALID, "gridding: delta_u/v must be > 0");
+    if (!aligned16(vis)) return set_error(BGI_ERR_INVALID, "gridding: vis must be 16-byte aligned");
+    if ((reinterpret_cast<uintptr_t>(grids) & 7u) != 0) return set_error(BGI_ERR_INVALID, "gridding: grids must be 8-byte aligned");
+    GridParams p{};
+    p.vis = vis;
+    p.u = u;
+    p.v = v;
+    p.flags = baseline_flags;
+    p.freqs = freqs_hz;
+    p.grids = reinterpret_cast<float2 *>(grids);
+    p.counters = counters;
+    p.du = delta_u;
+    p.dv = delta_v;
+    p.min_uv = min_uv;
+    p.n_baselines = baselines_of(n_ant);
+    p.n_channels = n_channels;
+    p.n_intervals = n_intervals;
+    p.n_uvw_sets = n_uvw_sets;
+    p.n_pixels = n_pixels;
+    p.pol = pol;
+    p.img_begin = 0;
+    p.img_count = n_channels * n_intervals;
+    p.img_base = 0;
+    p.counter_mode = counters ? counter_mode : -1;
+    return launch_gridding(p, as_stream(stream));
+}
+
+int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_images,
+                        void *stream) {
+    if (!grids || !images || n_images < 0) return set_error(BGI_ERR_INVALID, "fft_inverse: bad arguments");
+    if (!fft_size_supported(n_pixels))
+        return set_error(BGI_ERR_UNSUPPORTED, "fft_inverse: image side %d (powers of two 16..4096)", n_pixels);
+    if ((const void *)grids == (const void *)images)
+        return set_error(BGI_ERR_INVALID, "fft_inverse: out of place only (grids != images)");
+    cudaStream_t s = as_stream(stream);
+    BGI_TRY(launch_fft_rows(reinterpret_cast<const float2 *>(grids), reinterpret_cast<float2 *>(images),
+                            n_pixels, n_images, false, s));
+    return launch_fft_cols(reinterpret_cast<float2 *>(images), n_pixels, n_images, nullptr, s);
+}
+
+int bgi_fft_shift_and_norm_gpu(float *images, int x_side, int y_side, int n_images,
+                               const float *fnorm, int fnorm_size, void *stream) {
+    if (x_side % 2 != 0)  // src/gpu/gpu_utils.cpp:129-131
+        return set_error(BGI_ERR_INVALID, "fft_shift_and_norm: only even image size is handled");
+    if (!images || !fnorm || fnorm_size < 1 || x_side < 0 || y_side < 0 || n_images < 0)
+        return set_error(BGI_ERR_INVALID, "fft_shift_and_norm: bad arguments");
+    return launch_shift_and_norm(reinterpret_cast<float2 *>(images), x_side, y_side, n_images, fnorm,
+                                 fnorm_size, as_stream(stream));
+}
+
+int bgi_vector_sum_gpu(const float *data, int64_t image_size, int n_images, float *sums,
+                       void *stream) {
+    if (!data || !sums || image_size < 0 || n_images < 0)
+        return set_error(BGI_ERR_INVALID, "vector_sum: bad arguments");
+    return launch_vector_sum(data, image_size, n_images, sums, as_stream(stream));
+}
+
+int bgi_image_averaging_gpu(const float *images, int64_t image_size, int n_images, float *out,
+                            void *stream) {
+    if (!images || !out || image_size < 0 || n_images < 1)
+        return set_error(BGI_ERR_INVALID, "image_averaging: bad arguments");
+    return launch_image_average(reinterpret_cast<const float2 *>(images), image_size, n_images,
+                                reinterpret_cast<float2 *>(out), as_stream(stream));
+}
+
+// ------------------------------------------------------------------------------------------
+// Imager handle
+// ------------------------------------------------------------------------------------------
+int bgi_create(const bgi_config *cfg, bgi_imager **out) {
+    if (!cfg || !out) return set_error(BGI_ERR_INVALID, "create: null argument");
+    *out = nullptr;
+    if (!fft_size_supported(cfg->n_pixels))
+        return set_error(BGI_ERR_UNSUPPORTED, "create: image side %d (powers of two 16..4096)", cfg->n_pixels);
+    if (!(cfg->oversampling_factor > 0.0f)) return set_error(BGI_ERR_INVALID, "create: oversampling_factor must be > 0");
+    if (cfg->pol < BGI_POL_XX || cfg->pol > BGI_POL_V) return set_error(BGI_ERR_INVALID, "create: bad pol %d", cfg->pol);
+    if (cfg->max_images_per_wave < 0) return set_error(BGI_ERR_INVALID, "create: max_images_per_wave < 0");
+    int n_dev = 0;
+    BGI_TRY(check_cuda(cudaGetDeviceCount(&n_dev), "cudaGetDeviceCount"));
+    if (cfg->device < 0 || cfg->device >= n_dev) return set_error(BGI_ERR_INVALID, "create: no device %d", cfg->device);
+    bgi_imager *im = new (std::nothrow) bgi_imager();
+    if (!im) return set_error(BGI_ERR_ALLOC, "create: out of host memory");
+    im->cfg = *cfg;
+    *out = im;
+    return BGI_OK;
+}
+
+int bgi_destroy(bgi_imager *im) {
+    if (!im) return BGI_OK;
+    im->activate();
+    im->release_array();
+    dev_free(im->d_freqs);
+    for (cudaEvent_t e : im->ev_pool) cudaEventDestroy(e);
+    im->grid.release();
+    im->wsum.release();
+    im->io_vis.release();
+    im->io_img.release();
+    delete im;
+    return BGI_OK;
+}
+
+int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, const float *v,
+                  const float *w, const int *baseline_flags, const double *cable_lengths) {
+    if (!im || !u || !v || !baseline_flags || n_ant < 1 || n_uvw_sets < 1)
+        return set_error(BGI_ERR_INVALID, "set_array: bad arguments");
+    BGI_TRY(im->activate());
+    const long long nb = baselines_of(n_ant);
+    const size_t nuv = (size_t)nb * n_uvw_sets;
+    // u_max, v_max over unflagged baselines (src/pacer_imager.cpp:213-221), every set
+    double um = -std::numeric_limits<double>::infinity(), vm = um;
+    for (int s = 0; s < n_uvw_sets; ++s)
+        for (long long b = 0; b < nb; ++b)
+            if (baseline_flags[b] == 0) {
+                um = std::max(um, (double)std::fabs(u[s * nb + b]));
+                vm = std::max(vm, (double)std::fabs(v[s * nb + b]));
+            }
+    std::vector<double> dl(nb, 0.0);
+    if (cable_lengths) {
+        for (int a1 = 0; a1 < n_ant; ++a1)
+            for (int a2 = 0; a2 <= a1; ++a2)
+                dl[(size_t)a1 * (a1 + 1) / 2 + a2] = cable_lengths[a2] - cable_lengths[a1];
+    }
+    im->release_array();
+    BGI_TRY(dev_alloc(&im->d_u, nuv, "set_array u"));
+    BGI_TRY(dev_alloc(&im->d_v, nuv, "set_array v"));
+    BGI_TRY(dev_alloc(&im->d_w, nuv, "set_array w"));
+    BGI_TRY(dev_alloc(&im->d_dl, (size_t)nb, "set_array dl"));
+    BGI_TRY(dev_alloc(&im->d_flags, (size_t)nb, "set_array flags"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->d_u, u, sizeof(float) * nuv, cudaMemcpyHostToDevice), "set_array copy"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->d_v, v, sizeof(float) * nuv, cudaMemcpyHostToDevice), "set_array copy"));
+    if (w) BGI_TRY(check_cuda(cudaMemcpy(im->d_w, w, sizeof(float) * nuv, cudaMemcpyHostToDevice), "set_array copy"));
+    else BGI_TRY(check_cuda(cudaMemset(im->d_w, 0, sizeof(float) * nuv), "set_array memset"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->d_dl, dl.data(), sizeof(double) * nb, cudaMemcpyHostToDevice), "set_array copy"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->d_flags, baseline_flags, sizeof(int) * nb, cudaMemcpyHostToDevice), "set_array copy"));
+    im->n_ant = n_ant;
+    im->n_baselines = nb;
+    im->n_uvw_sets = n_uvw_sets;
+    im->u_max = um;
+    im->v_max = vm;
+    // src/pacer_imager.cpp:497-499: float oversampling factor promoted to double
+    im->delta_u = (double)im->cfg.oversampling_factor * um / im->cfg.n_pixels;
+    im->delta_v = (double)im->cfg.oversampling_factor * vm / im->cfg.n_pixels;
+    return BGI_OK;
+}
+
+int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz) {
+    if (!im || !freqs_hz || n_channels < 1) return set_error(BGI_ERR_INVALID, "set_frequencies: bad arguments");
+    for (int c = 0; c < n_channels; ++c)
+        if (!(freqs_hz[c] > 0.0) || !std::isfinite(freqs_hz[c]))
+            return set_error(BGI_ERR_INVALID, "set_frequencies: frequency %d is not a positive number", c);
+    BGI_TRY(im->activate());
+    dev_free(im->d_freqs);
+    BGI_TRY(dev_alloc(&im->d_freqs, (size_t)n_channels, "set_frequencies"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->d_freqs, freqs_hz, sizeof(double) * n_channels, cudaMemcpyHostToDevice),
+                       "set_frequencies copy"));
+    im->n_channels = n_channels;
+    return BGI_OK;
+}
+
+int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
+                    double *v_max) {
+    if (!im) return set_error(BGI_ERR_INVALID, "get_uv_cell: null handle");
+    if (im->n_ant == 0) return set_error(BGI_ERR_STATE, "get_uv_cell: array not set");
+    if (delta_u) *delta_u = im->delta_u;
+    if (delta_v) *delta_v = im->delta_v;
+    if (u_max) *u_max = im->u_max;
+    if (v_max) *v_max = im->v_max;
+    return BGI_OK;
+}
+
+static int image_checks(bgi_imager *im, int n_intervals, unsigned flags) {
+    if (!im) return set_error(BGI_ERR_INVALID, "image: null handle");
+    if (im->n_ant == 0 || im->n_channels == 0)
+        return set_error(BGI_ERR_STATE, "image: set_array and set_frequencies first");
+    if (n_intervals < 1) return set_error(BGI_ERR_INVALID, "image: n_intervals must be >= 1");
+    if (im->n_uvw_sets != 1 && im->n_uvw_sets != n_intervals)
+        return set_error(BGI_ERR_INVALID, "image: array has %d UVW sets for %d intervals", im->n_uvw_sets, n_intervals);
+    if (flags & ~(BGI_APPLY_GEOMETRIC | BGI_APPLY_CABLE)) return set_error(BGI_ERR_INVALID, "image: unknown flags");
+    if (!(im->delta_u > 0) || !(im->delta_v > 0))
+        return set_error(BGI_ERR_STATE, "image: u_max/v_max is zero (no unflagged baseline?)");
+    return BGI_OK;
+}
+
+int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
+              void *stream) {
+    BGI_TRY(image_checks(im, n_intervals, flags));
+    if (!vis || !images) return set_error(BGI_ERR_INVALID, "image: null buffer");
+    if (!aligned16(vis) || (reinterpret_cast<uintptr_t>(images) & 7u) != 0)
+        return set_error(BGI_ERR_INVALID, "image: vis must be 16-byte and images 8-byte aligned");
+    BGI_TRY(im->activate());
+    cudaStream_t s = as_stream(stream);
+    const int n = im->cfg.n_pixels;
+    const size_t npix = (size_t)n * n;
+    const int n_images = n_intervals * im->n_channels;
+    int wave = im->cfg.max_images_per_wave;
+    if (wave == 0) {
+        const size_t budget = (size_t)256 << 20;  // grid scratch bytes per wave
+        wave = (int)std::max<size_t>(1, budget / (npix * sizeof(float2)));
+    }
+    wave = std::min(wave, n_images);
+    bool fresh = false;
+    BGI_TRY(im->grid.ensure((size_t)wave * npix, "grid scratch", &fresh));
+    if (fresh || im->grid_dirty) {
+        BGI_TRY(check_cuda(cudaMemsetAsync(im->grid.ptr, 0, sizeof(float2) * im->grid.cap, s), "grid scratch clear"));
+        im->grid_dirty = false;
+    }
+    BGI_TRY(im->wsum.ensure((size_t)n_images, "weight sums"));
+    BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * n_images, s), "weight sums clear"));
+
+    GridParams p{};
+    p.vis = vis;
+    p.u = im->d_u;
+    p.v = im->d_v;
+    p.w = im->d_w;
+    p.dl = im->d_dl;
+    p.flags = im->d_flags;
+    p.freqs = im->d_freqs;
+    p.grids = im->grid.ptr;
+    p.du = im->delta_u;
+    p.dv = im->delta_v;
+    p.min_uv = im->cfg.min_uv;
+    p.n_baselines = im->n_baselines;
+    p.n_channels = im->n_channels;
+    p.n_intervals = n_intervals;
+    p.n_uvw_sets = im->n_uvw_sets;
+    p.n_pixels = n;
+    p.pol = im->cfg.pol;
+    p.counter_mode = -1;
+    p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
+    p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
+    float2 *out = reinterpret_cast<float2 *>(images);
+    for (int img0 = 0; img0 < n_images; img0 += wave) {
+        const int cnt = std::min(wave, n_images - img0);
+        p.img_begin = img0;
+        p.img_count = cnt;
+        p.img_base = img0;
+        p.wsum = im->wsum.ptr + img0;  // indexed img - img_base
+        im->grid_dirty = true;
+        BGI_TRY(im->mark(s));
+        BGI_TRY(launch_gridding(p, s));
+        BGI_TRY(im->mark(s));
+        BGI_TRY(launch_fft_rows(im->grid.ptr, out + (size_t)img0 * npix, n, cnt, true, s));
+        im->grid_dirty = false;
+        BGI_TRY(im->mark(s));
+        BGI_TRY(launch_fft_cols(out + (size_t)img0 * npix, n, cnt, im->wsum.ptr + img0, s));
+        BGI_TRY(im->mark(s));
+    }
+    im->last_images = n_images;
+    return BGI_OK;
+}
+
+int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsigned flags,
+                   float *images_host, void *stream) {
+    BGI_TRY(image_checks(im, n_intervals, flags));
+    if (!vis_host || !images_host) return set_error(BGI_ERR_INVALID, "image_host: null buffer");
+    BGI_TRY(im->activate());
+    cudaStream_t s = as_stream(stream);
+    const size_t n_images = (size_t)n_intervals * im->n_channels;
+    const size_t vis_floats = n_images * (size_t)im->n_baselines * 8;
+    const size_t img_floats = n_images * (size_t)im->cfg.n_pixels * im->cfg.n_pixels * 2;
+    BGI_TRY(im->io_vis.ensure(vis_floats, "image_host vis staging"));
+    BGI_TRY(im->io_img.ensure(img_floats, "image_host image staging"));
+    BGI_TRY(check_cuda(cudaMemcpyAsync(im->io_vis.ptr, vis_host, sizeof(float) * vis_floats,
+                                       cudaMemcpyHostToDevice, s), "image_host H2D"));
+    BGI_TRY(bgi_image(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, stream));
+    BGI_TRY(check_cuda(cudaMemcpyAsync(images_host, im->io_img.ptr, sizeof(float) * img_floats,
+                                       cudaMemcpyDeviceToHost, s), "image_host D2H"));
+    return check_cuda(cudaStreamSynchronize(s), "image_host sync");
+}
+
+int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream) {
+    if (!im || !sums_host || n_images < 0) return set_error(BGI_ERR_INVALID, "last_weight_sums: bad arguments");
+    if (n_images > im->last_images) return set_error(BGI_ERR_INVALID, "last_weight_sums: last call had %d images", im->last_images);
+    BGI_TRY(im->activate());
+    cudaStream_t s = as_stream(stream);
+    BGI_TRY(check_cuda(cudaMemcpyAsync(sums_host, im->wsum.ptr, sizeof(uint32_t) * n_images,
+                                       cudaMemcpyDeviceToHost, s), "last_weight_sums copy"));
+    return check_cuda(cudaStreamSynchronize(s), "last_weight_sums sync");
+}
+
+int bgi_set_stage_timing(bgi_imager *im, int enable) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_stage_timing: null handle");
+    im->timing = enable != 0;
+    im->ev_used = 0;
+    return BGI_OK;
+}
+
+int bgi_get_stage_times(bgi_imager *im, double ms[3], int64_t launches[3]) {
+    if (!im || !ms || !launches) return set_error(BGI_ERR_INVALID, "get_stage_times: bad arguments");
+    BGI_TRY(im->activate());
+    for (int k = 0; k < 3; ++k) {
+        ms[k] = 0.0;
+        launches[k] = 0;
+    }
+    for (size_t q = 0; q + 3 < im->ev_used; q += 4) {
+        BGI_TRY(check_cuda(cudaEventSynchronize(im->ev_pool[q + 3]), "stage timing sync"));
+        for (int k = 0; k < 3; ++k) {
+            float t = 0.f;
+            BGI_TRY(check_cuda(cudaEventElapsedTime(&t, im->ev_pool[q + k], im->ev_pool[q + k + 1]),
+                               "stage timing elapsed"));
+            ms[k] += t;
+            launches[k] += 1;
+        }
+    }
+    im->ev_used = 0;
+    return BGI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// Shared device helpers of the BLINK GB300 imaging kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "blink_imager_gb300.h"
+
+namespace bgi {
+
+constexpr double kVelLight = 299792458.0;  // src/pacer_imager_defs.h:12-13
+constexpr float kMaxVis = 1e12f;           // src/pacer_imager_defs.h:21 (1e12 is exact in float)
+
+// ------------------------------------------------------------------------------------------
+// Host-side error reporting (thread-local message, status codes of blink_imager_gb300.h)
+// ------------------------------------------------------------------------------------------
+int set_error(int status, const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+int check_launch(const char *what);
+
+// Per-channel constants for gridding.
+struct ChannelConst {
+    double wavelength;  // VEL_LIGHT / nu, as src/gpu/gridding_gpu.cpp:102
+    double turns_per_m; // nu / VEL_LIGHT (delay in metres -> turns of phase)
+    float su, sv;       // nu / (VEL_LIGHT * delta_u), ... rounded to float (fast cell filter)
+    float inv_wl;       // 1 / wavelength rounded to float (fast min_uv filter)
+    float pad;
+};
+
+// ------------------------------------------------------------------------------------------
+// uv cell index, bit-exact with calculate_pos (src/gpu/gridding_gpu.cpp:18-54).
+//
+// The reference computes in FP64: ul = u/lambda; dist = sqrt(ul^2 + vl^2) (no fused
+// multiply-add, as its x86-64 CPU build); cut unless dist > min_uv; pix = round(ul/delta_u)
+// (half away from zero); wrap(+-pix) = i >= 0 ? i % N : N + i; pos = N*v_idx + u_idx.
+//
+// FP64 is slow on this GPU, so the pixel coordinate is first computed in FP32 as
+// x = u * su with su = nu/(c*delta_u) rounded to float.  Its relative error against the exact
+// real value is below 2^-23 (one rounding of su, one of the product) and the FP64 value's is
+// below 2^-51, so |x - x64| <= |x| * 2^-21 with a 4x margin.  round(x64) == round(x) whenever
+// x is farther than that from a half-integer; otherwise (about 1e-4 of visibilities near the
+// grid edge) the exact FP64 recipe runs.  This is the filtered-arithmetic scheme of
+// Shewchuk's adaptive predicates: a cheap approximation with a proven error bound, and the
+// exact computation only where the bound cannot decide.  The min_uv cut uses the same scheme.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int wrap_index(int i, int side) { return i >= 0 ? i % side : side + i; }
+
+// Exact FP64 path (no contraction: explicit _rn intrinsics).
+__device__ __forceinline__ bool uv_pixels_exact(float u, float v, double wavelength, double du,
+                                                double dv, double min_uv, double *up, double *vp) {
+    double ul = __ddiv_rn((double)u, wavelength);
+    double vl = __ddiv_rn((double)v, wavelength);
+    double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(ul, ul), __dmul_rn(vl, vl)));
+    if (!(dist > min_uv)) return false;
+    *up = round(__ddiv_rn(ul, du));
+    *vp = round(__ddiv_rn(vl, dv));
+    return true;
+}
+
+// True when x (FP32 estimate of a value whose exact counterpart lies within x*2^-21) rounds
+// to the same integer as the exact value.
+__device__ __forceinline__ bool round_is_certain(float x) {
+    float ax = fabsf(x);
+    float d = fabsf(ax - floorf(ax) - 0.5f);
+    float tol = ax * 4.76837158e-7f + 1e-30f;  // 2^-21
+    return d > tol && ax < 536870912.0f;       // and |x| < 2^29
+}
+
+// Returns false when the visibility is cut by min_uv (calculate_pos would return -1);
+// otherwise the rounded pixel coordinates (exact integers) in *ui, *vi.
+__device__ __forceinline__ bool uv_pixels(float u, float v, const ChannelConst &cc, double du,
+                                          double dv, double min_uv, bool min_uv_active, int *ui,
+                                          int *vi) {
+    bool need_exact = false;
+    if (min_uv_active) {
+        // d32 and (float)min_uv each lie within 2^-22 (relative) of their exact values
+        float d32 = sqrtf(u * u + v * v) * cc.inv_wl;
+        float md = (float)min_uv;
+        float tol = (fabsf(d32) + fabsf(md)) * 9.5367431640625e-7f + 1e-30f;  // 2^-20
+        if (!(fabsf(d32 - md) > tol)) {
+            need_exact = true;
+        } else if (!(d32 > md)) {
+            return false;
+        }
+    }
+    float xu = u * cc.su, xv = v * cc.sv;
+    if (!need_exact && round_is_certain(xu) && round_is_certain(xv)) {
+        *ui = (int)roundf(xu);
+        *vi = (int)roundf(xv);
+        return true;
+    }
+    double up, vp;
+    if (!uv_pixels_exact(u, v, cc.wavelength, du, dv, min_uv, &up, &vp)) return false;
+    if (!(fabs(up) < 1073741824.0) || !(fabs(vp) < 1073741824.0)) return false;
+    *ui = (int)up;
+    *vi = (int)vp;
+    return true;
+}
+
+// pos of calculate_pos for uv_sign = +1 / -1, or -1 when outside [0, N*N).
+__device__ __forceinline__ long long cell_pos(int ui, int vi, int sign, int n) {
+    long long pos = (long long)n * wrap_index(sign * vi, n) + wrap_index(sign * ui, n);
+    return (pos >= 0 && pos < (long long)n * n) ? pos : -1;
+}
+
+// ------------------------------------------------------------------------------------------
+// Polarisation selection (src/gpu/gridding_gpu.cpp:79-98, src/pacer_imager.cpp:301-325).
+// rec points at one 4-pol record: XX(0,1) XY(2,3) YX(4,5) YY(6,7).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 select_pol(const float4 lo, const float4 hi, int pol) {
+    // lo = (XX.re, XX.im, XY.re, XY.im), hi = (YX.re, YX.im, YY.re, YY.im)
+    if (pol == BGI_POL_XX) return make_float2(lo.x, lo.y);
+    if (pol == BGI_POL_YY) return make_float2(hi.z, hi.w);
+    if (pol == BGI_POL_V) {
+        // (0 + 0.5i) * (XY - YX)
+        float dr = __fsub_rn(lo.z, hi.x), di = __fsub_rn(lo.w, hi.y);
+        return make_float2(__fsub_rn(__fmul_rn(0.0f, dr), __fmul_rn(0.5f, di)),
+                           __fadd_rn(__fmul_rn(0.0f, di), __fmul_rn(0.5f, dr)));
+    }
+    return make_float2(__fdiv_rn(__fadd_rn(lo.x, hi.z), 2.0f), __fdiv_rn(__fadd_rn(lo.y, hi.w), 2.0f));
+}
+
+// ------------------------------------------------------------------------------------------
+// Delay phase: turns = delay_m * nu/c reduced to [-0.5, 0.5] in FP64 (the one step that needs
+// FP64: delays of km times nu/c reach 10^4 turns), then sin/cos of 2*pi*turns in FP32.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 phasor(double delay_m, double turns_per_m) {
+    double t = delay_m * turns_per_m;
+    double r = t - rint(t);
+    float s, c;
+    sincospif(2.0f * (float)r, &s, &c);
+    return make_float2(c, s);
+}
+
+__device__ __forceinline__ float2 rotate(float2 z, float2 p) {
+    // re' = re*cos - im*sin ; im' = im*cos + re*sin  (src/corrections.cpp:29-30)
+    return make_float2(z.x * p.x - z.y * p.y, z.y * p.x + z.x * p.y);
+}
+
+// Streaming 16-byte load (cache-streaming: the data is read once).  Needs 16-byte alignment,
+// which the host entry points check.
+__device__ __forceinline__ float4 ld_stream_f4(const float4 *p) { return __ldcs(p); }
+
+}  // namespace bgi

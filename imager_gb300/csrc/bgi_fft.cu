@@ -1,0 +1,453 @@
+// Batched inverse 2D FFT of our own (replaces gpufftExecC2C(..., BACKWARD) of
+// src/gpu/pacer_imager_hip.cpp:83-99) and the image epilogues of src/gpu/gpu_utils.cpp.
+//
+// The 2D transform is a row pass followed by a column pass.  Each 1D transform of length N
+// (power of two) is a Stockham autosort FFT (Govindaraju et al., "High Performance Discrete
+// Fourier Transforms on Graphics Processors", SC'08): P = N/R threads each hold R values in
+// registers, every pass applies inter-pass twiddles and an in-register radix-R DFT, and passes
+// exchange data through shared memory.  The first pass reads x[t + m*P] and the last pass
+// writes x[t + m*P'] -- consecutive threads touch consecutive elements -- so both HBM-facing
+// passes are coalesced and no separate transpose kernel exists.  Twiddles exp(+2*pi*i*k/N)
+// come from sincospif into shared memory once per block.
+//
+//   row pass:    grids -> images rows; in the fused path it also re-zeroes the grid scratch
+//                it has read, so the next wave's gridding finds a clean grid.
+//   column pass: in place on images; a block owns the column tile at x and its fftshift
+//                partner at x + N/2, so shifted stores never race with another block's loads.
+//                In the fused path the stores apply the fftshift and the 1/sum(weights)
+//                normalisation (src/pacer_imager.cpp:171-179).
+#include "bgi_internal.h"
+
+namespace bgi {
+namespace {
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+__host__ __device__ constexpr int bitrev(int i, int bits) {
+    return bits == 0 ? 0 : ((i & 1) << (bits - 1)) | bitrev(i >> 1, bits - 1);
+}
+
+// cos / sin of 2*pi*j/16
+constexpr float kC1 = 0.923879532511286756f;  // cos(pi/8)
+constexpr float kC2 = 0.707106781186547524f;  // cos(pi/4)
+constexpr float kC3 = 0.382683432365089772f;  // cos(3pi/8)
+__host__ __device__ constexpr float cos16(int j) {
+    return j == 0 ? 1.f : j == 1 ? kC1 : j == 2 ? kC2 : j == 3 ? kC3 : j == 4 ? 0.f
+         : j == 5 ? -kC3 : j == 6 ? -kC2 : j == 7 ? -kC1 : j == 8 ? -1.f : j == 9 ? -kC1
+         : j == 10 ? -kC2 : j == 11 ? -kC3 : j == 12 ? 0.f : j == 13 ? kC3 : j == 14 ? kC2 : kC1;
+}
+__host__ __device__ constexpr float sin16(int j) { return cos16((j + 12) & 15); }
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 w) {
+    return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+}
+
+// a * exp(+2*pi*i*j/16) with compile-time j
+template <int J>
+__device__ __forceinline__ float2 twiddle16(float2 a) {
+    constexpr int j = J & 15;
+    if (j == 0) return a;
+    if (j == 4) return make_float2(-a.y, a.x);
+    if (j == 8) return make_float2(-a.x, -a.y);
+    if (j == 12) return make_float2(a.y, -a.x);
+    return cmul(a, make_float2(cos16(j), sin16(j)));
+}
+
+// Butterflies of one radix-2 DIT stage of length LEN on the bit-reversed register array.
+template <int R, int LEN, int K, bool END = (K == LEN / 2)>
+struct StageLoop {
+    __device__ __forceinline__ static void run(float2 *a, int s) {
+        float2 u = a[s + K], v = twiddle16<K * (16 / LEN)>(a[s + K + LEN / 2]);
+        a[s + K] = make_float2(u.x + v.x, u.y + v.y);
+        a[s + K + LEN / 2] = make_float2(u.x - v.x, u.y - v.y);
+        StageLoop<R, LEN, K + 1>::run(a, s);
+    }
+};
+template <int R, int LEN, int K>
+struct StageLoop<R, LEN, K, true> {
+    __device__ __forceinline__ static void run(float2 *, int) {}
+};
+
+template <int R, int LEN, int S, bool END = (S >= R)>
+struct Blocks {
+    __device__ __forceinline__ static void run(float2 *a) {
+        StageLoop<R, LEN, 0>::run(a, S);
+        Blocks<R, LEN, S + LEN>::run(a);
+    }
+};
+template <int R, int LEN, int S>
+struct Blocks<R, LEN, S, true> {
+    __device__ __forceinline__ static void run(float2 *) {}
+};
+
+template <int R, int LEN, bool END = (LEN > R)>
+struct Stages {
+    __device__ __forceinline__ static void run(float2 *a) {
+        Blocks<R, LEN, 0>::run(a);
+        Stages<R, LEN * 2>::run(a);
+    }
+};
+template <int R, int LEN>
+struct Stages<R, LEN, true> {
+    __device__ __forceinline__ static void run(float2 *) {}
+};
+
+// Bit-reversal permutation of the register array, unrolled at compile time.
+template <int R, int I, bool END = (I == R)>
+struct BitRevSwap {
+    __device__ __forceinline__ static void run(float2 *a) {
+        constexpr int J = bitrev(I, ilog2(R));
+        if constexpr (I < J) {
+            float2 tmp = a[I];
+            a[I] = a[J];
+            a[J] = tmp;
+        }
+        BitRevSwap<R, I + 1>::run(a);
+    }
+};
+template <int R, int I>
+struct BitRevSwap<R, I, true> {
+    __device__ __forceinline__ static void run(float2 *) {}
+};
+
+// In-register inverse DFT of size R (2..16): A_k = sum_m a_m exp(+2*pi*i*m*k/R).
+template <int R>
+__device__ __forceinline__ void dft(float2 *a) {
+    BitRevSwap<R, 0>::run(a);
+    Stages<R, 2>::run(a);
+}
+
+template <int N, int R>
+struct FftCfg {
+    static constexpr int P = N / R;  // threads per transform
+    static constexpr int LOGN = ilog2(N), LOGR = ilog2(R);
+    static constexpr int NFULL = LOGN / LOGR;  // radix-R passes
+    static constexpr int R2 = 1 << (LOGN % LOGR);  // radix of the final pass (1 = none)
+    static constexpr int NPASS = NFULL + (R2 > 1 ? 1 : 0);
+    static constexpr int PAD = 1;  // float2 padding per transform in shared memory
+    static_assert(NPASS >= 2, "at least two passes (global loads and stores are separated)");
+};
+
+// One 1D inverse transform of length N by P threads (t = 0..P-1).  sm: this transform's N
+// shared elements; tw: N twiddles.  gload(i) reads input element i, gstore(i, v) writes output
+// element i.  Every thread of the block must call this the same way (block barriers).
+template <int N, int R, class GLoad, class GStore>
+__device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *tw, GLoad gload,
+                                              GStore gstore) {
+    using C = FftCfg<N, R>;
+    constexpr int P = C::P;
+    constexpr int R2 = C::R2;
+    float2 a[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) a[m] = gload(t + m * P);
+    int Ns = 1;
+#pragma unroll
+    for (int p = 0; p < C::NFULL; ++p) {
+        const int k = t & (Ns - 1);
+        if (p > 0) {
+            const int step = N / (Ns * R);
+#pragma unroll
+            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw[m * k * step]);
+        }
+        dft<R>(a);
+        const int base = (t - k) * R + k;
+        if (p == C::NPASS - 1) {
+#pragma unroll
+            for (int m = 0; m < R; ++m) gstore(base + m * Ns, a[m]);
+        } else {
+            __syncthreads();
+#pragma unroll
+            for (int m = 0; m < R; ++m) sm[base + m * Ns] = a[m];
+            __syncthreads();
+            if (p + 1 < C::NFULL) {
+#pragma unroll
+                for (int m = 0; m < R; ++m) a[m] = sm[t + m * P];
+            } else {
+#pragma unroll
+                for (int q = 0; q < R / R2; ++q)
+#pragma unroll
+                    for (int m = 0; m < R2; ++m) a[q * R2 + m] = sm[t + q * P + m * (N / R2)];
+            }
+        }
+        Ns *= R;
+    }
+    if constexpr (R2 > 1) {
+#pragma unroll
+        for (int q = 0; q < R / R2; ++q) {
+            const int j = t + q * P;
+            constexpr int RB = R2 > 1 ? R2 : 2;
+            float2 b[RB];
+#pragma unroll
+            for (int m = 0; m < R2; ++m) b[m] = m ? cmul(a[q * R2 + m], tw[m * j]) : a[q * R2];
+            dft<RB>(b);
+#pragma unroll
+            for (int m = 0; m < R2; ++m) gstore(j + m * (N / R2), b[m]);
+        }
+    }
+}
+
+template <int N>
+__device__ __forceinline__ void init_twiddles(float2 *tw) {
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        float s, c;
+        sincospif(2.0f * (float)k / (float)N, &s, &c);
+        tw[k] = make_float2(c, s);
+    }
+}
+
+template <int N, int R, int ROWS, bool ZERO_SRC>
+__global__ void __launch_bounds__(ROWS *(N / R)) fft_rows_kernel(float2 *src, float2 *dst) {
+    using C = FftCfg<N, R>;
+    extern __shared__ float2 smem[];
+    float2 *tw = smem;
+    float2 *buf = smem + N;
+    init_twiddles<N>(tw);
+    __syncthreads();
+    const int r_local = threadIdx.x / C::P, t = threadIdx.x % C::P;
+    const size_t row = (size_t)blockIdx.x * ROWS + r_local;
+    float2 *s_row = src + row * N;
+    float2 *d_row = dst + row * N;
+    fft_transform<N, R>(
+        t, buf + r_local * (N + C::PAD), tw,
+        [&](int i) {
+            float2 v = s_row[i];
+            if (ZERO_SRC) s_row[i] = make_float2(0.f, 0.f);
+            return v;
+        },
+        [&](int i, float2 v) { d_row[i] = v; });
+}
+
+template <int N, int R, int CT, bool SHIFT_NORM>
+__global__ void __launch_bounds__(2 * CT *(N / R)) fft_cols_kernel(float2 *images,
+                                                                    const unsigned int *wsum) {
+    using C = FftCfg<N, R>;
+    constexpr int COLS = 2 * CT;
+    constexpr int TILES = (N / 2) / CT;
+    extern __shared__ float2 smem[];
+    float2 *tw = smem;
+    float2 *buf = smem + N;
+    init_twiddles<N>(tw);
+    __syncthreads();
+    const int c_local = threadIdx.x % COLS, t = threadIdx.x / COLS;
+    const size_t img = blockIdx.x / TILES;
+    const int tile = blockIdx.x % TILES;
+    const int col = c_local < CT ? tile * CT + c_local : N / 2 + tile * CT + (c_local - CT);
+    float2 *im = images + img * (size_t)N * N;
+    float scale = 1.0f;
+    if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img]);
+    const int dcol = SHIFT_NORM ? ((col + N / 2) & (N - 1)) : col;
+    fft_transform<N, R>(
+        t, buf + c_local * (N + C::PAD), tw,
+        [&](int i) { return im[(size_t)i * N + col]; },
+        [&](int i, float2 v) {
+            int r = i;
+            if (SHIFT_NORM) {
+                r = (i + N / 2) & (N - 1);
+                v = make_float2(v.x * scale, v.y * scale);
+            }
+            im[(size_t)r * N + dcol] = v;
+        });
+}
+
+// Per-size launch shapes: radix, rows per row-pass block, column tile width.
+struct Shape {
+    int r, rows, ct;
+};
+constexpr Shape shape_for(int n) {
+    return n <= 128 ? Shape{8, 16, 8}
+         : n == 256 ? Shape{8, 8, 4}
+         : n == 512 ? Shape{8, 4, 4}
+         : n == 1024 ? Shape{16, 4, 4}
+         : n == 2048 ? Shape{16, 2, 2}
+                     : Shape{16, 1, 2};
+}
+
+template <class K>
+int prepare(K kernel, size_t smem) {
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return check_cuda(e, "fft smem attribute");
+    }
+    return BGI_OK;
+}
+
+template <int N>
+int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStream_t s) {
+    constexpr Shape sh = shape_for(N);
+    constexpr int ROWS = sh.rows < N ? sh.rows : N;
+    constexpr int P = N / sh.r;
+    const size_t smem = sizeof(float2) * (N + ROWS * (N + 1));
+    const unsigned blocks = (unsigned)((size_t)n_images * N / ROWS);
+    if (zero_src) {
+        auto k = fft_rows_kernel<N, sh.r, ROWS, true>;
+        int st = prepare(k, smem);
+        if (st) return st;
+        k<<<blocks, ROWS * P, smem, s>>>(const_cast<float2 *>(src), dst);
+    } else {
+        auto k = fft_rows_kernel<N, sh.r, ROWS, false>;
+        int st = prepare(k, smem);
+        if (st) return st;
+        k<<<blocks, ROWS * P, smem, s>>>(const_cast<float2 *>(src), dst);
+    }
+    return check_launch("fft rows");
+}
+
+template <int N>
+int cols_n(float2 *images, int n_images, const unsigned int *wsum, cudaStream_t s) {
+    constexpr Shape sh = shape_for(N);
+    constexpr int CT = sh.ct;
+    constexpr int P = N / sh.r;
+    const size_t smem = sizeof(float2) * (N + 2 * CT * (N + 1));
+    const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / CT);
+    if (wsum) {
+        auto k = fft_cols_kernel<N, sh.r, CT, true>;
+        int st = prepare(k, smem);
+        if (st) return st;
+        k<<<blocks, 2 * CT * P, smem, s>>>(images, wsum);
+    } else {
+        auto k = fft_cols_kernel<N, sh.r, CT, false>;
+        int st = prepare(k, smem);
+        if (st) return st;
+        k<<<blocks, 2 * CT * P, smem, s>>>(images, nullptr);
+    }
+    return check_launch("fft cols");
+}
+
+// ---- src/gpu/gpu_utils.cpp:73-123: fftshift by half swaps, then divide -------------------
+__device__ __forceinline__ int calc_fft_shift(int pos, int side) {
+    return (pos + side / 2 + side % 2) % side;
+}
+
+__global__ void shift_x_kernel(float2 *data, int xs, int ys) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int half = xs / 2;
+    if (tid >= half * ys) return;
+    const int row = tid / half, col = tid % half;
+    float2 *im = data + (size_t)blockIdx.y * xs * ys;
+    const size_t src = (size_t)row * xs + col, dst = (size_t)row * xs + calc_fft_shift(col, xs);
+    float2 tmp = im[dst];
+    im[dst] = im[src];
+    im[src] = tmp;
+}
+
+__global__ void shift_y_norm_kernel(float2 *data, int xs, int ys, const float *fnorm,
+                                    int fnorm_size) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= xs * (ys / 2)) return;
+    const int row = tid / xs, col = tid % xs;
+    const int img = blockIdx.y;
+    float2 *im = data + (size_t)img * xs * ys;
+    const float f = fnorm[img % fnorm_size];
+    const size_t src = (size_t)row * xs + col, dst = (size_t)calc_fft_shift(row, ys) * xs + col;
+    float2 tmp = im[dst], v = im[src];
+    im[dst] = make_float2(__fdiv_rn(v.x, f), __fdiv_rn(v.y, f));
+    im[src] = make_float2(__fdiv_rn(tmp.x, f), __fdiv_rn(tmp.y, f));
+}
+
+// ---- src/gpu/gpu_utils.cpp:19-71: per-image sum (one block per image, FP64 partials) ------
+__global__ void __launch_bounds__(256) vector_sum_kernel(const float *data, int64_t n, float *sums) {
+    __shared__ double part[8];
+    const float *x = data + (size_t)blockIdx.x * n;
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += x[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+        sums[blockIdx.x] = (float)s;
+    }
+}
+
+// ---- src/gpu/gpu_utils.cpp:143-150: mean of the images ------------------------------------
+__global__ void average_kernel(const float2 *images, int64_t n_pix, int n_images, float2 *out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pix) return;
+    float2 acc = images[i];
+    for (int k = 1; k < n_images; ++k) {
+        float2 v = images[(size_t)k * n_pix + i];
+        acc.x += v.x;
+        acc.y += v.y;
+    }
+    out[i] = make_float2(__fdiv_rn(acc.x, (float)n_images), __fdiv_rn(acc.y, (float)n_images));
+}
+
+}  // namespace
+
+bool fft_size_supported(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
+
+int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool zero_src,
+                    cudaStream_t s) {
+    if (n_images <= 0) return BGI_OK;
+    switch (n) {
+        case 16: return rows_n<16>(src, dst, n_images, zero_src, s);
+        case 32: return rows_n<32>(src, dst, n_images, zero_src, s);
+        case 64: return rows_n<64>(src, dst, n_images, zero_src, s);
+        case 128: return rows_n<128>(src, dst, n_images, zero_src, s);
+        case 256: return rows_n<256>(src, dst, n_images, zero_src, s);
+        case 512: return rows_n<512>(src, dst, n_images, zero_src, s);
+        case 1024: return rows_n<1024>(src, dst, n_images, zero_src, s);
+        case 2048: return rows_n<2048>(src, dst, n_images, zero_src, s);
+        case 4096: return rows_n<4096>(src, dst, n_images, zero_src, s);
+        default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
+    }
+}
+
+int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsum,
+                    cudaStream_t s) {
+    if (n_images <= 0) return BGI_OK;
+    switch (n) {
+        case 16: return cols_n<16>(images, n_images, wsum, s);
+        case 32: return cols_n<32>(images, n_images, wsum, s);
+        case 64: return cols_n<64>(images, n_images, wsum, s);
+        case 128: return cols_n<128>(images, n_images, wsum, s);
+        case 256: return cols_n<256>(images, n_images, wsum, s);
+        case 512: return cols_n<512>(images, n_images, wsum, s);
+        case 1024: return cols_n<1024>(images, n_images, wsum, s);
+        case 2048: return cols_n<2048>(images, n_images, wsum, s);
+        case 4096: return cols_n<4096>(images, n_images, wsum, s);
+        default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
+    }
+}
+
+int launch_shift_and_norm(float2 *images, int xs, int ys, int n_images, const float *fnorm,
+                          int fnorm_size, cudaStream_t s) {
+    if (n_images <= 0 || xs <= 0 || ys <= 0) return BGI_OK;
+    for (int done = 0; done < n_images; done += 65535) {
+        const int cnt = n_images - done < 65535 ? n_images - done : 65535;
+        float2 *base = images + (size_t)done * xs * ys;
+        int nx = (xs / 2) * ys;
+        if (nx > 0) {
+            shift_x_kernel<<<dim3((nx + 255) / 256, cnt), 256, 0, s>>>(base, xs, ys);
+            int st = check_launch("fft_shift x");
+            if (st) return st;
+        }
+        int ny = xs * (ys / 2);
+        if (ny > 0) {
+            // fnorm index is img % fnorm_size with img counted from the first image
+            shift_y_norm_kernel<<<dim3((ny + 255) / 256, cnt), 256, 0, s>>>(base, xs, ys, fnorm, fnorm_size);
+            int st = check_launch("fft_shift y");
+            if (st) return st;
+        }
+        if (done + cnt < n_images && fnorm_size > 1 && (65535 % fnorm_size) != 0)
+            return set_error(BGI_ERR_UNSUPPORTED, "more than 65535 images need fnorm_size dividing 65535");
+    }
+    return BGI_OK;
+}
+
+int launch_vector_sum(const float *data, int64_t image_size, int n_images, float *sums,
+                      cudaStream_t s) {
+    if (n_images <= 0) return BGI_OK;
+    vector_sum_kernel<<<n_images, 256, 0, s>>>(data, image_size, sums);
+    return check_launch("vector_sum");
+}
+
+int launch_image_average(const float2 *images, int64_t image_size, int n_images, float2 *out,
+                         cudaStream_t s) {
+    if (n_images <= 0 || image_size <= 0) return BGI_OK;
+    const int64_t blocks = (image_size + 255) / 256;
+    average_kernel<<<(unsigned)blocks, 256, 0, s>>>(images, image_size, n_images, out);
+    return check_launch("image_averaging");
+}
+
+}  // namespace bgi

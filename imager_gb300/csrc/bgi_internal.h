@@ -1,0 +1,57 @@
+// Host-side launchers shared between the kernel files and the C ABI (bgi_capi.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bgi_common.cuh"
+
+namespace bgi {
+
+// ---- corrections (bgi_corrections.cu) ------------------------------------------------------
+// In place on all four pols.  geometric: delay = w[set][b]; cable: delay = -(L[a2]-L[a1]).
+int launch_geometric(float *vis, int n_ant, int n_channels, int n_intervals, const float *w,
+                     int n_uvw_sets, const double *freqs, cudaStream_t s);
+int launch_cable(float *vis, int n_ant, int n_channels, int n_intervals, const double *cable,
+                 const double *freqs, cudaStream_t s);
+
+// ---- gridding (bgi_gridding.cu) ------------------------------------------------------------
+struct GridParams {
+    const float *vis;        // [T][C][B][4][2]
+    const float *u, *v, *w;  // [n_uvw_sets][B]
+    const double *dl;        // [B] L[a2]-L[a1] (cable delay), or null
+    const int *flags;        // [B]
+    const double *freqs;     // [C] Hz
+    float2 *grids;           // images [img - img_base][N*N]
+    float *counters;         // optional counter grids
+    unsigned int *wsum;      // optional per-image weight counts, indexed img - img_base
+    double du, dv, min_uv;
+    long long n_baselines;
+    int n_channels, n_intervals, n_uvw_sets, n_pixels, pol;
+    int img_begin, img_count;  // images [img_begin, img_begin + img_count) of the block
+    int img_base;              // grids/wsum index = img - img_base
+    int counter_mode;          // -1 none, 0 first interval, 1 per image
+    int apply_geom, apply_cable;
+};
+int launch_gridding(const GridParams &p, cudaStream_t s);
+
+// ---- FFT and image epilogues (bgi_fft.cu) --------------------------------------------------
+bool fft_size_supported(int n);
+// Row pass: src rows -> dst rows (inverse DFT along x); zero_src clears src after reading.
+int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool zero_src,
+                    cudaStream_t s);
+// Column pass in place on images; with wsum != null, also fftshift and multiply image i by
+// (float)(1/wsum[i]).
+int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsum,
+                    cudaStream_t s);
+int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
+                          const float *fnorm, int fnorm_size, cudaStream_t s);
+int launch_vector_sum(const float *data, int64_t image_size, int n_images, float *sums,
+                      cudaStream_t s);
+int launch_image_average(const float2 *images, int64_t image_size, int n_images, float2 *out,
+                         cudaStream_t s);
+
+// number of SMs of the current device (cached)
+int sm_count();
+
+}  // namespace bgi

@@ -1,0 +1,196 @@
+"""Python host API over the C ABI, with torch tensors as device memory.
+
+Mirrors the reference imager's GPU entry points (PaCER-BLINK-Project/imager, src/gpu/*.h) and
+its CPacerImagerHip driver (src/gpu/pacer_imager_hip.cpp) for scripting, tests and the
+benchmark.  Every call goes to the CUDA library; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import capi
+from .capi import APPLY_CABLE, APPLY_GEOMETRIC, POL, call
+
+__all__ = ["Imager", "apply_geometric_corrections", "apply_cable_corrections", "gridding",
+           "fft_inverse", "fft_shift_and_norm", "vector_sum", "image_averaging",
+           "APPLY_GEOMETRIC", "APPLY_CABLE", "POL"]
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if isinstance(t, torch.Tensor):
+        if not t.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return C.c_void_p(t.data_ptr())
+    if isinstance(t, np.ndarray):
+        if not t.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return C.c_void_p(t.ctypes.data)
+    raise TypeError(type(t))
+
+
+def _stream(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _n_ant(n_baselines: int) -> int:
+    n = int(round((-1 + math.sqrt(1 + 8 * n_baselines)) / 2))
+    if n * (n + 1) // 2 != n_baselines:
+        raise ValueError(f"{n_baselines} is not a triangular baseline count")
+    return n
+
+
+def _vis_dims(vis: torch.Tensor):
+    """(T, C, B) of a visibility tensor: complex64 [T][C][B][4] or float32 [T][C][B][4][2]."""
+    if vis.dtype == torch.complex64:
+        if vis.dim() != 4 or vis.shape[3] != 4:
+            raise ValueError("complex visibilities must be [T][C][B][4]")
+    elif vis.dtype == torch.float32:
+        if vis.dim() != 5 or vis.shape[3:] != (4, 2):
+            raise ValueError("float visibilities must be [T][C][B][4][2]")
+    else:
+        raise TypeError(vis.dtype)
+    return int(vis.shape[0]), int(vis.shape[1]), int(vis.shape[2])
+
+
+# ----------------------------------------------------------------------------------------------
+# reference GPU entry points
+# ----------------------------------------------------------------------------------------------
+def apply_geometric_corrections(vis, w, freqs, n_uvw_sets=1, stream=None):
+    """apply_geometric_corrections_gpu (src/gpu/corrections_gpu.cpp:90): in place."""
+    T, Cn, B = _vis_dims(vis)
+    call("bgi_apply_geometric_corrections_gpu", _ptr(vis), _n_ant(B), Cn, T, _ptr(w), n_uvw_sets,
+         _ptr(freqs), _stream(stream))
+
+
+def apply_cable_corrections(vis, cable, freqs, stream=None):
+    """apply_cable_lengths_corrections_gpu (src/gpu/corrections_gpu.cpp:75): in place."""
+    T, Cn, B = _vis_dims(vis)
+    call("bgi_apply_cable_lengths_corrections_gpu", _ptr(vis), _n_ant(B), Cn, T, _ptr(cable),
+         _ptr(freqs), _stream(stream))
+
+
+def gridding(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv, pol, grids, counters=None,
+             counter_mode=capi.COUNTERS_PER_IMAGE, n_uvw_sets=1, stream=None):
+    """gridding_gpu (src/gpu/gridding_gpu.cpp:130): accumulates into grids (complex64
+    [T][C][N][N]) and counters."""
+    T, Cn, B = _vis_dims(vis)
+    call("bgi_gridding_gpu", _ptr(vis), _n_ant(B), Cn, T, _ptr(u), _ptr(v), n_uvw_sets, _ptr(flags),
+         None, _ptr(freqs), float(delta_u), float(delta_v), int(n_pixels), float(min_uv),
+         POL[pol] if isinstance(pol, str) else int(pol), int(counter_mode), _ptr(counters),
+         _ptr(grids), _stream(stream))
+
+
+def fft_inverse(grids, images, stream=None):
+    """gpufftExecC2C(..., BACKWARD) replacement: unnormalised inverse 2D FFT, out of place."""
+    n = int(grids.shape[-1])
+    call("bgi_fft_inverse_gpu", _ptr(grids), _ptr(images), n, grids.numel() // (n * n), _stream(stream))
+
+
+def fft_shift_and_norm(images, fnorm, stream=None):
+    """fft_shift_and_norm_gpu (src/gpu/gpu_utils.cpp:128), images complex64 [..., Y, X]."""
+    ys, xs = int(images.shape[-2]), int(images.shape[-1])
+    call("bgi_fft_shift_and_norm_gpu", _ptr(images), xs, ys, images.numel() // (xs * ys), _ptr(fnorm),
+         int(fnorm.numel()), _stream(stream))
+
+
+def vector_sum(data, image_size, n_images, sums, stream=None):
+    call("bgi_vector_sum_gpu", _ptr(data), int(image_size), int(n_images), _ptr(sums), _stream(stream))
+
+
+def image_averaging(images, out, stream=None):
+    n = int(images.shape[0])
+    call("bgi_image_averaging_gpu", _ptr(images), images[0].numel(), n, _ptr(out), _stream(stream))
+
+
+# ----------------------------------------------------------------------------------------------
+# imager handle
+# ----------------------------------------------------------------------------------------------
+class Imager:
+    """Resident-state imager (CPacerImagerHip's members, src/gpu/pacer_imager_hip.h:14-27)."""
+
+    def __init__(self, n_pixels: int, oversampling_factor: float = 2.0, pol="XX",
+                 min_uv: float = -math.inf, max_images_per_wave: int = 0, device: int = 0):
+        cfg = capi.Config(int(n_pixels), float(oversampling_factor),
+                          POL[pol] if isinstance(pol, str) else int(pol), float(min_uv),
+                          int(max_images_per_wave), int(device))
+        h = C.c_void_p()
+        call("bgi_create", C.byref(cfg), C.byref(h))
+        self._h = h
+        self.n_pixels = int(n_pixels)
+        self.device = int(device)
+        self.n_channels = 0
+
+    def close(self):
+        if self._h:
+            capi.lib().bgi_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_array(self, u, v, w, flags, cable):
+        u = np.ascontiguousarray(np.atleast_2d(u), np.float32)
+        v = np.ascontiguousarray(np.atleast_2d(v), np.float32)
+        w = None if w is None else np.ascontiguousarray(np.atleast_2d(w), np.float32)
+        flags = np.ascontiguousarray(flags, np.int32)
+        cable = None if cable is None else np.ascontiguousarray(cable, np.float64)
+        n_ant = _n_ant(u.shape[1])
+        call("bgi_set_array", self._h, n_ant, u.shape[0], _ptr(u), _ptr(v), _ptr(w), _ptr(flags),
+             _ptr(cable))
+
+    def set_frequencies(self, freqs):
+        f = np.ascontiguousarray(freqs, np.float64)
+        call("bgi_set_frequencies", self._h, len(f), _ptr(f))
+        self.n_channels = len(f)
+
+    @property
+    def uv_cell(self):
+        du, dv, um, vm = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        call("bgi_get_uv_cell", self._h, C.byref(du), C.byref(dv), C.byref(um), C.byref(vm))
+        return du.value, dv.value, um.value, vm.value
+
+    def image(self, vis: torch.Tensor, flags: int = APPLY_GEOMETRIC | APPLY_CABLE, out=None,
+              stream=None) -> torch.Tensor:
+        """Dirty images complex64 [T][C][N][N] of device visibilities."""
+        T, Cn, _ = _vis_dims(vis)
+        n = self.n_pixels
+        if out is None:
+            out = torch.empty((T, Cn, n, n), dtype=torch.complex64, device=vis.device)
+        call("bgi_image", self._h, _ptr(vis), T, int(flags), _ptr(out), _stream(stream))
+        return out
+
+    def image_host(self, vis, flags: int = APPLY_GEOMETRIC | APPLY_CABLE, out=None, stream=None):
+        """Host buffers in and out (pinned torch tensors or numpy arrays); synchronous."""
+        T = int(vis.shape[0])
+        Cn = int(vis.shape[1])
+        n = self.n_pixels
+        if out is None:
+            out = np.empty((T, Cn, n, n), np.complex64)
+        call("bgi_image_host", self._h, _ptr(vis), T, int(flags), _ptr(out), _stream(stream))
+        return out
+
+    def set_stage_timing(self, enable: bool = True):
+        call("bgi_set_stage_timing", self._h, int(bool(enable)))
+
+    def stage_times(self):
+        """{stage: (total ms, launches)} since the last read, for gridding, fft_rows, fft_cols."""
+        ms = (C.c_double * 3)()
+        n = (C.c_int64 * 3)()
+        call("bgi_get_stage_times", self._h, ms, n)
+        return {k: (ms[i], int(n[i])) for i, k in enumerate(("gridding", "fft_rows", "fft_cols"))}
+
+    def weight_sums(self, n_images: int, stream=None) -> np.ndarray:
+        out = np.zeros(n_images, np.uint32)
+        call("bgi_last_weight_sums", self._h, _ptr(out), int(n_images), _stream(stream))
+        return out

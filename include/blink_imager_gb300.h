@@ -1,0 +1,182 @@
+/*
+ * blink_imager_gb300 -- C ABI of the GB300-native BLINK dirty-imaging path.
+ *
+ * Replaces the GPU half of PaCER-BLINK-Project/imager: the phase corrections, nearest-
+ * neighbour uv gridding, inverse 2D FFT, fftshift and normalisation that CPacerImagerHip runs
+ * (src/gpu/pacer_imager_hip.cpp:36-146).  Two layers:
+ *
+ *  1. Free functions with the reference's argument meaning, on device pointers, one per
+ *     reference GPU entry point (src/gpu/*.h).  A caller that already holds device buffers
+ *     (the CPacerImagerHip shape) swaps the call and nothing else.
+ *  2. An imager handle that keeps the array state (UVW, flags, cable lengths, frequencies)
+ *     resident on the device and images whole blocks in one call, with the corrections fused
+ *     into gridding and the fftshift / normalisation fused into the FFT (bgi_image).
+ *
+ * Data layout (as the reference, src/gpu/gridding_gpu.cpp:72-76):
+ *   visibilities  float[T][C][B][4 pols][re,im]; pols XX, XY, YX, YY; B = A(A+1)/2;
+ *                 baseline b = a1*(a1+1)/2 + a2 with a1 >= a2
+ *   grids/images  float[T][C][N][N][re,im]      counters float[...][N][N]
+ *   u, v, w       float[n_uvw_sets][B] metres; set t serves interval t when n_uvw_sets == T,
+ *                 set 0 serves every interval when n_uvw_sets == 1 (the reference's case)
+ *
+ * Every function returns BGI_OK (0) or a negative status; bgi_last_error() gives the message
+ * of the calling thread's last failure.  Nothing throws across this interface.  Streams are
+ * cudaStream_t passed as void* (NULL = legacy default stream).  Launches are asynchronous
+ * unless stated otherwise.
+ */
+#ifndef BLINK_IMAGER_GB300_H
+#define BLINK_IMAGER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Exported symbols: the library is built with hidden visibility and exports only these. */
+#if defined(__GNUC__)
+#define BGI_API __attribute__((visibility("default")))
+#else
+#define BGI_API
+#endif
+
+#define BGI_VERSION_MAJOR 0
+#define BGI_VERSION_MINOR 1
+
+enum bgi_status {
+    BGI_OK = 0,
+    BGI_ERR_INVALID = -1,     /* bad argument (size, pointer, enum) */
+    BGI_ERR_CUDA = -2,        /* a CUDA call or launch failed */
+    BGI_ERR_ALLOC = -3,       /* device or pinned allocation failed */
+    BGI_ERR_UNSUPPORTED = -4, /* valid input this build does not handle (e.g. image side) */
+    BGI_ERR_STATE = -5        /* handle not ready (array or frequencies not set) */
+};
+
+/* Polarisation to image; same order as the reference's enum class Polarization
+ * (src/gridding.hpp:4). */
+enum bgi_pol { BGI_POL_XX = 0, BGI_POL_YY = 1, BGI_POL_I = 2, BGI_POL_V = 3 };
+
+/* Counter layout for bgi_gridding_gpu. */
+enum bgi_counter_mode {
+    /* counters float[C][N][N], counted for interval 0 only (src/gpu/gridding_gpu.cpp:107,117) */
+    BGI_COUNTERS_FIRST_INTERVAL = 0,
+    /* counters float[T][C][N][N], one per image (the CPU path, src/pacer_imager.cpp:269,387) */
+    BGI_COUNTERS_PER_IMAGE = 1
+};
+
+/* Flags of bgi_image / bgi_image_host. */
+#define BGI_APPLY_GEOMETRIC 0x1u /* ApplyGeometricCorrections (src/pacer_imager.cpp:463-464) */
+#define BGI_APPLY_CABLE 0x2u     /* ApplyCableCorrections (src/pacer_imager.cpp:466-473) */
+
+BGI_API const char *bgi_last_error(void);
+BGI_API int bgi_version(void); /* 100 * major + minor */
+
+/* ------------------------------------------------------------------------------------------
+ * 1. Reference GPU entry points on device pointers
+ * ------------------------------------------------------------------------------------------ */
+
+/* apply_geometric_corrections_gpu (src/gpu/corrections_gpu.cpp:90-101): in place,
+ * V <- V * exp(+2*pi*i*w[b]*nu/c) on all four pols; w indexed per triangular baseline. */
+BGI_API int bgi_apply_geometric_corrections_gpu(float *vis, int n_ant, int n_channels, int n_intervals,
+                                        const float *w, int n_uvw_sets, const double *freqs_hz,
+                                        void *stream);
+
+/* apply_cable_lengths_corrections_gpu (src/gpu/corrections_gpu.cpp:75-87): in place,
+ * V <- V * exp(-2*pi*i*(L[a2]-L[a1])*nu/c). */
+BGI_API int bgi_apply_cable_lengths_corrections_gpu(float *vis, int n_ant, int n_channels,
+                                            int n_intervals, const double *cable_lengths,
+                                            const double *freqs_hz, void *stream);
+
+/* gridding_gpu (src/gpu/gridding_gpu.cpp:130-155): adds every unflagged, finite visibility
+ * (|re|,|im| < 1e12) with uv distance > min_uv at its uv cell and its conjugate at the mirrored
+ * cell of grids[T][C][N][N], and 1 to the matching counters cells.  Cell indices are bit-exact
+ * with the reference (FP64 round-half-away of u/lambda/delta_u).  Grids and counters are
+ * accumulated into, not cleared (the caller zeroes them, as the reference's caller does).
+ * antenna_weights is accepted for signature parity and unused, as in the reference. */
+BGI_API int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
+                     const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                     const float *antenna_weights, const double *freqs_hz, double delta_u,
+                     double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
+                     float *counters, float *grids, void *stream);
+
+/* gpufftPlanMany + gpufftExecC2C(..., BACKWARD) (src/gpu/pacer_imager_hip.cpp:83-99): batched
+ * unnormalised inverse 2D FFT, out of place, our own kernels.  n_pixels: power of two,
+ * 16..4096. */
+BGI_API int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_images,
+                        void *stream);
+
+/* fft_shift_and_norm_gpu (src/gpu/gpu_utils.cpp:128-140): swap halves along x then y and
+ * divide every pixel of image i by fnorm[i % fnorm_size].  x_side must be even. */
+BGI_API int bgi_fft_shift_and_norm_gpu(float *images, int x_side, int y_side, int n_images,
+                               const float *fnorm, int fnorm_size, void *stream);
+
+/* vector_sum_gpu (src/gpu/gpu_utils.cpp:62-71): sums[i] = sum of data[i*image_size ...]. */
+BGI_API int bgi_vector_sum_gpu(const float *data, int64_t image_size, int n_images, float *sums,
+                       void *stream);
+
+/* image_averaging_gpu (src/gpu/gpu_utils.cpp:153-161): out = mean of n_images complex
+ * images of image_size pixels. */
+BGI_API int bgi_image_averaging_gpu(const float *images, int64_t image_size, int n_images, float *out,
+                            void *stream);
+
+/* ------------------------------------------------------------------------------------------
+ * 2. Imager handle: resident array state, fused whole-path imaging
+ *    (CPacerImagerHip with its members, src/gpu/pacer_imager_hip.h:12-58)
+ * ------------------------------------------------------------------------------------------ */
+typedef struct bgi_imager bgi_imager;
+
+typedef struct bgi_config {
+    int n_pixels;              /* image side N (power of two, 16..4096) */
+    float oversampling_factor; /* delta_u = osf * u_max / N (src/pacer_imager.cpp:497) */
+    int pol;                   /* enum bgi_pol */
+    double min_uv;             /* uv distance cut in wavelengths (strictly greater passes) */
+    int max_images_per_wave;   /* images gridded and transformed per launch wave; 0 = auto */
+    int device;                /* CUDA device ordinal */
+} bgi_config;
+
+BGI_API int bgi_create(const bgi_config *cfg, bgi_imager **out);
+BGI_API int bgi_destroy(bgi_imager *im);
+
+/* Resident array state from host arrays (copied).  u, v, w: float[n_uvw_sets][B];
+ * baseline_flags: int[B] (nonzero = flagged; autos are flagged by the caller as in
+ * CPacerImager::UpdateFlags, src/pacer_imager.cpp:60-86); cable_lengths: double[n_ant].
+ * Computes u_max/v_max over unflagged baselines of every set and delta_u/delta_v
+ * (src/pacer_imager.cpp:213-221, 497-499). */
+BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, const float *v,
+                  const float *w, const int *baseline_flags, const double *cable_lengths);
+
+/* Channel frequencies in Hz (host array, copied). */
+BGI_API int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz);
+
+/* delta_u, delta_v (metres) and u_max, v_max of the current array state. */
+BGI_API int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
+                    double *v_max);
+
+/* Whole path on device buffers: vis float[T][C][B][4][2] (read only: corrections are applied
+ * in registers and not written back), images float[T][C][N][N][2] out.  Each image is
+ * normalised by its own weight sum (the CPU path, src/pacer_imager.cpp:171-178) and
+ * fftshifted.  Stream-ordered; no host synchronisation. */
+BGI_API int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
+              void *stream);
+
+/* The same on host buffers: copies vis to the device, images it, copies images back and
+ * synchronises the stream before returning. */
+BGI_API int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsigned flags,
+                   float *images_host, void *stream);
+
+/* Per-image weight sums (number of gridded points) of the last bgi_image call on this
+ * handle, as uint32[n_images]; copies to host and synchronises the stream. */
+BGI_API int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream);
+
+/* Stage timing of bgi_image: when enabled, CUDA events are recorded on the call's stream
+ * around each launch (gridding, FFT row pass, FFT column pass).  Recording adds no host
+ * synchronisation.  bgi_get_stage_times synchronises on the recorded events, writes the summed
+ * milliseconds and launch counts of the three stages since the last read, and resets them. */
+BGI_API int bgi_set_stage_timing(bgi_imager *im, int enable);
+BGI_API int bgi_get_stage_times(bgi_imager *im, double ms[3], int64_t launches[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,61 @@
+"""C ABI library on the host: it builds, loads, exports every symbol the public header
+declares, and rejects bad arguments before touching the GPU."""
+import ctypes as C
+import shutil
+
+import pytest
+
+from imager_gb300 import capi
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if shutil.which("nvcc") is None and not __import__("os").path.exists(capi.library_path()):
+        pytest.skip("nvcc not available to build the library")
+    return capi.lib(build_if_missing=True)
+
+
+def test_exports_every_header_symbol(lib):
+    names = capi.header_functions()
+    assert len(names) >= 17
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) == set(capi._SIGNATURES), "ctypes signatures out of date with the header"
+
+
+def test_version(lib):
+    assert lib.bgi_version() == 1
+
+
+def test_host_side_argument_checks(lib):
+    # odd x side is rejected as in src/gpu/gpu_utils.cpp:129-131
+    assert lib.bgi_fft_shift_and_norm_gpu(C.c_void_p(16), 3, 2, 1, C.c_void_p(16), 1, None) == capi.ERR_INVALID
+    assert b"even" in lib.bgi_last_error()
+    # unsupported FFT size
+    assert lib.bgi_fft_inverse_gpu(C.c_void_p(16), C.c_void_p(32), 100, 1, None) == capi.ERR_UNSUPPORTED
+    # in-place FFT is refused
+    assert lib.bgi_fft_inverse_gpu(C.c_void_p(16), C.c_void_p(16), 64, 1, None) == capi.ERR_INVALID
+    # null buffers
+    assert lib.bgi_gridding_gpu(None, 4, 1, 1, None, None, 1, None, None, None, 1.0, 1.0, 64, -1.0, 0,
+                                1, None, None, None) == capi.ERR_INVALID
+    assert lib.bgi_vector_sum_gpu(None, 10, 1, None, None) == capi.ERR_INVALID
+    # misaligned visibilities
+    assert lib.bgi_apply_cable_lengths_corrections_gpu(C.c_void_p(8), 4, 1, 1, C.c_void_p(16),
+                                                      C.c_void_p(16), None) == capi.ERR_INVALID
+    # bad pol
+    assert lib.bgi_gridding_gpu(C.c_void_p(16), 4, 1, 1, C.c_void_p(16), C.c_void_p(16), 1, C.c_void_p(16),
+                                None, C.c_void_p(16), 1.0, 1.0, 64, -1.0, 7, 1, None,
+                                C.c_void_p(16), None) == capi.ERR_INVALID
+
+
+def test_create_rejects_bad_config(lib):
+    h = C.c_void_p()
+    for cfg in (capi.Config(100, 2.0, 0, -1.0, 0, 0), capi.Config(512, 0.0, 0, -1.0, 0, 0),
+                capi.Config(512, 2.0, 9, -1.0, 0, 0), capi.Config(512, 2.0, 0, -1.0, -3, 0)):
+        st = lib.bgi_create(C.byref(cfg), C.byref(h))
+        assert st in (capi.ERR_UNSUPPORTED, capi.ERR_INVALID), (cfg.n_pixels, st)
+        assert not h.value
+    assert lib.bgi_create(None, C.byref(h)) == capi.ERR_INVALID
+    # null handle calls
+    assert lib.bgi_image(None, C.c_void_p(16), 1, 0, C.c_void_p(16), None) == capi.ERR_INVALID
+    assert lib.bgi_destroy(None) == capi.OK

@@ -1,0 +1,333 @@
+"""CUDA path against the oracle and the reference's own outputs (golden vectors), through the
+C ABI.  Tolerances: cell indices and counters bit-exact; grids within FP32 summation-order
+error; images within 1e-4 relative L2 of the FP64 oracle (the path's stated bound)."""
+import ast
+import math
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from imager_gb300 import capi, synth  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+IMAGE_TOL = 1e-4      # relative L2 per image vs the FP64 oracle
+C_LIGHT = 299792458.0
+
+
+@pytest.fixture(scope="module")
+def im():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    capi.lib(build_if_missing=True)
+    O.build()
+    from imager_gb300 import imager
+    return imager
+
+
+def dev(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# ------------------------------------------------------------------------------------------
+# corrections
+# ------------------------------------------------------------------------------------------
+def test_corrections_against_reference_golden(im):
+    g = np.load(os.path.join(GOLD, "corrections.npz"))
+    vis = g["vis"]
+    for name, fn, after in (("geometric", lambda t: im.apply_geometric_corrections(t, dev(g["w"]), dev(g["freqs"])),
+                             g["after_geometric"]),
+                            ("cable", lambda t: im.apply_cable_corrections(t, dev(g["cable"]), dev(g["freqs"])),
+                             g["after_cable"])):
+        t = dev(vis)
+        fn(t)
+        out = t.cpu().numpy()
+        err = np.abs(out - after).max() / np.abs(after).max()
+        assert err < 2e-6, (name, err)
+        assert rel_l2(out.view(np.complex64), after.view(np.complex64)) < 1e-6, name
+
+
+def test_corrections_per_interval_uvw(im):
+    obs = synth.small(seed=21, n_ant=30, n_intervals=3, n_channels=2)
+    vis = obs.vis_f32().copy()
+    ref = vis.copy()
+    O.apply_geometric(ref, obs.w, obs.freqs, n_uvw_sets=3)
+    t = dev(vis)
+    im.apply_geometric_corrections(t, dev(obs.w), dev(obs.freqs), n_uvw_sets=3)
+    assert rel_l2(t.cpu().numpy().view(np.complex64), ref.view(np.complex64)) < 1e-6
+
+
+# ------------------------------------------------------------------------------------------
+# gridding: counters exact (proves every cell index), grids within summation-order error
+# ------------------------------------------------------------------------------------------
+def _grid_gpu(im, vis, u, v, flags, freqs, du, dv, n, min_uv, pol, n_uvw_sets, mode=capi.COUNTERS_PER_IMAGE):
+    T, Cn = vis.shape[:2]
+    grids = torch.zeros((T, Cn, n, n), dtype=torch.complex64, device="cuda")
+    cshape = (T, Cn, n, n) if mode == capi.COUNTERS_PER_IMAGE else (Cn, n, n)
+    counters = torch.zeros(cshape, dtype=torch.float32, device="cuda")
+    im.gridding(dev(vis), dev(u), dev(v), dev(flags), dev(freqs), du, dv, n, min_uv, pol, grids,
+                counters, counter_mode=mode, n_uvw_sets=n_uvw_sets)
+    return grids.cpu().numpy(), counters.cpu().numpy()
+
+
+def _check_grids(g_gpu, g_ref_f32):
+    ref = g_ref_f32.view(np.complex64)[..., 0]
+    scale = max(np.abs(ref).max(), 1e-30)
+    assert np.abs(g_gpu - ref).max() <= 1e-5 * scale
+    # cells the oracle never touched stay exactly zero
+    assert np.all(g_gpu[ref == 0] == 0)
+
+
+@pytest.mark.parametrize("pol", ["XX", "YY", "I", "V"])
+@pytest.mark.parametrize("min_uv", [-1000.0, 3.0])
+def test_gridding_against_oracle(im, pol, min_uv):
+    obs = synth.small(seed=31, n_ant=40, n_intervals=3, n_channels=4, n_pixels=128)
+    vis = obs.vis_f32().copy()
+    vis[0, 1, 17, 0, 0] = np.nan
+    vis[1, 0, 23, 3, 1] = np.inf
+    vis[2, 3, 40, 0, 1] = 3e12
+    umax, vmax = O.uv_max(obs.u, obs.v, obs.flags)
+    du, dv = O.delta_uv(2.0, umax, 128), O.delta_uv(2.0, vmax, 128)
+    g_ref, c_ref, _ = O.gridding(vis, obs.u, obs.v, obs.flags, obs.freqs, du, dv, 128, min_uv, pol, n_uvw_sets=3)
+    g, c = _grid_gpu(im, vis, obs.u, obs.v, obs.flags, obs.freqs, du, dv, 128, min_uv, pol, 3)
+    assert np.array_equal(c, c_ref)
+    _check_grids(g, g_ref)
+    # counters of interval 0 only, laid out per channel (src/gpu/gridding_gpu.cpp:107,117)
+    _, c0 = _grid_gpu(im, vis, obs.u, obs.v, obs.flags, obs.freqs, du, dv, 128, min_uv, pol, 3,
+                      mode=capi.COUNTERS_FIRST_INTERVAL)
+    assert np.array_equal(c0, c_ref[0])
+
+
+def test_gridding_rounding_ties_and_wraps(im):
+    """Pixel coordinates at and one ulp either side of half-integers, min_uv equal to the uv
+    distance, and coordinates beyond the grid (wrapped or dropped as in calculate_pos)."""
+    n_ant, n = 32, 64
+    nb = n_ant * (n_ant + 1) // 2
+    rng = np.random.default_rng(3)
+    base = rng.integers(-40, 40, nb).astype(np.float32) + np.float32(0.5)
+    u = base.copy()
+    u[::3] = np.nextafter(base[::3], np.float32(np.inf))
+    u[1::3] = np.nextafter(base[1::3], np.float32(-np.inf))
+    v = (rng.integers(-40, 40, nb) + 0.5).astype(np.float32)
+    v[5] = 4.0
+    u[5] = 3.0                       # distance exactly 5 wavelengths
+    u[7], v[7] = 100.5, 2.0          # beyond N/2: wraps
+    u[8], v[8] = -70.5, 3.5          # below -N: negative index, dropped or wrapped as the reference
+    u[9], v[9] = 2.5, -80.0
+    flags = np.zeros(nb, np.int32)
+    freqs = np.array([C_LIGHT, C_LIGHT * 0.75])  # wavelength exactly 1 m, then 4/3 m
+    vis = (rng.standard_normal((1, 2, nb, 4, 2))).astype(np.float32)
+    for min_uv in (-1.0, 5.0):
+        g_ref, c_ref, _ = O.gridding(vis, u, v, flags, freqs, 1.0, 1.0, n, min_uv, "XX")
+        g, c = _grid_gpu(im, vis, u, v, flags, freqs, 1.0, 1.0, n, min_uv, "XX", 1)
+        assert np.array_equal(c, c_ref), min_uv
+        _check_grids(g, g_ref)
+
+
+def test_gridding_against_reference_golden(im):
+    """bgi_gridding_gpu on the reference's corrected visibilities reproduces the reference's
+    counters exactly and its grids to summation order, including the 48-pixel case."""
+    g = np.load(os.path.join(GOLD, "imager_run.npz"))
+    meta = ast.literal_eval(str(g["meta"]))
+    pols = ["XX", "YY", "I", "V"]
+    for name, m in meta.items():
+        if m.get("weighting") == "U":
+            continue
+        vis_c = g[f"{name}__vis_out"]
+        Cn = vis_c.shape[1]
+        freqs = (np.full(Cn, m["freq_override_mhz"] * 1e6) if "freq_override_mhz" in m else g["freqs_cotter"])
+        flags = O.update_flags(len(g["cable"]), m.get("flagged", (3,)))
+        du, dv = g[f"{name}__scalars"][:2]
+        gr, c = _grid_gpu(im, vis_c, g["u"], g["v"], flags, freqs, du, dv, m["n_pixels"],
+                          m.get("min_uv", -1000.0), pols[m["pol"]], 1)
+        assert np.array_equal(c, g[f"{name}__counters"]), name
+        _check_grids(gr, g[f"{name}__grids"])
+
+
+# ------------------------------------------------------------------------------------------
+# FFT and epilogues
+# ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("n,batch", [(16, 3), (32, 2), (64, 3), (128, 2), (256, 2), (512, 2),
+                                     (1024, 1), (2048, 1), (4096, 1)])
+def test_fft_inverse_against_numpy(im, n, batch):
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal((batch, n, n)) + 1j * rng.standard_normal((batch, n, n))).astype(np.complex64)
+    out = torch.empty((batch, n, n), dtype=torch.complex64, device="cuda")
+    im.fft_inverse(dev(x), out)
+    ref = np.fft.ifft2(x.astype(np.complex128)) * n * n
+    assert rel_l2(out.cpu().numpy(), ref) < 2e-6 * math.log2(n)
+
+
+def _shift_norm_reference_gpu_semantics(data, fnorm):
+    """numpy restatement of fft_shift_and_norm_x/_y (src/gpu/gpu_utils.cpp:80-123)."""
+    out = data.copy()
+    n_img, ys, xs = out.shape
+    sh = lambda p, s: (p + s // 2 + s % 2) % s  # noqa: E731
+    for i in range(n_img):
+        for y in range(ys):
+            for x in range(xs // 2):
+                d = sh(x, xs)
+                out[i, y, x], out[i, y, d] = out[i, y, d], out[i, y, x]
+        f = np.float32(fnorm[i % len(fnorm)])
+        for y in range(ys // 2):
+            d = sh(y, ys)
+            a, b = out[i, y].copy(), out[i, d].copy()
+            out[i, d] = (a.real / f) + 1j * (a.imag / f)
+            out[i, y] = (b.real / f) + 1j * (b.imag / f)
+    return out.astype(np.complex64)
+
+
+def test_fft_shift_and_norm_known_answer(im):
+    """tests/gpu_utils_test.cpp:60-88 of the reference."""
+    x = np.tile(np.array([0, 1, 2, 3], np.complex64), 3).reshape(3, 2, 2)
+    t = dev(x)
+    im.fft_shift_and_norm(t, dev(np.ones(3, np.float32)))
+    assert np.array_equal(t.cpu().numpy().ravel(), np.tile(np.array([3, 2, 1, 0], np.complex64), 3))
+
+
+@pytest.mark.parametrize("ys,xs,nf", [(8, 6, 3), (5, 8, 2), (16, 16, 1)])
+def test_fft_shift_and_norm_against_reference_semantics(im, ys, xs, nf):
+    rng = np.random.default_rng(ys * xs)
+    x = (rng.standard_normal((4, ys, xs)) + 1j * rng.standard_normal((4, ys, xs))).astype(np.complex64)
+    fn = rng.uniform(1, 50, nf).astype(np.float32)
+    t = dev(x)
+    im.fft_shift_and_norm(t, dev(fn))
+    assert np.array_equal(t.cpu().numpy(), _shift_norm_reference_gpu_semantics(x, fn))
+
+
+def test_vector_sum_known_answer(im):
+    """tests/gpu_utils_test.cpp:20-58 of the reference: 5 images x 3000 ints in [0, 50)."""
+    rng = np.random.default_rng(1)
+    data = rng.integers(0, 50, (5, 3000)).astype(np.float32)
+    sums = torch.zeros(5, dtype=torch.float32, device="cuda")
+    im.vector_sum(dev(data), 3000, 5, sums)
+    assert np.array_equal(sums.cpu().numpy(), data.sum(1).astype(np.float32))
+
+
+def test_image_averaging_known_answer(im):
+    """tests/gpu_utils_test.cpp:91-125 of the reference: 4 images 512^2 of (i % 100)."""
+    n_pix = 512 * 512
+    x = np.tile((np.arange(n_pix) % 100).astype(np.complex64), (4, 1)).reshape(4, 512, 512)
+    out = torch.empty((512, 512), dtype=torch.complex64, device="cuda")
+    im.image_averaging(dev(x), out)
+    assert np.array_equal(out.cpu().numpy(), x[0])
+
+
+# ------------------------------------------------------------------------------------------
+# whole path (bgi_image)
+# ------------------------------------------------------------------------------------------
+def _imager_for(im, obs, n, pol="XX", min_uv=-1000.0, wave=0):
+    h = im.Imager(n, 2.0, pol, min_uv, max_images_per_wave=wave)
+    h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+    h.set_frequencies(obs.freqs)
+    return h
+
+
+@pytest.mark.parametrize("pol", ["XX", "YY", "I", "V"])
+@pytest.mark.parametrize("n,wave", [(64, 0), (128, 2)])
+def test_image_against_oracle(im, pol, n, wave):
+    obs = synth.small(seed=41, n_ant=40, n_intervals=2, n_channels=3, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, counters, ref, (du, dv) = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags,
+                                                    obs.freqs, n, pol=pol, n_uvw_sets=2)
+    h = _imager_for(im, obs, n, pol, wave=wave)
+    assert h.uv_cell[:2] == (du, dv)
+    out = h.image(dev(vis)).cpu().numpy()
+    for i in range(out.shape[0]):
+        for j in range(out.shape[1]):
+            assert rel_l2(out[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+    sums = h.weight_sums(6)
+    assert np.array_equal(sums, counters.reshape(6, -1).sum(1).astype(np.uint32))
+    # the host-buffer entry point gives the same images
+    host = h.image_host(np.ascontiguousarray(vis))
+    assert rel_l2(host, out) < 1e-6
+    h.close()
+
+
+def test_image_against_reference_golden(im):
+    """bgi_image on the reference's inputs against the reference's own dirty images."""
+    g = np.load(os.path.join(GOLD, "imager_run.npz"))
+    meta = ast.literal_eval(str(g["meta"]))
+    pols = ["XX", "YY", "I", "V"]
+    checked = 0
+    for name, m in meta.items():
+        n = m["n_pixels"]
+        if m.get("weighting") == "U" or n & (n - 1):
+            continue
+        vis = g["vis_bad"] if name.endswith("_bad") else g["vis"]
+        Cn = vis.shape[1]
+        freqs = (np.full(Cn, m["freq_override_mhz"] * 1e6) if "freq_override_mhz" in m else g["freqs_cotter"])
+        flags = O.update_flags(len(g["cable"]), m.get("flagged", (3,)))
+        h = im.Imager(n, 2.0, pols[m["pol"]], m.get("min_uv", -1000.0))
+        h.set_array(g["u"], g["v"], g["w"], flags, g["cable"])
+        h.set_frequencies(freqs)
+        assert h.uv_cell[:2] == tuple(g[f"{name}__scalars"][:2]), name
+        fl = (im.APPLY_GEOMETRIC if m.get("geom", 1) else 0) | (im.APPLY_CABLE if m.get("cable", 1) else 0)
+        out = h.image(dev(vis), flags=fl).cpu().numpy()
+        ref = g[f"{name}__images"].view(np.complex64)[..., 0]
+        for i in range(out.shape[0]):
+            for j in range(out.shape[1]):
+                assert rel_l2(out[i, j], ref[i, j]) < IMAGE_TOL, (name, i, j)
+        h.close()
+        checked += 1
+    assert checked >= 7
+
+
+def test_image_state_errors(im):
+    h = im.Imager(64)
+    with pytest.raises(capi.BgiError) as e:
+        h.image(torch.zeros((1, 1, 3, 4, 2), device="cuda"))
+    assert e.value.status == capi.ERR_STATE
+    obs = synth.small(seed=5, n_ant=2, n_intervals=2, n_channels=1, n_pixels=64)
+    h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+    h.set_frequencies(obs.freqs)
+    with pytest.raises(capi.BgiError) as e:  # 2 UVW sets for 3 intervals
+        h.image(torch.zeros((3, 1, 3, 4, 2), device="cuda"))
+    assert e.value.status == capi.ERR_INVALID
+    h.close()
+
+
+# ------------------------------------------------------------------------------------------
+# the measured workload at full size: 256 antennas, 64 channels x 10 intervals, 512^2
+# ------------------------------------------------------------------------------------------
+def test_full_size_workload_properties(im):
+    obs = synth.config2(device="cuda")
+    vis = obs.vis_f32()
+    n = obs.n_pixels
+    h = _imager_for(im, obs, n)
+    out = h.image(dev(vis))
+    torch.cuda.synchronize()
+    T, Cn = vis.shape[:2]
+    sums = h.weight_sums(T * Cn)
+    # every unflagged baseline lands twice (min_uv = -1000, all cells in range)
+    assert np.all(sums == 2 * int((obs.flags == 0).sum()))
+    # centre pixel = sum of all grid cells / weight sum = 2 * sum(Re z) / sum(w)
+    corr = vis.copy()
+    O.apply_geometric(corr, obs.w, obs.freqs, n_uvw_sets=T)
+    O.apply_cable(corr, obs.cable, obs.freqs)
+    re = corr[..., 0, 0].astype(np.float64)                     # XX real parts [T][C][B]
+    expect = 2 * (re * (obs.flags == 0)).sum(-1) / sums.reshape(T, Cn)
+    centre = out[:, :, n // 2, n // 2].real.cpu().numpy()
+    peak = out.abs().amax(dim=(2, 3)).cpu().numpy()
+    # FP32 summation over N^2 cells: bound the error by the image peak, not the (small) sum
+    assert np.all(np.abs(centre - expect) <= 1e-5 * peak)
+    # a few whole images against the FP64 oracle
+    du, dv, _, _ = h.uv_cell
+    for t, c in ((0, 0), (4, 31), (9, 63)):
+        g, cnt, _ = O.gridding(corr[t:t + 1, c:c + 1], obs.u[t:t + 1], obs.v[t:t + 1], obs.flags,
+                               obs.freqs[c:c + 1], du, dv, n)
+        ref = O.image_f64(g, cnt)[0, 0]
+        assert rel_l2(out[t, c].cpu().numpy(), ref) < IMAGE_TOL, (t, c)
+    h.close()
