@@ -106,7 +106,7 @@ struct bgi_imager {
     long long n_baselines = 0;
     double u_max = 0, v_max = 0, delta_u = 0, delta_v = 0;
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
-    double *d_dl = nullptr;
+    float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
     int *d_flags = nullptr;
     double *d_freqs = nullptr;
     DevBuf<float2> grid;          // wave scratch: images x N*N
@@ -310,11 +310,14 @@ int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, con
                 um = std::max(um, (double)std::fabs(u[s * nb + b]));
                 vm = std::max(vm, (double)std::fabs(v[s * nb + b]));
             }
-    std::vector<double> dl(nb, 0.0);
+    std::vector<float2> dl(nb, make_float2(0.f, 0.f));
     if (cable_lengths) {
         for (int a1 = 0; a1 < n_ant; ++a1)
-            for (int a2 = 0; a2 <= a1; ++a2)
-                dl[(size_t)a1 * (a1 + 1) / 2 + a2] = cable_lengths[a2] - cable_lengths[a1];
+            for (int a2 = 0; a2 <= a1; ++a2) {
+                const double d = cable_lengths[a2] - cable_lengths[a1];
+                const float hi = (float)d;
+                dl[(size_t)a1 * (a1 + 1) / 2 + a2] = make_float2(hi, (float)(d - (double)hi));
+            }
     }
     im->release_array();
     BGI_TRY(dev_alloc(&im->d_u, nuv, "set_array u"));
@@ -326,7 +329,7 @@ int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, con
     BGI_TRY(check_cuda(cudaMemcpy(im->d_v, v, sizeof(float) * nuv, cudaMemcpyHostToDevice), "set_array copy"));
     if (w) BGI_TRY(check_cuda(cudaMemcpy(im->d_w, w, sizeof(float) * nuv, cudaMemcpyHostToDevice), "set_array copy"));
     else BGI_TRY(check_cuda(cudaMemset(im->d_w, 0, sizeof(float) * nuv), "set_array memset"));
-    BGI_TRY(check_cuda(cudaMemcpy(im->d_dl, dl.data(), sizeof(double) * nb, cudaMemcpyHostToDevice), "set_array copy"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->d_dl, dl.data(), sizeof(float2) * nb, cudaMemcpyHostToDevice), "set_array copy"));
     BGI_TRY(check_cuda(cudaMemcpy(im->d_flags, baseline_flags, sizeof(int) * nb, cudaMemcpyHostToDevice), "set_array copy"));
     im->n_ant = n_ant;
     im->n_baselines = nb;

@@ -19,7 +19,7 @@ int launch_cable(float *vis, int n_ant, int n_channels, int n_intervals, const d
 struct GridParams {
     const float *vis;        // [T][C][B][4][2]
     const float *u, *v, *w;  // [n_uvw_sets][B]
-    const double *dl;        // [B] L[a2]-L[a1] (cable delay), or null
+    const float2 *dl;        // [B] L[a2]-L[a1] (cable delay) as a float pair (hi, lo), or null
     const int *flags;        // [B]
     const double *freqs;     // [C] Hz
     float2 *grids;           // images [img - img_base][N*N]
