@@ -56,7 +56,10 @@ __device__ __forceinline__ ChannelConst make_channel_const(double nu, double du,
 // Shewchuk's adaptive predicates: a cheap approximation with a proven error bound, and the
 // exact computation only where the bound cannot decide.  The min_uv cut uses the same scheme.
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ int wrap_index(int i, int side) { return i >= 0 ? i % side : side + i; }
+__device__ __forceinline__ int wrap_index(int i, int side) {
+    if ((unsigned)i < (unsigned)side) return i;  // the common case, without a division
+    return i >= 0 ? i % side : side + i;
+}
 
 // Exact FP64 path (no contraction: explicit _rn intrinsics).
 __device__ __forceinline__ bool uv_pixels_exact(float u, float v, double wavelength, double du,
@@ -120,6 +123,28 @@ __device__ __forceinline__ long long cell_pos(int ui, int vi, int sign, int n) {
 // Polarisation selection (src/gpu/gridding_gpu.cpp:79-98, src/pacer_imager.cpp:301-325).
 // rec points at one 4-pol record: XX(0,1) XY(2,3) YX(4,5) YY(6,7).
 // ------------------------------------------------------------------------------------------
+// The 8-byte pol values one visibility needs: XX -> (XX, -), YY -> (YY, -), I -> (XX, YY),
+// V -> (XY, YX).  Streaming loads (read once).
+template <int POL>
+__device__ __forceinline__ void load_pols(const float2 *rec, float2 &a, float2 &b) {
+    if (POL == BGI_POL_XX) a = __ldcs(rec);
+    else if (POL == BGI_POL_YY) a = __ldcs(rec + 3);
+    else if (POL == BGI_POL_I) { a = __ldcs(rec); b = __ldcs(rec + 3); }
+    else { a = __ldcs(rec + 1); b = __ldcs(rec + 2); }
+}
+
+template <int POL>
+__device__ __forceinline__ float2 combine_pols(float2 a, float2 b) {
+    if (POL == BGI_POL_XX || POL == BGI_POL_YY) return a;
+    if (POL == BGI_POL_V) {
+        // (0 + 0.5i) * (XY - YX)
+        float dr = __fsub_rn(a.x, b.x), di = __fsub_rn(a.y, b.y);
+        return make_float2(__fsub_rn(__fmul_rn(0.0f, dr), __fmul_rn(0.5f, di)),
+                           __fadd_rn(__fmul_rn(0.0f, di), __fmul_rn(0.5f, dr)));
+    }
+    return make_float2(__fdiv_rn(__fadd_rn(a.x, b.x), 2.0f), __fdiv_rn(__fadd_rn(a.y, b.y), 2.0f));
+}
+
 __device__ __forceinline__ float2 select_pol(const float4 lo, const float4 hi, int pol) {
     // lo = (XX.re, XX.im, XY.re, XY.im), hi = (YX.re, YX.im, YY.re, YY.im)
     if (pol == BGI_POL_XX) return make_float2(lo.x, lo.y);
@@ -157,8 +182,9 @@ __device__ __forceinline__ float2 phasor_df(float d_hi, float d_lo, float f_hi, 
     e = fmaf(d_hi, f_lo, e);
     e = fmaf(d_lo, f_hi, e);
     const float r = (p - rintf(p)) + e;
+    // |2*pi*r| <= pi: the SFU sine/cosine is accurate to 2^-21.4 absolute on [-pi, pi]
     float s, c;
-    sincospif(2.0f * r, &s, &c);
+    __sincosf(6.28318530717958648f * r, &s, &c);
     return make_float2(c, s);
 }
 

@@ -26,37 +26,41 @@ __host__ __device__ constexpr int bitrev(int i, int bits) {
     return bits == 0 ? 0 : ((i & 1) << (bits - 1)) | bitrev(i >> 1, bits - 1);
 }
 
-// cos / sin of 2*pi*j/16
-constexpr float kC1 = 0.923879532511286756f;  // cos(pi/8)
-constexpr float kC2 = 0.707106781186547524f;  // cos(pi/4)
-constexpr float kC3 = 0.382683432365089772f;  // cos(3pi/8)
-__host__ __device__ constexpr float cos16(int j) {
-    return j == 0 ? 1.f : j == 1 ? kC1 : j == 2 ? kC2 : j == 3 ? kC3 : j == 4 ? 0.f
-         : j == 5 ? -kC3 : j == 6 ? -kC2 : j == 7 ? -kC1 : j == 8 ? -1.f : j == 9 ? -kC1
-         : j == 10 ? -kC2 : j == 11 ? -kC3 : j == 12 ? 0.f : j == 13 ? kC3 : j == 14 ? kC2 : kC1;
+// cos(2*pi*j/32) for j = 0..8 (cos(k*pi/16)); the other octants follow by symmetry
+__host__ __device__ constexpr float cos32_base(int j) {
+    return j == 0 ? 1.0f : j == 1 ? 0.980785280403230449f : j == 2 ? 0.923879532511286756f
+         : j == 3 ? 0.831469612302545237f : j == 4 ? 0.707106781186547524f
+         : j == 5 ? 0.555570233019602225f : j == 6 ? 0.382683432365089772f
+         : j == 7 ? 0.195090322016128268f : 0.0f;
 }
-__host__ __device__ constexpr float sin16(int j) { return cos16((j + 12) & 15); }
+__host__ __device__ constexpr float cos32(int j) {
+    return (j & 31) <= 8 ? cos32_base(j & 31)
+         : (j & 31) <= 16 ? -cos32_base(16 - (j & 31))
+         : (j & 31) <= 24 ? -cos32_base((j & 31) - 16)
+                          : cos32_base(32 - (j & 31));
+}
+__host__ __device__ constexpr float sin32(int j) { return cos32(j - 8); }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 w) {
     return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
 }
 
-// a * exp(+2*pi*i*j/16) with compile-time j
+// a * exp(+2*pi*i*j/32) with compile-time j
 template <int J>
-__device__ __forceinline__ float2 twiddle16(float2 a) {
-    constexpr int j = J & 15;
+__device__ __forceinline__ float2 twiddle32(float2 a) {
+    constexpr int j = J & 31;
     if (j == 0) return a;
-    if (j == 4) return make_float2(-a.y, a.x);
-    if (j == 8) return make_float2(-a.x, -a.y);
-    if (j == 12) return make_float2(a.y, -a.x);
-    return cmul(a, make_float2(cos16(j), sin16(j)));
+    if (j == 8) return make_float2(-a.y, a.x);
+    if (j == 16) return make_float2(-a.x, -a.y);
+    if (j == 24) return make_float2(a.y, -a.x);
+    return cmul(a, make_float2(cos32(j), sin32(j)));
 }
 
 // Butterflies of one radix-2 DIT stage of length LEN on the bit-reversed register array.
 template <int R, int LEN, int K, bool END = (K == LEN / 2)>
 struct StageLoop {
     __device__ __forceinline__ static void run(float2 *a, int s) {
-        float2 u = a[s + K], v = twiddle16<K * (16 / LEN)>(a[s + K + LEN / 2]);
+        float2 u = a[s + K], v = twiddle32<K * (32 / LEN)>(a[s + K + LEN / 2]);
         a[s + K] = make_float2(u.x + v.x, u.y + v.y);
         a[s + K + LEN / 2] = make_float2(u.x - v.x, u.y - v.y);
         StageLoop<R, LEN, K + 1>::run(a, s);
@@ -109,7 +113,7 @@ struct BitRevSwap<R, I, true> {
     __device__ __forceinline__ static void run(float2 *) {}
 };
 
-// In-register inverse DFT of size R (2..16): A_k = sum_m a_m exp(+2*pi*i*m*k/R).
+// In-register inverse DFT of size R (2..32): A_k = sum_m a_m exp(+2*pi*i*m*k/R).
 template <int R>
 __device__ __forceinline__ void dft(float2 *a) {
     BitRevSwap<R, 0>::run(a);
@@ -120,22 +124,37 @@ template <int N, int R>
 struct FftCfg {
     static constexpr int P = N / R;  // threads per transform
     static constexpr int LOGN = ilog2(N), LOGR = ilog2(R);
-    static constexpr int NFULL = LOGN / LOGR;  // radix-R passes
+    static constexpr int NFULL = LOGN / LOGR;      // radix-R passes
     static constexpr int R2 = 1 << (LOGN % LOGR);  // radix of the final pass (1 = none)
     static constexpr int NPASS = NFULL + (R2 > 1 ? 1 : 0);
-    static constexpr int PAD = 1;  // float2 padding per transform in shared memory
-    static_assert(NPASS >= 2, "at least two passes (global loads and stores are separated)");
+    static constexpr int LEN = N + N / R;  // shared elements of one transform, padded
+    static_assert(NPASS >= 2, "at least two passes (loads and stores are separated by barriers)");
 };
 
-// One 1D inverse transform of length N by P threads (t = 0..P-1).  sm: this transform's N
-// shared elements; tw: N twiddles.  gload(i) reads input element i, gstore(i, v) writes output
-// element i.  Every thread of the block must call this the same way (block barriers).
-template <int N, int R, class GLoad, class GStore>
+// Shared-memory index with one pad element after every R elements, so that the first pass's
+// Stockham writes (stride R between consecutive threads) fall on distinct banks.
+template <int LOGR>
+__device__ __forceinline__ int pidx(int i) { return i + (i >> LOGR); }
+
+template <bool WARP>
+__device__ __forceinline__ void fft_sync() {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+}
+
+// One 1D inverse transform of length N by P = N/R threads (t = 0..P-1).  sm: this transform's
+// LEN shared elements; tw: N twiddles.  gload(i) reads input element i, gstore(i, v) writes
+// output element i.  WARP: the P threads of a transform lie in one warp (P <= 32), so passes
+// synchronise with __syncwarp; otherwise every thread of the block calls this in lockstep and
+// passes use block barriers.  ALIASED: gstore writes into sm, so the final stores wait until
+// every thread has read its last inputs.
+template <int N, int R, bool WARP, bool ALIASED, class GLoad, class GStore>
 __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *tw, GLoad gload,
                                               GStore gstore) {
     using C = FftCfg<N, R>;
     constexpr int P = C::P;
     constexpr int R2 = C::R2;
+    constexpr int LR = C::LOGR;
     float2 a[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = gload(t + m * P);
@@ -151,63 +170,91 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
         dft<R>(a);
         const int base = (t - k) * R + k;
         if (p == C::NPASS - 1) {
+            if (ALIASED) fft_sync<WARP>();
 #pragma unroll
             for (int m = 0; m < R; ++m) gstore(base + m * Ns, a[m]);
         } else {
-            __syncthreads();
+            fft_sync<WARP>();
 #pragma unroll
-            for (int m = 0; m < R; ++m) sm[base + m * Ns] = a[m];
-            __syncthreads();
+            for (int m = 0; m < R; ++m) sm[pidx<LR>(base + m * Ns)] = a[m];
+            fft_sync<WARP>();
             if (p + 1 < C::NFULL) {
 #pragma unroll
-                for (int m = 0; m < R; ++m) a[m] = sm[t + m * P];
+                for (int m = 0; m < R; ++m) a[m] = sm[pidx<LR>(t + m * P)];
             } else {
 #pragma unroll
                 for (int q = 0; q < R / R2; ++q)
 #pragma unroll
-                    for (int m = 0; m < R2; ++m) a[q * R2 + m] = sm[t + q * P + m * (N / R2)];
+                    for (int m = 0; m < R2; ++m) a[q * R2 + m] = sm[pidx<LR>(t + q * P + m * (N / R2))];
             }
         }
         Ns *= R;
     }
     if constexpr (R2 > 1) {
+        if (ALIASED) fft_sync<WARP>();
 #pragma unroll
         for (int q = 0; q < R / R2; ++q) {
             const int j = t + q * P;
-            constexpr int RB = R2 > 1 ? R2 : 2;
-            float2 b[RB];
+            float2 b[R2];
 #pragma unroll
             for (int m = 0; m < R2; ++m) b[m] = m ? cmul(a[q * R2 + m], tw[m * j]) : a[q * R2];
-            dft<RB>(b);
+            dft<R2>(b);
 #pragma unroll
             for (int m = 0; m < R2; ++m) gstore(j + m * (N / R2), b[m]);
         }
     }
 }
 
+// Twiddles exp(+2*pi*i*j/N), j < N, into shared memory: sincospif on the first octant
+// (N/8 + 1 values, in oct[]), then every entry from the octant by the exact symmetries of sine
+// and cosine (each entry written once, so the table is deterministic).  Ends with a barrier.
 template <int N>
-__device__ __forceinline__ void init_twiddles(float2 *tw) {
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+__device__ __forceinline__ void init_twiddles(float2 *tw, float2 *oct) {
+    constexpr int Q = N / 4, O = N / 8;
+    for (int k = threadIdx.x; k <= O; k += blockDim.x) {
         float s, c;
         sincospif(2.0f * (float)k / (float)N, &s, &c);
-        tw[k] = make_float2(c, s);
+        oct[k] = make_float2(c, s);
     }
+    __syncthreads();
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const int quad = j / Q, k = j % Q;
+        float2 v = k <= O ? oct[k] : make_float2(oct[Q - k].y, oct[Q - k].x);
+        if (quad == 1) v = make_float2(-v.y, v.x);
+        else if (quad == 2) v = make_float2(-v.x, -v.y);
+        else if (quad == 3) v = make_float2(v.y, -v.x);
+        tw[j] = v;
+    }
+    __syncthreads();
 }
 
-template <int N, int R, int ROWS, bool ZERO_SRC>
-__global__ void __launch_bounds__(ROWS *(N / R)) fft_rows_kernel(float2 *src, float2 *dst) {
-    using C = FftCfg<N, R>;
+// Launch shapes per image side: radix R, warp-synchronous transforms (P <= 32) or block
+// barriers, transforms per row-pass block, columns per column-pass block (a tile pair).
+template <int N>
+struct Shape {
+    static constexpr int R = N <= 128 ? 8 : N <= 512 ? 16 : N == 1024 ? 32 : 16;
+    static constexpr int P = N / R;
+    static constexpr bool WARP = P <= 32;
+    static constexpr int ROWS = WARP ? ((256 / P) < N ? (256 / P) : N) : 256 / P;
+    static constexpr int COLS = WARP ? ROWS : 4;
+    static constexpr int OCT = N / 8 + 2;  // octant scratch, even for 16-byte alignment
+};
+
+template <int N, bool ZERO_SRC>
+__global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(float2 *src, float2 *dst) {
+    using S = Shape<N>;
+    using C = FftCfg<N, S::R>;
     extern __shared__ float2 smem[];
     float2 *tw = smem;
-    float2 *buf = smem + N;
-    init_twiddles<N>(tw);
-    __syncthreads();
-    const int r_local = threadIdx.x / C::P, t = threadIdx.x % C::P;
-    const size_t row = (size_t)blockIdx.x * ROWS + r_local;
+    float2 *oct = tw + N;
+    float2 *buf = oct + S::OCT;
+    init_twiddles<N>(tw, oct);
+    const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
+    const size_t row = (size_t)blockIdx.x * S::ROWS + slot;
     float2 *s_row = src + row * N;
     float2 *d_row = dst + row * N;
-    fft_transform<N, R>(
-        t, buf + r_local * (N + C::PAD), tw,
+    fft_transform<N, S::R, S::WARP, false>(
+        t, buf + slot * C::LEN, tw,
         [&](int i) {
             float2 v = s_row[i];
             if (ZERO_SRC) s_row[i] = make_float2(0.f, 0.f);
@@ -216,49 +263,55 @@ __global__ void __launch_bounds__(ROWS *(N / R)) fft_rows_kernel(float2 *src, fl
         [&](int i, float2 v) { d_row[i] = v; });
 }
 
-template <int N, int R, int CT, bool SHIFT_NORM>
-__global__ void __launch_bounds__(2 * CT *(N / R)) fft_cols_kernel(float2 *images,
-                                                                    const unsigned int *wsum) {
-    using C = FftCfg<N, R>;
-    constexpr int COLS = 2 * CT;
-    constexpr int TILES = (N / 2) / CT;
+// Column pass on a tile pair: columns [x0, x0+CT) and their fftshift partners [x0+N/2, ...),
+// all N rows, staged in shared memory (column-major, padded).  Loads and stores move whole
+// row segments of the tile, so both are coalesced; each transform works on one contiguous
+// column.  With SHIFT_NORM the stores apply the fftshift and multiply by (float)(1/sum(w)).
+template <int N, bool SHIFT_NORM>
+__global__ void __launch_bounds__(Shape<N>::COLS *Shape<N>::P) fft_cols_kernel(float2 *images,
+                                                                               const unsigned int *wsum) {
+    using S = Shape<N>;
+    using C = FftCfg<N, S::R>;
+    constexpr int COLS = S::COLS, CT = COLS / 2, TILES = (N / 2) / CT;
+    constexpr int LR = C::LOGR;
+    constexpr int MOD = COLS >= 16 ? 1 : 16 / COLS;  // column stride modulo 16 (banks)
+    constexpr int STRIDE = C::LEN + ((MOD - C::LEN % 16) + 16) % 16;
     extern __shared__ float2 smem[];
     float2 *tw = smem;
-    float2 *buf = smem + N;
-    init_twiddles<N>(tw);
-    __syncthreads();
-    const int c_local = threadIdx.x % COLS, t = threadIdx.x / COLS;
+    float2 *oct = tw + N;
+    float2 *tile = oct + S::OCT;
+    init_twiddles<N>(tw, oct);
     const size_t img = blockIdx.x / TILES;
-    const int tile = blockIdx.x % TILES;
-    const int col = c_local < CT ? tile * CT + c_local : N / 2 + tile * CT + (c_local - CT);
+    const int x0 = (blockIdx.x % TILES) * CT;
     float2 *im = images + img * (size_t)N * N;
+    for (int e = threadIdx.x; e < N * COLS; e += blockDim.x) {
+        const int r = e / COLS, c = e % COLS;
+        const int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
+        tile[c * STRIDE + pidx<LR>(r)] = im[(size_t)r * N + col];
+    }
+    __syncthreads();
+    {
+        const int c = threadIdx.x / S::P, t = threadIdx.x % S::P;
+        float2 *col_buf = tile + c * STRIDE;
+        fft_transform<N, S::R, S::WARP, true>(
+            t, col_buf, tw, [&](int i) { return col_buf[pidx<LR>(i)]; },
+            [&](int i, float2 v) { col_buf[pidx<LR>(i)] = v; });
+    }
+    __syncthreads();
     float scale = 1.0f;
     if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img]);
-    const int dcol = SHIFT_NORM ? ((col + N / 2) & (N - 1)) : col;
-    fft_transform<N, R>(
-        t, buf + c_local * (N + C::PAD), tw,
-        [&](int i) { return im[(size_t)i * N + col]; },
-        [&](int i, float2 v) {
-            int r = i;
-            if (SHIFT_NORM) {
-                r = (i + N / 2) & (N - 1);
-                v = make_float2(v.x * scale, v.y * scale);
-            }
-            im[(size_t)r * N + dcol] = v;
-        });
-}
-
-// Per-size launch shapes: radix, rows per row-pass block, column tile width.
-struct Shape {
-    int r, rows, ct;
-};
-constexpr Shape shape_for(int n) {
-    return n <= 128 ? Shape{8, 16, 8}
-         : n == 256 ? Shape{8, 8, 4}
-         : n == 512 ? Shape{8, 4, 4}
-         : n == 1024 ? Shape{16, 4, 4}
-         : n == 2048 ? Shape{16, 2, 2}
-                     : Shape{16, 1, 2};
+    for (int e = threadIdx.x; e < N * COLS; e += blockDim.x) {
+        const int r = e / COLS, c = e % COLS;
+        int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
+        float2 v = tile[c * STRIDE + pidx<LR>(r)];
+        int row = r;
+        if (SHIFT_NORM) {
+            row = (r + N / 2) & (N - 1);
+            col = (col + N / 2) & (N - 1);
+            v = make_float2(v.x * scale, v.y * scale);
+        }
+        __stcs(im + (size_t)row * N + col, v);
+    }
 }
 
 template <class K>
@@ -272,43 +325,28 @@ int prepare(K kernel, size_t smem) {
 
 template <int N>
 int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStream_t s) {
-    constexpr Shape sh = shape_for(N);
-    constexpr int ROWS = sh.rows < N ? sh.rows : N;
-    constexpr int P = N / sh.r;
-    const size_t smem = sizeof(float2) * (N + ROWS * (N + 1));
-    const unsigned blocks = (unsigned)((size_t)n_images * N / ROWS);
-    if (zero_src) {
-        auto k = fft_rows_kernel<N, sh.r, ROWS, true>;
-        int st = prepare(k, smem);
-        if (st) return st;
-        k<<<blocks, ROWS * P, smem, s>>>(const_cast<float2 *>(src), dst);
-    } else {
-        auto k = fft_rows_kernel<N, sh.r, ROWS, false>;
-        int st = prepare(k, smem);
-        if (st) return st;
-        k<<<blocks, ROWS * P, smem, s>>>(const_cast<float2 *>(src), dst);
-    }
+    using S = Shape<N>;
+    const size_t smem = sizeof(float2) * (N + S::OCT + (size_t)S::ROWS * FftCfg<N, S::R>::LEN);
+    const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
+    auto k = zero_src ? fft_rows_kernel<N, true> : fft_rows_kernel<N, false>;
+    int st = prepare(k, smem);
+    if (st) return st;
+    k<<<blocks, S::ROWS * S::P, smem, s>>>(const_cast<float2 *>(src), dst);
     return check_launch("fft rows");
 }
 
 template <int N>
 int cols_n(float2 *images, int n_images, const unsigned int *wsum, cudaStream_t s) {
-    constexpr Shape sh = shape_for(N);
-    constexpr int CT = sh.ct;
-    constexpr int P = N / sh.r;
-    const size_t smem = sizeof(float2) * (N + 2 * CT * (N + 1));
-    const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / CT);
-    if (wsum) {
-        auto k = fft_cols_kernel<N, sh.r, CT, true>;
-        int st = prepare(k, smem);
-        if (st) return st;
-        k<<<blocks, 2 * CT * P, smem, s>>>(images, wsum);
-    } else {
-        auto k = fft_cols_kernel<N, sh.r, CT, false>;
-        int st = prepare(k, smem);
-        if (st) return st;
-        k<<<blocks, 2 * CT * P, smem, s>>>(images, nullptr);
-    }
+    using S = Shape<N>;
+    using C = FftCfg<N, S::R>;
+    constexpr int MOD = S::COLS >= 16 ? 1 : 16 / S::COLS;
+    constexpr int STRIDE = C::LEN + ((MOD - C::LEN % 16) + 16) % 16;
+    const size_t smem = sizeof(float2) * (N + S::OCT + (size_t)S::COLS * STRIDE);
+    const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / (S::COLS / 2));
+    auto k = wsum ? fft_cols_kernel<N, true> : fft_cols_kernel<N, false>;
+    int st = prepare(k, smem);
+    if (st) return st;
+    k<<<blocks, S::COLS * S::P, smem, s>>>(images, wsum);
     return check_launch("fft cols");
 }
 

@@ -5,9 +5,8 @@
 // Grid: x = blocks of 256 baselines, y = groups of CPT consecutive images.  A thread owns one
 // baseline for CPT images (consecutive channels of an interval in the common case), so the
 // flags, u/v/w and cable delay it loads serve several visibilities, and all CPT record loads
-// are issued before any is used (memory-level parallelism: the kernel is latency-bound
-// otherwise).  The CPT channels' constants (wavelength and fast cell scales, FP64) are computed
-// by CPT threads in parallel while those loads are in flight.
+// are issued before any is used.  The CPT channels' constants (wavelength and fast cell
+// scales, FP64) are computed by CPT threads in parallel while those loads are in flight.
 //
 // Per visibility: optional fused corrections (one delay phasor in double-float arithmetic and
 // one rotation of the selected pol -- selection is linear, so rotating after selecting equals
@@ -22,14 +21,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kCPT = 8;  // images per thread
 
-template <int POL>
-__device__ __forceinline__ void load_record(const float4 *rec, float4 &lo, float4 &hi) {
-    if (POL != BGI_POL_YY) lo = ld_stream_f4(rec);
-    if (POL != BGI_POL_XX) hi = ld_stream_f4(rec + 1);
-}
-
-template <int POL>
-__global__ void __launch_bounds__(kThreads) grid_kernel(const GridParams p) {
+template <int POL, bool COUNTERS>
+__global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
     __shared__ ChannelConst s_cc[kCPT];
     const int img_first = p.img_begin + blockIdx.y * kCPT;
     const int img_end = p.img_begin + p.img_count;
@@ -37,36 +30,47 @@ __global__ void __launch_bounds__(kThreads) grid_kernel(const GridParams p) {
     const long long nb = p.n_baselines;
     const long long b = (long long)blockIdx.x * kThreads + threadIdx.x;
     const bool in_range = b < nb;
+    const int ch_first = img_first % p.n_channels;
+    const int t_first = img_first / p.n_channels;
 
     // ---- issue every load of this thread ----------------------------------------------------
     int flag = 1;
-    float4 lo[kCPT], hi[kCPT];
+    float2 pa[kCPT], pb[kCPT];
     float uu[kCPT], vv[kCPT], ww[kCPT];
     float2 dl = make_float2(0.f, 0.f);
     if (in_range) {
         flag = p.flags[b];
         if (p.apply_cable) dl = p.dl[b];
+        int ch = ch_first, t = t_first;
 #pragma unroll
         for (int j = 0; j < kCPT; ++j) {
-            lo[j] = hi[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            pa[j] = pb[j] = make_float2(0.f, 0.f);
             uu[j] = vv[j] = ww[j] = 0.f;
             if (j < n_here) {
-                const int img = img_first + j;
-                const size_t set = p.n_uvw_sets > 1 ? (size_t)(img / p.n_channels) : 0;
-                load_record<POL>(reinterpret_cast<const float4 *>(p.vis) + ((size_t)img * nb + b) * 2, lo[j], hi[j]);
-                uu[j] = p.u[set * nb + b];
-                vv[j] = p.v[set * nb + b];
-                if (p.apply_geom) ww[j] = p.w[set * nb + b];
+                const size_t img = (size_t)img_first + j;
+                const size_t off = (p.n_uvw_sets > 1 ? (size_t)t * nb : 0) + b;
+                load_pols<POL>(reinterpret_cast<const float2 *>(p.vis) + (img * nb + b) * 4, pa[j], pb[j]);
+                uu[j] = p.u[off];
+                vv[j] = p.v[off];
+                if (p.apply_geom) ww[j] = p.w[off];
+            }
+            if (++ch == p.n_channels) {
+                ch = 0;
+                ++t;
             }
         }
     }
-    if (threadIdx.x < n_here)
-        s_cc[threadIdx.x] = make_channel_const(p.freqs[(img_first + threadIdx.x) % p.n_channels], p.du, p.dv);
+    if (threadIdx.x < n_here) {
+        int ch = ch_first + threadIdx.x;
+        while (ch >= p.n_channels) ch -= p.n_channels;
+        s_cc[threadIdx.x] = make_channel_const(p.freqs[ch], p.du, p.dv);
+    }
     __syncthreads();
 
     const int n = p.n_pixels;
     const long long npix = (long long)n * n;
     const bool corr = p.apply_geom || p.apply_cable;
+    const bool min_uv_active = p.min_uv >= 0.0;
 #pragma unroll
     for (int j = 0; j < kCPT; ++j) {
         if (j >= n_here) break;  // uniform across the block
@@ -74,8 +78,8 @@ __global__ void __launch_bounds__(kThreads) grid_kernel(const GridParams p) {
         const int local = img - p.img_base;
         unsigned int counted = 0;
         if (in_range && flag <= 0) {
-            const ChannelConst cc = s_cc[j];
-            float2 z = select_pol(lo[j], hi[j], POL);
+            const ChannelConst &cc = s_cc[j];
+            float2 z = combine_pols<POL>(pa[j], pb[j]);
             if (corr) {
                 float d_hi, d_lo;
                 delay_df(ww[j], dl.x, dl.y, d_hi, d_lo);
@@ -83,24 +87,23 @@ __global__ void __launch_bounds__(kThreads) grid_kernel(const GridParams p) {
             }
             int ui, vi;
             if (!isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
-                uv_pixels(uu[j], vv[j], cc, p.du, p.dv, p.min_uv, p.min_uv >= 0.0, &ui, &vi)) {
+                uv_pixels(uu[j], vv[j], cc, p.du, p.dv, p.min_uv, min_uv_active, &ui, &vi)) {
                 const long long pos = cell_pos(ui, vi, +1, n);
                 const long long pos2 = cell_pos(ui, vi, -1, n);
                 float2 *grid = p.grids + (size_t)local * npix;
                 float *cnt = nullptr;
-                if (p.counter_mode == BGI_COUNTERS_PER_IMAGE) {
-                    cnt = p.counters + (size_t)img * npix;
-                } else if (p.counter_mode == BGI_COUNTERS_FIRST_INTERVAL && img < p.n_channels) {
-                    cnt = p.counters + (size_t)img * npix;
+                if (COUNTERS) {
+                    if (p.counter_mode == BGI_COUNTERS_PER_IMAGE || img < p.n_channels)
+                        cnt = p.counters + (size_t)img * npix;
                 }
                 if (pos >= 0) {
                     atomicAdd(grid + pos, z);
-                    if (cnt) atomicAdd(cnt + pos, 1.0f);
+                    if (COUNTERS && cnt) atomicAdd(cnt + pos, 1.0f);
                     ++counted;
                 }
                 if (pos2 >= 0) {
                     atomicAdd(grid + pos2, make_float2(z.x, -z.y));
-                    if (cnt) atomicAdd(cnt + pos2, 1.0f);
+                    if (COUNTERS && cnt) atomicAdd(cnt + pos2, 1.0f);
                     ++counted;
                 }
             }
@@ -110,6 +113,12 @@ __global__ void __launch_bounds__(kThreads) grid_kernel(const GridParams p) {
             if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(p.wsum + local, warp_total);
         }
     }
+}
+
+template <int POL>
+void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
+    if (q.counter_mode >= 0) grid_kernel<POL, true><<<grid, kThreads, 0, s>>>(q);
+    else grid_kernel<POL, false><<<grid, kThreads, 0, s>>>(q);
 }
 
 }  // namespace
@@ -124,10 +133,10 @@ int launch_gridding(const GridParams &p, cudaStream_t s) {
         q.img_count = std::min(p.img_count - done, max_groups * kCPT);
         const dim3 grid((unsigned)bx, (unsigned)((q.img_count + kCPT - 1) / kCPT));
         switch (p.pol) {
-            case BGI_POL_XX: grid_kernel<BGI_POL_XX><<<grid, kThreads, 0, s>>>(q); break;
-            case BGI_POL_YY: grid_kernel<BGI_POL_YY><<<grid, kThreads, 0, s>>>(q); break;
-            case BGI_POL_I: grid_kernel<BGI_POL_I><<<grid, kThreads, 0, s>>>(q); break;
-            default: grid_kernel<BGI_POL_V><<<grid, kThreads, 0, s>>>(q); break;
+            case BGI_POL_XX: launch_pol<BGI_POL_XX>(grid, q, s); break;
+            case BGI_POL_YY: launch_pol<BGI_POL_YY>(grid, q, s); break;
+            case BGI_POL_I: launch_pol<BGI_POL_I>(grid, q, s); break;
+            default: launch_pol<BGI_POL_V>(grid, q, s); break;
         }
         int st = check_launch("gridding");
         if (st) return st;
