@@ -403,8 +403,9 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
         BGI_TRY(check_cuda(cudaMemsetAsync(im->grid.ptr, 0, sizeof(float2) * im->grid.cap, s), "grid scratch clear"));
         im->grid_dirty = false;
     }
-    BGI_TRY(im->wsum.ensure((size_t)n_images, "weight sums"));
-    BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * n_images, s), "weight sums clear"));
+    BGI_TRY(im->wsum.ensure((size_t)n_images * kWsumStride, "weight sums"));
+    BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * kWsumStride * n_images, s),
+                       "weight sums clear"));
 
     GridParams p{};
     p.vis = vis;
@@ -433,7 +434,7 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
         p.img_begin = img0;
         p.img_count = cnt;
         p.img_base = img0;
-        p.wsum = im->wsum.ptr + img0;  // indexed img - img_base
+        p.wsum = im->wsum.ptr + (size_t)img0 * kWsumStride;  // indexed img - img_base
         im->grid_dirty = true;
         BGI_TRY(im->mark(s));
         BGI_TRY(launch_gridding(p, s));
@@ -441,7 +442,7 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
         BGI_TRY(launch_fft_rows(im->grid.ptr, out + (size_t)img0 * npix, n, cnt, true, s));
         im->grid_dirty = false;
         BGI_TRY(im->mark(s));
-        BGI_TRY(launch_fft_cols(out + (size_t)img0 * npix, n, cnt, im->wsum.ptr + img0, s));
+        BGI_TRY(launch_fft_cols(out + (size_t)img0 * npix, n, cnt, im->wsum.ptr + (size_t)img0 * kWsumStride, s));
         BGI_TRY(im->mark(s));
     }
     im->last_images = n_images;
@@ -472,8 +473,9 @@ int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void
     if (n_images > im->last_images) return set_error(BGI_ERR_INVALID, "last_weight_sums: last call had %d images", im->last_images);
     BGI_TRY(im->activate());
     cudaStream_t s = as_stream(stream);
-    BGI_TRY(check_cuda(cudaMemcpyAsync(sums_host, im->wsum.ptr, sizeof(uint32_t) * n_images,
-                                       cudaMemcpyDeviceToHost, s), "last_weight_sums copy"));
+    BGI_TRY(check_cuda(cudaMemcpy2DAsync(sums_host, sizeof(uint32_t), im->wsum.ptr,
+                                         sizeof(uint32_t) * kWsumStride, sizeof(uint32_t), n_images,
+                                         cudaMemcpyDeviceToHost, s), "last_weight_sums copy"));
     return check_cuda(cudaStreamSynchronize(s), "last_weight_sums sync");
 }
 

@@ -142,8 +142,22 @@ __device__ __forceinline__ void fft_sync() {
     else __syncthreads();
 }
 
+// Twiddle tables per pass, laid out [m-1][k] so that consecutive threads (consecutive k) read
+// consecutive entries: full pass p >= 1 (Ns = R^p) holds exp(+2*pi*i*m*k/(Ns*R)) for m in
+// [1, R), k in [0, Ns); the final radix-R2 pass holds exp(+2*pi*i*m*j/N) for m in [1, R2),
+// j in [0, N/R2).
+template <int N, int R>
+struct TwTables {
+    using C = FftCfg<N, R>;
+    static constexpr int ns(int p) { return p == 0 ? 1 : R * ns(p - 1); }
+    static constexpr int off_full(int p) { return p <= 1 ? 0 : off_full(p - 1) + (R - 1) * ns(p - 1); }
+    static constexpr int OFF_REM = off_full(C::NFULL);
+    static constexpr int TOTAL = OFF_REM + (C::R2 > 1 ? (C::R2 - 1) * (N / C::R2) : 0);
+    static constexpr int SIZE = TOTAL > 0 ? TOTAL : 1;
+};
+
 // One 1D inverse transform of length N by P = N/R threads (t = 0..P-1).  sm: this transform's
-// LEN shared elements; tw: N twiddles.  gload(i) reads input element i, gstore(i, v) writes
+// LEN shared elements; tw: the pass twiddle tables (TwTables).  gload(i) reads input element i, gstore(i, v) writes
 // output element i.  WARP: the P threads of a transform lie in one warp (P <= 32), so passes
 // synchronise with __syncwarp; otherwise every thread of the block calls this in lockstep and
 // passes use block barriers.  ALIASED: gstore writes into sm, so the final stores wait until
@@ -152,6 +166,7 @@ template <int N, int R, bool WARP, bool ALIASED, class GLoad, class GStore>
 __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *tw, GLoad gload,
                                               GStore gstore) {
     using C = FftCfg<N, R>;
+    using TT = TwTables<N, R>;
     constexpr int P = C::P;
     constexpr int R2 = C::R2;
     constexpr int LR = C::LOGR;
@@ -159,13 +174,14 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = gload(t + m * P);
     int Ns = 1;
+    int toff = 0;
 #pragma unroll
     for (int p = 0; p < C::NFULL; ++p) {
         const int k = t & (Ns - 1);
         if (p > 0) {
-            const int step = N / (Ns * R);
 #pragma unroll
-            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw[m * k * step]);
+            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw[toff + (m - 1) * Ns + k]);
+            toff += (R - 1) * Ns;
         }
         dft<R>(a);
         const int base = (t - k) * R + k;
@@ -197,7 +213,8 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
             const int j = t + q * P;
             float2 b[R2];
 #pragma unroll
-            for (int m = 0; m < R2; ++m) b[m] = m ? cmul(a[q * R2 + m], tw[m * j]) : a[q * R2];
+            for (int m = 0; m < R2; ++m)
+                b[m] = m ? cmul(a[q * R2 + m], tw[TT::OFF_REM + (m - 1) * (N / R2) + j]) : a[q * R2];
             dft<R2>(b);
 #pragma unroll
             for (int m = 0; m < R2; ++m) gstore(j + m * (N / R2), b[m]);
@@ -205,25 +222,47 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
     }
 }
 
-// Twiddles exp(+2*pi*i*j/N), j < N, into shared memory: sincospif on the first octant
-// (N/8 + 1 values, in oct[]), then every entry from the octant by the exact symmetries of sine
-// and cosine (each entry written once, so the table is deterministic).  Ends with a barrier.
+// exp(+2*pi*i*idx/N) from the first-octant table oct[0..N/8] by the exact symmetries of sine and
+// cosine.
 template <int N>
-__device__ __forceinline__ void init_twiddles(float2 *tw, float2 *oct) {
+__device__ __forceinline__ float2 tw_from_octant(const float2 *oct, int idx) {
     constexpr int Q = N / 4, O = N / 8;
+    const int quad = idx / Q, k = idx % Q;
+    float2 v = k <= O ? oct[k] : make_float2(oct[Q - k].y, oct[Q - k].x);
+    if (quad == 1) v = make_float2(-v.y, v.x);
+    else if (quad == 2) v = make_float2(-v.x, -v.y);
+    else if (quad == 3) v = make_float2(v.y, -v.x);
+    return v;
+}
+
+// Builds the pass twiddle tables (TwTables<N, R>) in shared memory: sincospif on the first
+// octant (N/8 + 1 values in oct[]), every table entry from it (each written once, so the
+// tables are deterministic).  Ends with a barrier.
+template <int N, int R>
+__device__ __forceinline__ void init_twiddles(float2 *tw, float2 *oct) {
+    using C = FftCfg<N, R>;
+    using TT = TwTables<N, R>;
+    constexpr int O = N / 8;
     for (int k = threadIdx.x; k <= O; k += blockDim.x) {
         float s, c;
         sincospif(2.0f * (float)k / (float)N, &s, &c);
         oct[k] = make_float2(c, s);
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < N; j += blockDim.x) {
-        const int quad = j / Q, k = j % Q;
-        float2 v = k <= O ? oct[k] : make_float2(oct[Q - k].y, oct[Q - k].x);
-        if (quad == 1) v = make_float2(-v.y, v.x);
-        else if (quad == 2) v = make_float2(-v.x, -v.y);
-        else if (quad == 3) v = make_float2(v.y, -v.x);
-        tw[j] = v;
+#pragma unroll
+    for (int p = 1; p < C::NFULL; ++p) {
+        const int Ns = TT::ns(p), step = N / (Ns * R), base = TT::off_full(p);
+        for (int e = threadIdx.x; e < (R - 1) * Ns; e += blockDim.x) {
+            const int m = e / Ns + 1, k = e % Ns;
+            tw[base + e] = tw_from_octant<N>(oct, m * k * step);
+        }
+    }
+    if constexpr (C::R2 > 1) {
+        constexpr int J = N / C::R2;
+        for (int e = threadIdx.x; e < (C::R2 - 1) * J; e += blockDim.x) {
+            const int m = e / J + 1, j = e % J;
+            tw[TT::OFF_REM + e] = tw_from_octant<N>(oct, m * j);
+        }
     }
     __syncthreads();
 }
@@ -238,6 +277,7 @@ struct Shape {
     static constexpr int ROWS = WARP ? ((256 / P) < N ? (256 / P) : N) : 256 / P;
     static constexpr int COLS = WARP ? ROWS : 4;
     static constexpr int OCT = N / 8 + 2;  // octant scratch, even for 16-byte alignment
+    static constexpr int TW = (TwTables<N, R>::SIZE + 1) & ~1;  // pass twiddle tables, even
 };
 
 template <int N, bool ZERO_SRC>
@@ -246,9 +286,9 @@ __global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(f
     using C = FftCfg<N, S::R>;
     extern __shared__ float2 smem[];
     float2 *tw = smem;
-    float2 *oct = tw + N;
+    float2 *oct = tw + S::TW;
     float2 *buf = oct + S::OCT;
-    init_twiddles<N>(tw, oct);
+    init_twiddles<N, S::R>(tw, oct);
     const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
     const size_t row = (size_t)blockIdx.x * S::ROWS + slot;
     float2 *s_row = src + row * N;
@@ -278,9 +318,9 @@ __global__ void __launch_bounds__(Shape<N>::COLS *Shape<N>::P) fft_cols_kernel(f
     constexpr int STRIDE = C::LEN + ((MOD - C::LEN % 16) + 16) % 16;
     extern __shared__ float2 smem[];
     float2 *tw = smem;
-    float2 *oct = tw + N;
+    float2 *oct = tw + S::TW;
     float2 *tile = oct + S::OCT;
-    init_twiddles<N>(tw, oct);
+    init_twiddles<N, S::R>(tw, oct);
     const size_t img = blockIdx.x / TILES;
     const int x0 = (blockIdx.x % TILES) * CT;
     float2 *im = images + img * (size_t)N * N;
@@ -299,7 +339,7 @@ __global__ void __launch_bounds__(Shape<N>::COLS *Shape<N>::P) fft_cols_kernel(f
     }
     __syncthreads();
     float scale = 1.0f;
-    if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img]);
+    if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
     for (int e = threadIdx.x; e < N * COLS; e += blockDim.x) {
         const int r = e / COLS, c = e % COLS;
         int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
@@ -326,7 +366,7 @@ int prepare(K kernel, size_t smem) {
 template <int N>
 int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStream_t s) {
     using S = Shape<N>;
-    const size_t smem = sizeof(float2) * (N + S::OCT + (size_t)S::ROWS * FftCfg<N, S::R>::LEN);
+    const size_t smem = sizeof(float2) * (S::TW + S::OCT + (size_t)S::ROWS * FftCfg<N, S::R>::LEN);
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
     auto k = zero_src ? fft_rows_kernel<N, true> : fft_rows_kernel<N, false>;
     int st = prepare(k, smem);
@@ -341,7 +381,7 @@ int cols_n(float2 *images, int n_images, const unsigned int *wsum, cudaStream_t 
     using C = FftCfg<N, S::R>;
     constexpr int MOD = S::COLS >= 16 ? 1 : 16 / S::COLS;
     constexpr int STRIDE = C::LEN + ((MOD - C::LEN % 16) + 16) % 16;
-    const size_t smem = sizeof(float2) * (N + S::OCT + (size_t)S::COLS * STRIDE);
+    const size_t smem = sizeof(float2) * (S::TW + S::OCT + (size_t)S::COLS * STRIDE);
     const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / (S::COLS / 2));
     auto k = wsum ? fft_cols_kernel<N, true> : fft_cols_kernel<N, false>;
     int st = prepare(k, smem);

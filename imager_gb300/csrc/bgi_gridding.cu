@@ -19,11 +19,12 @@ namespace bgi {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kCPT = 8;  // images per thread
+constexpr int kCPT = 4;  // images per thread
 
 template <int POL, bool COUNTERS>
 __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
     __shared__ ChannelConst s_cc[kCPT];
+    __shared__ unsigned int s_count[kCPT];
     const int img_first = p.img_begin + blockIdx.y * kCPT;
     const int img_end = p.img_begin + p.img_count;
     const int n_here = min(kCPT, img_end - img_first);
@@ -64,6 +65,7 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
         int ch = ch_first + threadIdx.x;
         while (ch >= p.n_channels) ch -= p.n_channels;
         s_cc[threadIdx.x] = make_channel_const(p.freqs[ch], p.du, p.dv);
+        s_count[threadIdx.x] = 0;
     }
     __syncthreads();
 
@@ -110,8 +112,14 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
         }
         if (p.wsum) {
             const unsigned int warp_total = __reduce_add_sync(0xffffffffu, counted);
-            if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(p.wsum + local, warp_total);
+            if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(&s_count[j], warp_total);
         }
+    }
+    // one global atomic per block and image
+    if (p.wsum) {
+        __syncthreads();
+        if (threadIdx.x < n_here && s_count[threadIdx.x])
+            atomicAdd(p.wsum + (size_t)(img_first + threadIdx.x - p.img_base) * kWsumStride, s_count[threadIdx.x]);
     }
 }
 

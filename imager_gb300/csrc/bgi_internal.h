@@ -8,6 +8,10 @@
 
 namespace bgi {
 
+// Per-image weight counts live 128 bytes apart: blocks of many images add to them at once, and
+// counters sharing a cache line would serialise those atomics in one L2 slice.
+constexpr int kWsumStride = 32;
+
 // ---- corrections (bgi_corrections.cu) ------------------------------------------------------
 // In place on all four pols.  geometric: delay = w[set][b]; cable: delay = -(L[a2]-L[a1]).
 int launch_geometric(float *vis, int n_ant, int n_channels, int n_intervals, const float *w,
@@ -24,7 +28,7 @@ struct GridParams {
     const double *freqs;     // [C] Hz
     float2 *grids;           // images [img - img_base][N*N]
     float *counters;         // optional counter grids
-    unsigned int *wsum;      // optional per-image weight counts, indexed img - img_base
+    unsigned int *wsum;      // optional per-image weight counts at wsum[(img - img_base) * kWsumStride]
     double du, dv, min_uv;
     long long n_baselines;
     int n_channels, n_intervals, n_uvw_sets, n_pixels, pol;
@@ -41,7 +45,7 @@ bool fft_size_supported(int n);
 int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool zero_src,
                     cudaStream_t s);
 // Column pass in place on images; with wsum != null, also fftshift and multiply image i by
-// (float)(1/wsum[i]).
+// (float)(1/wsum[i * kWsumStride]).
 int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsum,
                     cudaStream_t s);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
