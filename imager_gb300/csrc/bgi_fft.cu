@@ -180,7 +180,7 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
         const int k = t & (Ns - 1);
         if (p > 0) {
 #pragma unroll
-            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw[toff + (m - 1) * Ns + k]);
+            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], __ldg(tw + toff + (m - 1) * Ns + k));
             toff += (R - 1) * Ns;
         }
         dft<R>(a);
@@ -214,7 +214,7 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
             float2 b[R2];
 #pragma unroll
             for (int m = 0; m < R2; ++m)
-                b[m] = m ? cmul(a[q * R2 + m], tw[TT::OFF_REM + (m - 1) * (N / R2) + j]) : a[q * R2];
+                b[m] = m ? cmul(a[q * R2 + m], __ldg(tw + TT::OFF_REM + (m - 1) * (N / R2) + j)) : a[q * R2];
             dft<R2>(b);
 #pragma unroll
             for (int m = 0; m < R2; ++m) gstore(j + m * (N / R2), b[m]);
@@ -222,49 +222,78 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
     }
 }
 
-// exp(+2*pi*i*idx/N) from the first-octant table oct[0..N/8] by the exact symmetries of sine and
-// cosine.
-template <int N>
-__device__ __forceinline__ float2 tw_from_octant(const float2 *oct, int idx) {
-    constexpr int Q = N / 4, O = N / 8;
-    const int quad = idx / Q, k = idx % Q;
-    float2 v = k <= O ? oct[k] : make_float2(oct[Q - k].y, oct[Q - k].x);
-    if (quad == 1) v = make_float2(-v.y, v.x);
-    else if (quad == 2) v = make_float2(-v.x, -v.y);
-    else if (quad == 3) v = make_float2(v.y, -v.x);
-    return v;
+// ---- twiddle tables, evaluated at compile time -------------------------------------------
+// exp(+2*pi*i*idx/N) for the pass tables is computed by the compiler: the index is reduced to
+// the first octant with exact integer arithmetic (symmetries of sine and cosine), and sine and
+// cosine of the octant angle (<= pi/4) come from their Taylor series in double precision (the
+// terms fall below 1e-20 after 12 orders), then round to float.  The tables live in the
+// module's global memory, initialised when the module loads: no set-up launch and no shared
+// memory; kernels read them through L1.
+struct TwEntry {
+    float x, y;
+};
+constexpr double kPi = 3.14159265358979323846;
+constexpr double taylor_sin(double a) {
+    double term = a, sum = a;
+    for (int n = 1; n < 14; ++n) {
+        term *= -a * a / (double)((2 * n) * (2 * n + 1));
+        sum += term;
+    }
+    return sum;
+}
+constexpr double taylor_cos(double a) {
+    double term = 1.0, sum = 1.0;
+    for (int n = 1; n < 14; ++n) {
+        term *= -a * a / (double)((2 * n - 1) * (2 * n));
+        sum += term;
+    }
+    return sum;
+}
+constexpr TwEntry twiddle_exact(int idx, int n) {
+    const int q = n / 4, quad = (idx / q) & 3, k = idx % q;
+    const bool swap = k > n / 8;
+    const double a = 2.0 * kPi * (double)(swap ? q - k : k) / (double)n;
+    double c = taylor_cos(a), s = taylor_sin(a);
+    if (swap) {
+        const double t = c;
+        c = s;
+        s = t;
+    }
+    double x = c, y = s;
+    if (quad == 1) { x = -s; y = c; }
+    else if (quad == 2) { x = -c; y = -s; }
+    else if (quad == 3) { x = s; y = -c; }
+    return TwEntry{(float)x, (float)y};
 }
 
-// Builds the pass twiddle tables (TwTables<N, R>) in shared memory: sincospif on the first
-// octant (N/8 + 1 values in oct[]), every table entry from it (each written once, so the
-// tables are deterministic).  Ends with a barrier.
 template <int N, int R>
-__device__ __forceinline__ void init_twiddles(float2 *tw, float2 *oct) {
+struct TwData {
+    TwEntry v[TwTables<N, R>::SIZE];
+};
+
+template <int N, int R>
+constexpr TwData<N, R> make_twiddles() {
     using C = FftCfg<N, R>;
     using TT = TwTables<N, R>;
-    constexpr int O = N / 8;
-    for (int k = threadIdx.x; k <= O; k += blockDim.x) {
-        float s, c;
-        sincospif(2.0f * (float)k / (float)N, &s, &c);
-        oct[k] = make_float2(c, s);
-    }
-    __syncthreads();
-#pragma unroll
+    TwData<N, R> d{};
     for (int p = 1; p < C::NFULL; ++p) {
-        const int Ns = TT::ns(p), step = N / (Ns * R), base = TT::off_full(p);
-        for (int e = threadIdx.x; e < (R - 1) * Ns; e += blockDim.x) {
-            const int m = e / Ns + 1, k = e % Ns;
-            tw[base + e] = tw_from_octant<N>(oct, m * k * step);
-        }
+        const int ns = TT::ns(p), step = N / (ns * R), base = TT::off_full(p);
+        for (int e = 0; e < (R - 1) * ns; ++e) d.v[base + e] = twiddle_exact((e / ns + 1) * (e % ns) * step, N);
     }
-    if constexpr (C::R2 > 1) {
-        constexpr int J = N / C::R2;
-        for (int e = threadIdx.x; e < (C::R2 - 1) * J; e += blockDim.x) {
-            const int m = e / J + 1, j = e % J;
-            tw[TT::OFF_REM + e] = tw_from_octant<N>(oct, m * j);
-        }
+    if (C::R2 > 1) {
+        const int j_count = N / C::R2;
+        for (int e = 0; e < (C::R2 - 1) * j_count; ++e)
+            d.v[TT::OFF_REM + e] = twiddle_exact((e / j_count + 1) * (e % j_count), N);
     }
-    __syncthreads();
+    return d;
+}
+
+template <int N, int R>
+__device__ const TwData<N, R> g_twiddles = make_twiddles<N, R>();
+
+template <int N, int R>
+__device__ __forceinline__ const float2 *twiddles() {
+    return reinterpret_cast<const float2 *>(g_twiddles<N, R>.v);
 }
 
 // Launch shapes per image side: radix R, warp-synchronous transforms (P <= 32) or block
@@ -275,9 +304,17 @@ struct Shape {
     static constexpr int P = N / R;
     static constexpr bool WARP = P <= 32;
     static constexpr int ROWS = WARP ? ((256 / P) < N ? (256 / P) : N) : 256 / P;
-    static constexpr int COLS = WARP ? ROWS : 4;
-    static constexpr int OCT = N / 8 + 2;  // octant scratch, even for 16-byte alignment
-    static constexpr int TW = (TwTables<N, R>::SIZE + 1) & ~1;  // pass twiddle tables, even
+};
+
+// Column-pass shape: COLS columns per block (a tile pair), P threads per column, block barriers.
+template <int N>
+struct ColShape {
+    static constexpr int R = Shape<N>::R;
+    static constexpr int P = N / R;
+    static constexpr int COLS = (256 / P) < 4 ? 4 : ((256 / P) > N ? N : (256 / P));
+    static constexpr int MOD = COLS >= 16 ? 1 : 16 / COLS;  // column stride modulo 16 (banks)
+    static constexpr int LEN = FftCfg<N, R>::LEN;
+    static constexpr int STRIDE = LEN + ((MOD - LEN % 16) + 16) % 16;
 };
 
 template <int N, bool ZERO_SRC>
@@ -285,10 +322,8 @@ __global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(f
     using S = Shape<N>;
     using C = FftCfg<N, S::R>;
     extern __shared__ float2 smem[];
-    float2 *tw = smem;
-    float2 *oct = tw + S::TW;
-    float2 *buf = oct + S::OCT;
-    init_twiddles<N, S::R>(tw, oct);
+    float2 *buf = smem;
+    const float2 *tw = twiddles<N, S::R>();
     const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
     const size_t row = (size_t)blockIdx.x * S::ROWS + slot;
     float2 *s_row = src + row * N;
@@ -303,55 +338,39 @@ __global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(f
         [&](int i, float2 v) { d_row[i] = v; });
 }
 
-// Column pass on a tile pair: columns [x0, x0+CT) and their fftshift partners [x0+N/2, ...),
-// all N rows, staged in shared memory (column-major, padded).  Loads and stores move whole
-// row segments of the tile, so both are coalesced; each transform works on one contiguous
-// column.  With SHIFT_NORM the stores apply the fftshift and multiply by (float)(1/sum(w)).
+// Column pass in place on a tile pair: columns [x0, x0+CT) and their fftshift partners
+// [x0+N/2, ...).  Thread c + COLS*t runs point t of column c, so the lanes of a warp cover
+// adjacent columns and every global load and store moves whole 32-byte row segments of the
+// tile; the transforms of the COLS columns step through their passes together (block
+// barriers).  All loads of the pair happen in the first pass, before any store, so the shifted
+// stores never race with this block's loads, and no other block touches these columns.  With
+// SHIFT_NORM the stores apply the fftshift and multiply by (float)(1/sum(w)).
 template <int N, bool SHIFT_NORM>
-__global__ void __launch_bounds__(Shape<N>::COLS *Shape<N>::P) fft_cols_kernel(float2 *images,
-                                                                               const unsigned int *wsum) {
-    using S = Shape<N>;
+__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_kernel(float2 *images,
+                                                                                    const unsigned int *wsum) {
+    using S = ColShape<N>;
     using C = FftCfg<N, S::R>;
     constexpr int COLS = S::COLS, CT = COLS / 2, TILES = (N / 2) / CT;
-    constexpr int LR = C::LOGR;
-    constexpr int MOD = COLS >= 16 ? 1 : 16 / COLS;  // column stride modulo 16 (banks)
-    constexpr int STRIDE = C::LEN + ((MOD - C::LEN % 16) + 16) % 16;
     extern __shared__ float2 smem[];
-    float2 *tw = smem;
-    float2 *oct = tw + S::TW;
-    float2 *tile = oct + S::OCT;
-    init_twiddles<N, S::R>(tw, oct);
+    const float2 *tw = twiddles<N, S::R>();
     const size_t img = blockIdx.x / TILES;
     const int x0 = (blockIdx.x % TILES) * CT;
+    const int c = threadIdx.x % COLS, t = threadIdx.x / COLS;
+    const int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
     float2 *im = images + img * (size_t)N * N;
-    for (int e = threadIdx.x; e < N * COLS; e += blockDim.x) {
-        const int r = e / COLS, c = e % COLS;
-        const int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
-        tile[c * STRIDE + pidx<LR>(r)] = im[(size_t)r * N + col];
-    }
-    __syncthreads();
-    {
-        const int c = threadIdx.x / S::P, t = threadIdx.x % S::P;
-        float2 *col_buf = tile + c * STRIDE;
-        fft_transform<N, S::R, S::WARP, true>(
-            t, col_buf, tw, [&](int i) { return col_buf[pidx<LR>(i)]; },
-            [&](int i, float2 v) { col_buf[pidx<LR>(i)] = v; });
-    }
-    __syncthreads();
     float scale = 1.0f;
     if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
-    for (int e = threadIdx.x; e < N * COLS; e += blockDim.x) {
-        const int r = e / COLS, c = e % COLS;
-        int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
-        float2 v = tile[c * STRIDE + pidx<LR>(r)];
-        int row = r;
-        if (SHIFT_NORM) {
-            row = (r + N / 2) & (N - 1);
-            col = (col + N / 2) & (N - 1);
-            v = make_float2(v.x * scale, v.y * scale);
-        }
-        __stcs(im + (size_t)row * N + col, v);
-    }
+    const int dcol = SHIFT_NORM ? ((col + N / 2) & (N - 1)) : col;
+    fft_transform<N, S::R, false, false>(
+        t, smem + c * S::STRIDE, tw, [&](int i) { return im[(size_t)i * N + col]; },
+        [&](int i, float2 v) {
+            int r = i;
+            if (SHIFT_NORM) {
+                r = (i + N / 2) & (N - 1);
+                v = make_float2(v.x * scale, v.y * scale);
+            }
+            __stcs(im + (size_t)r * N + dcol, v);
+        });
 }
 
 template <class K>
@@ -366,7 +385,7 @@ int prepare(K kernel, size_t smem) {
 template <int N>
 int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStream_t s) {
     using S = Shape<N>;
-    const size_t smem = sizeof(float2) * (S::TW + S::OCT + (size_t)S::ROWS * FftCfg<N, S::R>::LEN);
+    const size_t smem = sizeof(float2) * ((size_t)S::ROWS * FftCfg<N, S::R>::LEN);
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
     auto k = zero_src ? fft_rows_kernel<N, true> : fft_rows_kernel<N, false>;
     int st = prepare(k, smem);
@@ -377,11 +396,8 @@ int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStre
 
 template <int N>
 int cols_n(float2 *images, int n_images, const unsigned int *wsum, cudaStream_t s) {
-    using S = Shape<N>;
-    using C = FftCfg<N, S::R>;
-    constexpr int MOD = S::COLS >= 16 ? 1 : 16 / S::COLS;
-    constexpr int STRIDE = C::LEN + ((MOD - C::LEN % 16) + 16) % 16;
-    const size_t smem = sizeof(float2) * (S::TW + S::OCT + (size_t)S::COLS * STRIDE);
+    using S = ColShape<N>;
+    const size_t smem = sizeof(float2) * ((size_t)S::COLS * S::STRIDE);
     const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / (S::COLS / 2));
     auto k = wsum ? fft_cols_kernel<N, true> : fft_cols_kernel<N, false>;
     int st = prepare(k, smem);
