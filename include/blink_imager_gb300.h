@@ -169,6 +169,24 @@ BGI_API int bgi_image_host(bgi_imager *im, const float *vis_host, int n_interval
  * handle, as uint32[n_images]; copies to host and synchronises the stream. */
 BGI_API int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream);
 
+/* Dirty images with no device allocation.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory while they run -- a real-time pipeline that
+ * budgets all GPU memory when an observation starts, a host framework that owns the device
+ * allocator, or code that must not call cudaMalloc/cudaFree on a live stream because they can
+ * synchronise the device.  Same work and arguments as bgi_gridding_gpu on already-corrected
+ * visibilities followed by bgi_fft_inverse_gpu, the fftshift and 1/sum(weights) of each image
+ * (the CPU path's normalisation): vis float[T][C][B][4][2] in, images float[T][C][N][N][2] out.
+ * Scratch is a static 32 MiB grid plus weight counters that every GPU loading the library
+ * holds until exit; the image side is limited to 2048 (larger sides return
+ * BGI_ERR_UNSUPPORTED).  The first call on a device looks up the scratch address and should
+ * come before any stream capture.  All calls share the scratch: each clears what it uses, but
+ * calls that overlap on the GPU race -- serialise them.  Makes no allocating call. */
+BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n_intervals,
+                              const float *u, const float *v, int n_uvw_sets,
+                              const int *baseline_flags, const double *freqs_hz, double delta_u,
+                              double delta_v, int n_pixels, double min_uv, int pol, float *images,
+                              void *stream);
+
 /* Stage timing of bgi_image: when enabled, CUDA events are recorded on the call's stream
  * around each launch (gridding, FFT row pass, FFT column pass).  Recording adds no host
  * synchronisation.  bgi_get_stage_times synchronises on the recorded events, writes the summed
