@@ -47,6 +47,7 @@ _SIGNATURES = {
     "bgi_destroy": (_i, [_vp]),
     "bgi_set_array": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "bgi_set_frequencies": (_i, [_vp, _i, _vp]),
+    "bgi_set_uv_cell": (_i, [_vp, _d, _d]),
     "bgi_get_uv_cell": (_i, [_vp, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     "bgi_image": (_i, [_vp, _vp, _i, _u, _vp, _vp]),
     "bgi_image_host": (_i, [_vp, _vp, _i, _u, _vp, _vp]),

@@ -356,6 +356,16 @@ int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz) 
     return BGI_OK;
 }
 
+int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_uv_cell: null handle");
+    if (im->n_ant == 0) return set_error(BGI_ERR_STATE, "set_uv_cell: array not set");
+    if (!(delta_u > 0) || !(delta_v > 0) || !std::isfinite(delta_u) || !std::isfinite(delta_v))
+        return set_error(BGI_ERR_INVALID, "set_uv_cell: delta_u/v must be finite and > 0");
+    im->delta_u = delta_u;
+    im->delta_v = delta_v;
+    return BGI_OK;
+}
+
 int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
                     double *v_max) {
     if (!im) return set_error(BGI_ERR_INVALID, "get_uv_cell: null handle");

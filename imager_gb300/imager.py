@@ -154,6 +154,10 @@ class Imager:
         call("bgi_set_frequencies", self._h, len(f), _ptr(f))
         self.n_channels = len(f)
 
+    def set_uv_cell(self, delta_u: float, delta_v: float):
+        """Use the uv cell of a whole observation (when this handle images one shard of it)."""
+        call("bgi_set_uv_cell", self._h, float(delta_u), float(delta_v))
+
     @property
     def uv_cell(self):
         du, dv, um, vm = C.c_double(), C.c_double(), C.c_double(), C.c_double()

@@ -149,6 +149,11 @@ BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float
 /* Channel frequencies in Hz (host array, copied). */
 BGI_API int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz);
 
+/* Overrides delta_u and delta_v (metres) of the current array state, e.g. with the values of
+ * a whole observation when this handle images one shard of it (gridding_gpu takes them as
+ * arguments, src/gpu/gridding_gpu.cpp:134).  bgi_set_array recomputes them. */
+BGI_API int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v);
+
 /* delta_u, delta_v (metres) and u_max, v_max of the current array state. */
 BGI_API int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
                     double *v_max);

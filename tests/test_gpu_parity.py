@@ -331,3 +331,29 @@ def test_full_size_workload_properties(im):
         ref = O.image_f64(g, cnt)[0, 0]
         assert rel_l2(out[t, c].cpu().numpy(), ref) < IMAGE_TOL, (t, c)
     h.close()
+
+
+def test_sharded_images_equal_unsharded(im):
+    """Two shards of one block (by intervals), each on its own handle with the whole block's uv
+    cell, reproduce the unsharded images (the multi-GPU split, run here one after the other)."""
+    from imager_gb300 import shard as S
+    obs = synth.small(seed=61, n_ant=40, n_intervals=4, n_channels=3, n_pixels=64)
+    full = _imager_for(im, obs, 64)
+    ref = full.image(dev(obs.vis_f32())).cpu().numpy()
+    du, dv, _, _ = full.uv_cell
+    full.close()
+    parts, shards = [], []
+    for rank in range(2):
+        sh = S.plan_shard(4, 3, 2, rank)
+        vis, u, v, w, freqs = S.shard_inputs(obs, sh)
+        h = im.Imager(64, 2.0, "XX", -1000.0)
+        h.set_array(u, v, w, obs.flags, obs.cable)
+        h.set_frequencies(freqs)
+        h.set_uv_cell(du, dv)
+        parts.append(h.image(dev(vis.view(np.float32).reshape(vis.shape + (2,)))).cpu().numpy())
+        shards.append(sh)
+        h.close()
+    got = S.assemble(parts, shards, 4, 3, 64)
+    for i in range(4):
+        for j in range(3):
+            assert rel_l2(got[i, j], ref[i, j]) < 1e-6, (i, j)
