@@ -109,11 +109,26 @@ struct bgi_imager {
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
     int *d_flags = nullptr;
     double *d_freqs = nullptr;
-    DevBuf<float2> grid;          // wave scratch: images x N*N
+    // Two lanes (streams) image alternate waves, each with its own grid scratch, so one wave's
+    // FFT passes overlap the next wave's gridding; the scratch of a lane is reused wave after
+    // wave and sized to stay in L2.
+    static constexpr int kLanes = 2;
+    DevBuf<float2> grid[kLanes];  // wave scratch: images x N*N, zero between waves
+    bool grid_dirty[kLanes] = {false, false};
+    cudaStream_t lane[kLanes] = {nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {nullptr, nullptr};
     DevBuf<unsigned int> wsum;    // per-image weight counts of the last call
     DevBuf<float> io_vis, io_img; // device staging of bgi_image_host
-    bool grid_dirty = false;
     int last_images = 0;
+
+    int ensure_lanes() {
+        if (lane[0]) return BGI_OK;
+        for (int l = 0; l < kLanes; ++l) {
+            BGI_TRY(check_cuda(cudaStreamCreateWithFlags(&lane[l], cudaStreamNonBlocking), "lane stream"));
+            BGI_TRY(check_cuda(cudaEventCreateWithFlags(&ev_join[l], cudaEventDisableTiming), "lane event"));
+        }
+        return check_cuda(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "fork event");
+    }
     // stage timing: event quads (before gridding, after gridding, after rows, after cols)
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -287,7 +302,12 @@ int bgi_destroy(bgi_imager *im) {
     im->release_array();
     dev_free(im->d_freqs);
     for (cudaEvent_t e : im->ev_pool) cudaEventDestroy(e);
-    im->grid.release();
+    for (int l = 0; l < bgi_imager::kLanes; ++l) {
+        if (im->lane[l]) cudaStreamDestroy(im->lane[l]);
+        if (im->ev_join[l]) cudaEventDestroy(im->ev_join[l]);
+        im->grid[l].release();
+    }
+    if (im->ev_fork) cudaEventDestroy(im->ev_fork);
     im->wsum.release();
     im->io_vis.release();
     im->io_img.release();
@@ -403,19 +423,31 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     const int n_images = n_intervals * im->n_channels;
     int wave = im->cfg.max_images_per_wave;
     if (wave == 0) {
-        const size_t budget = (size_t)256 << 20;  // grid scratch bytes per wave
+        // 32 MiB of grid per lane: two lanes' scratch stays resident in the 129 MB L2
+        const size_t budget = (size_t)32 << 20;
         wave = (int)std::max<size_t>(1, budget / (npix * sizeof(float2)));
     }
     wave = std::min(wave, n_images);
-    bool fresh = false;
-    BGI_TRY(im->grid.ensure((size_t)wave * npix, "grid scratch", &fresh));
-    if (fresh || im->grid_dirty) {
-        BGI_TRY(check_cuda(cudaMemsetAsync(im->grid.ptr, 0, sizeof(float2) * im->grid.cap, s), "grid scratch clear"));
-        im->grid_dirty = false;
+    const int n_waves = (n_images + wave - 1) / wave;
+    const int n_lanes = std::min(n_waves, (int)bgi_imager::kLanes);
+    for (int l = 0; l < n_lanes; ++l) {
+        bool fresh = false;
+        BGI_TRY(im->grid[l].ensure((size_t)wave * npix, "grid scratch", &fresh));
+        if (fresh || im->grid_dirty[l]) {
+            BGI_TRY(check_cuda(cudaMemsetAsync(im->grid[l].ptr, 0, sizeof(float2) * im->grid[l].cap, s),
+                               "grid scratch clear"));
+            im->grid_dirty[l] = false;
+        }
     }
     BGI_TRY(im->wsum.ensure((size_t)n_images * kWsumStride, "weight sums"));
     BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * kWsumStride * n_images, s),
                        "weight sums clear"));
+    if (n_lanes > 1) {
+        BGI_TRY(im->ensure_lanes());
+        BGI_TRY(check_cuda(cudaEventRecord(im->ev_fork, s), "fork record"));
+        for (int l = 0; l < n_lanes; ++l)
+            BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
+    }
 
     GridParams p{};
     p.vis = vis;
@@ -425,7 +457,6 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     p.dl = im->d_dl;
     p.flags = im->d_flags;
     p.freqs = im->d_freqs;
-    p.grids = im->grid.ptr;
     p.du = im->delta_u;
     p.dv = im->delta_v;
     p.min_uv = im->cfg.min_uv;
@@ -439,21 +470,33 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
     float2 *out = reinterpret_cast<float2 *>(images);
-    for (int img0 = 0; img0 < n_images; img0 += wave) {
+    for (int k = 0; k < n_waves; ++k) {
+        const int l = k % n_lanes;
+        cudaStream_t ls = n_lanes > 1 ? im->lane[l] : s;
+        const int img0 = k * wave;
         const int cnt = std::min(wave, n_images - img0);
+        float2 *grid = im->grid[l].ptr;
+        unsigned int *ws = im->wsum.ptr + (size_t)img0 * kWsumStride;
+        p.grids = grid;
         p.img_begin = img0;
         p.img_count = cnt;
         p.img_base = img0;
-        p.wsum = im->wsum.ptr + (size_t)img0 * kWsumStride;  // indexed img - img_base
-        im->grid_dirty = true;
-        BGI_TRY(im->mark(s));
-        BGI_TRY(launch_gridding(p, s));
-        BGI_TRY(im->mark(s));
-        BGI_TRY(launch_fft_rows(im->grid.ptr, out + (size_t)img0 * npix, n, cnt, true, s));
-        im->grid_dirty = false;
-        BGI_TRY(im->mark(s));
-        BGI_TRY(launch_fft_cols(out + (size_t)img0 * npix, n, cnt, im->wsum.ptr + (size_t)img0 * kWsumStride, s));
-        BGI_TRY(im->mark(s));
+        p.wsum = ws;  // indexed img - img_base
+        im->grid_dirty[l] = true;
+        BGI_TRY(im->mark(ls));
+        BGI_TRY(launch_gridding(p, ls));
+        BGI_TRY(im->mark(ls));
+        BGI_TRY(launch_fft_rows(grid, grid, n, cnt, false, ls));  // in place in the scratch
+        BGI_TRY(im->mark(ls));
+        BGI_TRY(launch_fft_cols_to(grid, out + (size_t)img0 * npix, n, cnt, ws, true, ls));  // clears the scratch
+        BGI_TRY(im->mark(ls));
+        im->grid_dirty[l] = false;
+    }
+    if (n_lanes > 1) {
+        for (int l = 0; l < n_lanes; ++l) {
+            BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[l], im->lane[l]), "join record"));
+            BGI_TRY(check_cuda(cudaStreamWaitEvent(s, im->ev_join[l], 0), "join wait"));
+        }
     }
     im->last_images = n_images;
     return BGI_OK;

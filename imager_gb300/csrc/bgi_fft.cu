@@ -338,18 +338,18 @@ __global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(f
         [&](int i, float2 v) { d_row[i] = v; });
 }
 
-// Column pass in place on a tile pair: columns [x0, x0+CT) and their fftshift partners
-// [x0+N/2, ...).  Thread c + COLS*t runs point t of column c, so the lanes of a warp cover
-// adjacent columns and every global load and store moves whole 32-byte row segments of the
-// tile; the transforms of the COLS columns step through their passes together (block
-// barriers).  All loads of the pair happen in the first pass, before any store, so the shifted
-// stores never race with this block's loads, and no other block touches these columns.  With
-// SHIFT_NORM the stores apply the fftshift and multiply by (float)(1/sum(w)).
-template <int N, bool SHIFT_NORM>
-__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_kernel(float2 *images,
+// Column pass on a tile pair: columns [x0, x0+CT) and their fftshift partners [x0+N/2, ...).
+// Thread c + COLS*t runs point t of column c, so the lanes of a warp cover adjacent columns and
+// every global load and store moves whole 32-byte row segments of the tile; the transforms of
+// the COLS columns step through their passes together (block barriers).  All loads of the pair
+// happen in the first pass, before any store, and no other block touches these columns, so the
+// pass may run in place (src == dst) even with the fftshift.  With SHIFT_NORM the stores apply
+// the fftshift and multiply by (float)(1/sum(w)); with ZERO_SRC the loads clear src behind them
+// (src != dst), and the final stores stream past L2.
+template <int N, bool SHIFT_NORM, bool ZERO_SRC>
+__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_kernel(float2 *src, float2 *dst,
                                                                                     const unsigned int *wsum) {
     using S = ColShape<N>;
-    using C = FftCfg<N, S::R>;
     constexpr int COLS = S::COLS, CT = COLS / 2, TILES = (N / 2) / CT;
     extern __shared__ float2 smem[];
     const float2 *tw = twiddles<N, S::R>();
@@ -357,19 +357,25 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
     const int x0 = (blockIdx.x % TILES) * CT;
     const int c = threadIdx.x % COLS, t = threadIdx.x / COLS;
     const int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
-    float2 *im = images + img * (size_t)N * N;
+    float2 *in = src + img * (size_t)N * N;
+    float2 *out = dst + img * (size_t)N * N;
     float scale = 1.0f;
     if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
     const int dcol = SHIFT_NORM ? ((col + N / 2) & (N - 1)) : col;
     fft_transform<N, S::R, false, false>(
-        t, smem + c * S::STRIDE, tw, [&](int i) { return im[(size_t)i * N + col]; },
+        t, smem + c * S::STRIDE, tw,
+        [&](int i) {
+            float2 v = in[(size_t)i * N + col];
+            if (ZERO_SRC) in[(size_t)i * N + col] = make_float2(0.f, 0.f);
+            return v;
+        },
         [&](int i, float2 v) {
             int r = i;
             if (SHIFT_NORM) {
                 r = (i + N / 2) & (N - 1);
                 v = make_float2(v.x * scale, v.y * scale);
             }
-            __stcs(im + (size_t)r * N + dcol, v);
+            __stcs(out + (size_t)r * N + dcol, v);
         });
 }
 
@@ -395,14 +401,15 @@ int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStre
 }
 
 template <int N>
-int cols_n(float2 *images, int n_images, const unsigned int *wsum, cudaStream_t s) {
+int cols_n(float2 *src, float2 *dst, int n_images, const unsigned int *wsum, bool zero_src, cudaStream_t s) {
     using S = ColShape<N>;
     const size_t smem = sizeof(float2) * ((size_t)S::COLS * S::STRIDE);
     const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / (S::COLS / 2));
-    auto k = wsum ? fft_cols_kernel<N, true> : fft_cols_kernel<N, false>;
+    auto k = wsum ? (zero_src ? fft_cols_kernel<N, true, true> : fft_cols_kernel<N, true, false>)
+                  : (zero_src ? fft_cols_kernel<N, false, true> : fft_cols_kernel<N, false, false>);
     int st = prepare(k, smem);
     if (st) return st;
-    k<<<blocks, S::COLS * S::P, smem, s>>>(images, wsum);
+    k<<<blocks, S::COLS * S::P, smem, s>>>(src, dst, wsum);
     return check_launch("fft cols");
 }
 
@@ -489,17 +496,23 @@ int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool ze
 
 int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsum,
                     cudaStream_t s) {
+    return launch_fft_cols_to(images, images, n, n_images, wsum, false, s);
+}
+
+int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsigned int *wsum,
+                       bool zero_src, cudaStream_t s) {
     if (n_images <= 0) return BGI_OK;
+    if (zero_src && src == dst) return set_error(BGI_ERR_INVALID, "fft cols: clearing the source needs src != dst");
     switch (n) {
-        case 16: return cols_n<16>(images, n_images, wsum, s);
-        case 32: return cols_n<32>(images, n_images, wsum, s);
-        case 64: return cols_n<64>(images, n_images, wsum, s);
-        case 128: return cols_n<128>(images, n_images, wsum, s);
-        case 256: return cols_n<256>(images, n_images, wsum, s);
-        case 512: return cols_n<512>(images, n_images, wsum, s);
-        case 1024: return cols_n<1024>(images, n_images, wsum, s);
-        case 2048: return cols_n<2048>(images, n_images, wsum, s);
-        case 4096: return cols_n<4096>(images, n_images, wsum, s);
+        case 16: return cols_n<16>(src, dst, n_images, wsum, zero_src, s);
+        case 32: return cols_n<32>(src, dst, n_images, wsum, zero_src, s);
+        case 64: return cols_n<64>(src, dst, n_images, wsum, zero_src, s);
+        case 128: return cols_n<128>(src, dst, n_images, wsum, zero_src, s);
+        case 256: return cols_n<256>(src, dst, n_images, wsum, zero_src, s);
+        case 512: return cols_n<512>(src, dst, n_images, wsum, zero_src, s);
+        case 1024: return cols_n<1024>(src, dst, n_images, wsum, zero_src, s);
+        case 2048: return cols_n<2048>(src, dst, n_images, wsum, zero_src, s);
+        case 4096: return cols_n<4096>(src, dst, n_images, wsum, zero_src, s);
         default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
     }
 }

@@ -48,6 +48,10 @@ int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool ze
 // (float)(1/wsum[i * kWsumStride]).
 int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsum,
                     cudaStream_t s);
+// Column pass from src into dst (src == dst: in place); zero_src clears src behind the loads
+// (needs src != dst).  Final stores stream past L2.
+int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsigned int *wsum,
+                       bool zero_src, cudaStream_t s);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
                           const float *fnorm, int fnorm_size, cudaStream_t s);
 int launch_vector_sum(const float *data, int64_t image_size, int n_images, float *sums,
