@@ -121,6 +121,28 @@ struct bgi_imager {
     DevBuf<float> io_vis, io_img; // device staging of bgi_image_host
     int last_images = 0;
 
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    std::vector<cudaEvent_t> ev_in, ev_done;  // per chunk of bgi_image_host
+
+    int ensure_copy_streams() {
+        if (copy_in) return BGI_OK;
+        BGI_TRY(check_cuda(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking), "copy stream"));
+        return check_cuda(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking), "copy stream");
+    }
+    int ensure_chunk_events(int n_chunks) {
+        while ((int)ev_in.size() < n_chunks) {
+            cudaEvent_t e;
+            BGI_TRY(check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "chunk event"));
+            ev_in.push_back(e);
+        }
+        while ((int)ev_done.size() < n_chunks * kLanes) {
+            cudaEvent_t e;
+            BGI_TRY(check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "chunk event"));
+            ev_done.push_back(e);
+        }
+        return BGI_OK;
+    }
+
     int ensure_lanes() {
         if (lane[0]) return BGI_OK;
         for (int l = 0; l < kLanes; ++l) {
@@ -308,6 +330,10 @@ int bgi_destroy(bgi_imager *im) {
         im->grid[l].release();
     }
     if (im->ev_fork) cudaEventDestroy(im->ev_fork);
+    for (cudaEvent_t e : im->ev_in) cudaEventDestroy(e);
+    for (cudaEvent_t e : im->ev_done) cudaEventDestroy(e);
+    if (im->copy_in) cudaStreamDestroy(im->copy_in);
+    if (im->copy_out) cudaStreamDestroy(im->copy_out);
     im->wsum.release();
     im->io_vis.release();
     im->io_img.release();
@@ -410,17 +436,15 @@ static int image_checks(bgi_imager *im, int n_intervals, unsigned flags) {
     return BGI_OK;
 }
 
-int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
-              void *stream) {
-    BGI_TRY(image_checks(im, n_intervals, flags));
-    if (!vis || !images) return set_error(BGI_ERR_INVALID, "image: null buffer");
-    if (!aligned16(vis) || (reinterpret_cast<uintptr_t>(images) & 7u) != 0)
-        return set_error(BGI_ERR_INVALID, "image: vis must be 16-byte and images 8-byte aligned");
-    BGI_TRY(im->activate());
-    cudaStream_t s = as_stream(stream);
+}  // extern "C"
+
+namespace {
+
+// Per-call set-up on stream s: wave size, grid scratch of the lanes in use (cleared when new or
+// left dirty by a failed call), weight counters of every image cleared.
+int prepare_call(bgi_imager *im, int n_images, cudaStream_t s, int *wave_out, int *lanes_out) {
     const int n = im->cfg.n_pixels;
     const size_t npix = (size_t)n * n;
-    const int n_images = n_intervals * im->n_channels;
     int wave = im->cfg.max_images_per_wave;
     if (wave == 0) {
         // 32 MiB of grid per lane: two lanes' scratch stays resident in the 129 MB L2
@@ -442,13 +466,12 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     BGI_TRY(im->wsum.ensure((size_t)n_images * kWsumStride, "weight sums"));
     BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * kWsumStride * n_images, s),
                        "weight sums clear"));
-    if (n_lanes > 1) {
-        BGI_TRY(im->ensure_lanes());
-        BGI_TRY(check_cuda(cudaEventRecord(im->ev_fork, s), "fork record"));
-        for (int l = 0; l < n_lanes; ++l)
-            BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
-    }
+    *wave_out = wave;
+    *lanes_out = n_lanes;
+    return BGI_OK;
+}
 
+GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals, unsigned flags) {
     GridParams p{};
     p.vis = vis;
     p.u = im->d_u;
@@ -464,17 +487,26 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     p.n_channels = im->n_channels;
     p.n_intervals = n_intervals;
     p.n_uvw_sets = im->n_uvw_sets;
-    p.n_pixels = n;
+    p.n_pixels = im->cfg.n_pixels;
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
-    float2 *out = reinterpret_cast<float2 *>(images);
-    for (int k = 0; k < n_waves; ++k) {
-        const int l = k % n_lanes;
-        cudaStream_t ls = n_lanes > 1 ? im->lane[l] : s;
-        const int img0 = k * wave;
-        const int cnt = std::min(wave, n_images - img0);
+    return p;
+}
+
+// Images [img_first, img_first + count) of a block, in waves of `wave` images that alternate on
+// streams[0..n_streams) starting at stream *next.  Per wave: gridding into the stream's grid
+// scratch, the row pass in place, the column pass into the images (clearing the scratch).
+int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int count, int wave,
+              cudaStream_t *streams, int n_streams, int *next) {
+    const int n = im->cfg.n_pixels;
+    const size_t npix = (size_t)n * n;
+    for (int img0 = img_first; img0 < img_first + count; img0 += wave) {
+        const int l = *next;
+        *next = (*next + 1) % n_streams;
+        cudaStream_t ls = streams[l];
+        const int cnt = std::min(wave, img_first + count - img0);
         float2 *grid = im->grid[l].ptr;
         unsigned int *ws = im->wsum.ptr + (size_t)img0 * kWsumStride;
         p.grids = grid;
@@ -492,6 +524,36 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
         BGI_TRY(im->mark(ls));
         im->grid_dirty[l] = false;
     }
+    return BGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
+              void *stream) {
+    BGI_TRY(image_checks(im, n_intervals, flags));
+    if (!vis || !images) return set_error(BGI_ERR_INVALID, "image: null buffer");
+    if (!aligned16(vis) || (reinterpret_cast<uintptr_t>(images) & 7u) != 0)
+        return set_error(BGI_ERR_INVALID, "image: vis must be 16-byte and images 8-byte aligned");
+    BGI_TRY(im->activate());
+    cudaStream_t s = as_stream(stream);
+    const int n_images = n_intervals * im->n_channels;
+    int wave = 0, n_lanes = 0;
+    BGI_TRY(prepare_call(im, n_images, s, &wave, &n_lanes));
+    cudaStream_t streams[bgi_imager::kLanes] = {s, s};
+    if (n_lanes > 1) {
+        BGI_TRY(im->ensure_lanes());
+        BGI_TRY(check_cuda(cudaEventRecord(im->ev_fork, s), "fork record"));
+        for (int l = 0; l < n_lanes; ++l) {
+            streams[l] = im->lane[l];
+            BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
+        }
+    }
+    int next = 0;
+    BGI_TRY(run_waves(im, block_params(im, vis, n_intervals, flags), reinterpret_cast<float2 *>(images), 0,
+                      n_images, wave, streams, n_lanes, &next));
     if (n_lanes > 1) {
         for (int l = 0; l < n_lanes; ++l) {
             BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[l], im->lane[l]), "join record"));
@@ -502,22 +564,60 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     return BGI_OK;
 }
 
+// Host buffers: the block is cut into chunks of whole waves; each chunk's visibilities go up on
+// a copy stream, its waves run on the lanes as soon as they have landed, and its images come
+// back on a second copy stream as soon as they are done, so uploads, imaging and downloads of
+// different chunks overlap.
 int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsigned flags,
                    float *images_host, void *stream) {
     BGI_TRY(image_checks(im, n_intervals, flags));
     if (!vis_host || !images_host) return set_error(BGI_ERR_INVALID, "image_host: null buffer");
     BGI_TRY(im->activate());
     cudaStream_t s = as_stream(stream);
-    const size_t n_images = (size_t)n_intervals * im->n_channels;
-    const size_t vis_floats = n_images * (size_t)im->n_baselines * 8;
-    const size_t img_floats = n_images * (size_t)im->cfg.n_pixels * im->cfg.n_pixels * 2;
-    BGI_TRY(im->io_vis.ensure(vis_floats, "image_host vis staging"));
-    BGI_TRY(im->io_img.ensure(img_floats, "image_host image staging"));
-    BGI_TRY(check_cuda(cudaMemcpyAsync(im->io_vis.ptr, vis_host, sizeof(float) * vis_floats,
-                                       cudaMemcpyHostToDevice, s), "image_host H2D"));
-    BGI_TRY(bgi_image(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, stream));
-    BGI_TRY(check_cuda(cudaMemcpyAsync(images_host, im->io_img.ptr, sizeof(float) * img_floats,
-                                       cudaMemcpyDeviceToHost, s), "image_host D2H"));
+    const int n_images = n_intervals * im->n_channels;
+    const size_t rec_floats = (size_t)im->n_baselines * 8;  // one image's visibility records
+    const size_t img_floats = (size_t)im->cfg.n_pixels * im->cfg.n_pixels * 2;
+    BGI_TRY(im->io_vis.ensure(rec_floats * n_images, "image_host vis staging"));
+    BGI_TRY(im->io_img.ensure(img_floats * n_images, "image_host image staging"));
+    int wave = 0, n_lanes = 0;
+    BGI_TRY(prepare_call(im, n_images, s, &wave, &n_lanes));
+    BGI_TRY(im->ensure_lanes());
+    BGI_TRY(im->ensure_copy_streams());
+    // about eight chunks of whole waves
+    const int waves_total = (n_images + wave - 1) / wave;
+    const int chunk = wave * std::max(1, (waves_total + 7) / 8);
+    const int n_chunks = (n_images + chunk - 1) / chunk;
+    BGI_TRY(im->ensure_chunk_events(n_chunks));
+    BGI_TRY(check_cuda(cudaEventRecord(im->ev_fork, s), "fork record"));
+    BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_in, im->ev_fork, 0), "fork wait"));
+    BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_out, im->ev_fork, 0), "fork wait"));
+    for (int l = 0; l < n_lanes; ++l)
+        BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
+    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags);
+    int next = 0;
+    for (int c = 0; c < n_chunks; ++c) {
+        const int img0 = c * chunk;
+        const int cnt = std::min(chunk, n_images - img0);
+        BGI_TRY(check_cuda(cudaMemcpyAsync(im->io_vis.ptr + rec_floats * img0, vis_host + rec_floats * img0,
+                                           sizeof(float) * rec_floats * cnt, cudaMemcpyHostToDevice, im->copy_in),
+                           "image_host H2D"));
+        BGI_TRY(check_cuda(cudaEventRecord(im->ev_in[c], im->copy_in), "chunk in record"));
+        for (int l = 0; l < n_lanes; ++l)
+            BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_in[c], 0), "chunk in wait"));
+        BGI_TRY(run_waves(im, p, reinterpret_cast<float2 *>(im->io_img.ptr), img0, cnt, wave, im->lane, n_lanes,
+                          &next));
+        for (int l = 0; l < n_lanes; ++l) {
+            BGI_TRY(check_cuda(cudaEventRecord(im->ev_done[c * bgi_imager::kLanes + l], im->lane[l]), "chunk done"));
+            BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_out, im->ev_done[c * bgi_imager::kLanes + l], 0),
+                               "chunk done wait"));
+        }
+        BGI_TRY(check_cuda(cudaMemcpyAsync(images_host + img_floats * img0, im->io_img.ptr + img_floats * img0,
+                                           sizeof(float) * img_floats * cnt, cudaMemcpyDeviceToHost, im->copy_out),
+                           "image_host D2H"));
+    }
+    BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[0], im->copy_out), "join record"));
+    BGI_TRY(check_cuda(cudaStreamWaitEvent(s, im->ev_join[0], 0), "join wait"));
+    im->last_images = n_images;
     return check_cuda(cudaStreamSynchronize(s), "image_host sync");
 }
 

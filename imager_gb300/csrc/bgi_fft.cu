@@ -300,7 +300,7 @@ __device__ __forceinline__ const float2 *twiddles() {
 // barriers, transforms per row-pass block, columns per column-pass block (a tile pair).
 template <int N>
 struct Shape {
-    static constexpr int R = N <= 128 ? 8 : N <= 512 ? 16 : N == 1024 ? 32 : 16;
+    static constexpr int R = N <= 128 ? 8 : N <= 256 ? 16 : N <= 1024 ? 32 : 16;
     static constexpr int P = N / R;
     static constexpr bool WARP = P <= 32;
     static constexpr int ROWS = WARP ? ((256 / P) < N ? (256 / P) : N) : 256 / P;

@@ -357,3 +357,17 @@ def test_sharded_images_equal_unsharded(im):
     for i in range(4):
         for j in range(3):
             assert rel_l2(got[i, j], ref[i, j]) < 1e-6, (i, j)
+
+
+def test_image_host_many_chunks_equals_device(im):
+    """bgi_image_host cuts the block into chunks whose uploads, waves and downloads overlap;
+    with a 2-image wave, 24 images make 12 waves in 6 chunks over both lanes."""
+    obs = synth.small(seed=63, n_ant=40, n_intervals=3, n_channels=8, n_pixels=128)
+    h = _imager_for(im, obs, 128, wave=2)
+    vis = np.ascontiguousarray(obs.vis_f32())
+    dev_out = h.image(dev(vis)).cpu().numpy()
+    host_out = h.image_host(vis)
+    sums = h.weight_sums(24)
+    assert rel_l2(host_out, dev_out) < 1e-6
+    assert np.all(sums == 2 * int((obs.flags == 0).sum()))
+    h.close()
