@@ -28,7 +28,8 @@ class BgiError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("n_pixels", C.c_int), ("oversampling_factor", C.c_float), ("pol", C.c_int),
-                ("min_uv", C.c_double), ("max_images_per_wave", C.c_int), ("device", C.c_int)]
+                ("min_uv", C.c_double), ("max_images_per_wave", C.c_int), ("device", C.c_int),
+                ("full_plane", C.c_int)]
 
 
 _vp, _i, _i64, _d, _f, _u = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_float, C.c_uint
@@ -47,6 +48,7 @@ _SIGNATURES = {
     "bgi_destroy": (_i, [_vp]),
     "bgi_set_array": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "bgi_set_frequencies": (_i, [_vp, _i, _vp]),
+    "bgi_half_plane": (_i, [_vp]),
     "bgi_set_uv_cell": (_i, [_vp, _d, _d]),
     "bgi_get_uv_cell": (_i, [_vp, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     "bgi_image": (_i, [_vp, _vp, _i, _u, _vp, _vp]),

@@ -5,6 +5,7 @@
 // and runs the fused path: per wave of images, one gridding launch (corrections fused), one
 // row-FFT launch (which also re-zeroes the grid scratch) and one column-FFT launch (fftshift
 // and 1/sum(weights) fused into its stores).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -105,6 +106,17 @@ struct bgi_imager {
     int n_ant = 0, n_uvw_sets = 0, n_channels = 0;
     long long n_baselines = 0;
     double u_max = 0, v_max = 0, delta_u = 0, delta_v = 0;
+    double freq_max = 0;  // highest channel frequency (Hz)
+
+    // The half-plane path needs every gridded point's mirror cell: |u|,|v| pixels < N.  The
+    // largest pixel coordinate is u_max * nu_max / (c * delta_u); one pixel of margin covers
+    // the rounding of the FP64 recipe.
+    bool half_plane() const {
+        if (cfg.full_plane || half_plane_width(cfg.n_pixels) == 0 || freq_max <= 0) return false;
+        const double up = u_max * freq_max / (kVelLight * delta_u);
+        const double vp = v_max * freq_max / (kVelLight * delta_v);
+        return up < cfg.n_pixels - 1 && vp < cfg.n_pixels - 1;
+    }
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
     int *d_flags = nullptr;
@@ -399,7 +411,15 @@ int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz) 
     BGI_TRY(check_cuda(cudaMemcpy(im->d_freqs, freqs_hz, sizeof(double) * n_channels, cudaMemcpyHostToDevice),
                        "set_frequencies copy"));
     im->n_channels = n_channels;
+    im->freq_max = *std::max_element(freqs_hz, freqs_hz + n_channels);
     return BGI_OK;
+}
+
+int bgi_half_plane(const bgi_imager *im) {
+    if (!im) return set_error(BGI_ERR_INVALID, "half_plane: null handle");
+    if (im->n_ant == 0 || im->n_channels == 0)
+        return set_error(BGI_ERR_STATE, "half_plane: set_array and set_frequencies first");
+    return im->half_plane() ? 1 : 0;
 }
 
 int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v) {
@@ -490,6 +510,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.n_pixels = im->cfg.n_pixels;
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
+    p.half_width = im->half_plane() ? half_plane_width(im->cfg.n_pixels) : 0;
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
     return p;
@@ -518,9 +539,15 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         BGI_TRY(im->mark(ls));
         BGI_TRY(launch_gridding(p, ls));
         BGI_TRY(im->mark(ls));
-        BGI_TRY(launch_fft_rows(grid, grid, n, cnt, false, ls));  // in place in the scratch
-        BGI_TRY(im->mark(ls));
-        BGI_TRY(launch_fft_cols_to(grid, out + (size_t)img0 * npix, n, cnt, ws, true, ls));  // clears the scratch
+        if (p.half_width > 0) {
+            BGI_TRY(launch_fft_cols_half(grid, n, cnt, ls));                   // in place, rows shifted
+            BGI_TRY(im->mark(ls));
+            BGI_TRY(launch_c2r_rows(grid, out + (size_t)img0 * npix, n, cnt, ws, ls));  // clears the scratch
+        } else {
+            BGI_TRY(launch_fft_rows(grid, grid, n, cnt, false, ls));  // in place in the scratch
+            BGI_TRY(im->mark(ls));
+            BGI_TRY(launch_fft_cols_to(grid, out + (size_t)img0 * npix, n, cnt, ws, true, ls));  // clears the scratch
+        }
         BGI_TRY(im->mark(ls));
         im->grid_dirty[l] = false;
     }

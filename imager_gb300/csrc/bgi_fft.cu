@@ -379,6 +379,102 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
         });
 }
 
+// ---- half-plane path: real images of Hermitian grids ---------------------------------------
+// A grid that holds every visibility and its conjugate at the mirrored cell is Hermitian, so its
+// inverse transform is real.  Only columns u = 0..N/2 are kept (width W = N/2 + one column tile,
+// the padding columns stay zero); the column pass transforms those along v, and each row is
+// then finished by a complex-to-real transform of length N built on a complex FFT of length N/2:
+// with M = N/2 and w = exp(+2*pi*i*k/N), Z[k] = X[k](1 + i w) + conj(X[M-k])(1 - i w) for
+// k < M, z = IDFT_M(Z), and the image row is x[2m] = Re z[m], x[2m+1] = Im z[m].
+
+// exp(+2*pi*i*k/N) for k < N/2 (compile-time, as the pass tables).
+template <int N>
+struct ZTwData {
+    TwEntry v[N / 2];
+};
+template <int N>
+constexpr ZTwData<N> make_z_twiddles() {
+    ZTwData<N> d{};
+    for (int k = 0; k < N / 2; ++k) d.v[k] = twiddle_exact(k, N);
+    return d;
+}
+template <int N>
+__device__ const ZTwData<N> g_z_twiddles = make_z_twiddles<N>();
+
+template <int N>
+constexpr int half_width_of() { return N / 2 + ColShape<N>::COLS; }
+
+// Column pass of half-plane grids [img][N][W], in place: tiles of COLS adjacent columns, lanes
+// across the columns (coalesced row segments), transforms stepping together (block barriers);
+// row y is stored at (y + N/2) mod N, the fftshift of rows.
+template <int N>
+__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_half_kernel(float2 *grids) {
+    using S = ColShape<N>;
+    constexpr int COLS = S::COLS, W = half_width_of<N>(), TILES = W / COLS;
+    extern __shared__ float2 smem[];
+    const float2 *tw = twiddles<N, S::R>();
+    const size_t img = blockIdx.x / TILES;
+    const int x0 = (blockIdx.x % TILES) * COLS;
+    const int c = threadIdx.x % COLS, t = threadIdx.x / COLS;
+    float2 *g = grids + img * (size_t)N * W + x0 + c;
+    fft_transform<N, S::R, false, false>(
+        t, smem + c * S::STRIDE, tw, [&](int i) { return g[(size_t)i * W]; },
+        [&](int i, float2 v) { g[(size_t)((i + N / 2) & (N - 1)) * W] = v; });
+}
+
+// Complex-to-real row pass shape: transforms of length M = N/2.
+template <int N>
+struct C2RShape {
+    static constexpr int M = N / 2;
+    static constexpr int R = Shape<M>::R;
+    static constexpr int P = M / R;
+    static constexpr bool WARP = P <= 32;
+    static constexpr int ROWS = WARP ? ((256 / P) < N ? (256 / P) : N) : 256 / P;
+    static constexpr int LEN = FftCfg<M, R>::LEN;
+    static constexpr int BUF = ((LEN > M + 1 ? LEN : M + 1) + 1) & ~1;
+};
+
+// Complex-to-real pass: half-plane row y (already at its fftshifted position) -> image row y.
+// The row's N/2 + 1 values are staged in shared memory and cleared in the grid behind the
+// loads; the first pass forms Z[k] from X[k] and X[M-k]; the stores apply the fftshift of
+// columns (x -> (x + N/2) mod N keeps pairs 2m, 2m+1 together) and (float)(1/sum(w)), and
+// write complex pixels with zero imaginary parts, streaming past L2.
+template <int N>
+__global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
+                                                                                    const unsigned int *wsum) {
+    using S = C2RShape<N>;
+    constexpr int M = S::M, W = half_width_of<N>();
+    extern __shared__ float2 smem[];
+    const float2 *tw = twiddles<M, S::R>();
+    const float2 *wz = reinterpret_cast<const float2 *>(g_z_twiddles<N>.v);
+    const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
+    const size_t row = (size_t)blockIdx.x * S::ROWS + slot;
+    const size_t img = row / N;
+    float2 *src = grids + row * W;
+    float2 *buf = smem + slot * S::BUF;
+    for (int k = t; k <= M; k += S::P) {
+        buf[k] = src[k];
+        src[k] = make_float2(0.f, 0.f);
+    }
+    fft_sync<S::WARP>();
+    const float scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
+    float2 *dst = images + row * N;
+    fft_transform<M, S::R, S::WARP, false>(
+        t, buf, tw,
+        [&](int k) {
+            const float2 a = buf[k], b = buf[M - k], w = __ldg(wz + k);
+            // a * (1 + i w) + conj(b) * (1 - i w)
+            const float pr = 1.f - w.y, pi = w.x, qr = 1.f + w.y, qi = -w.x;
+            const float br = b.x, bi = -b.y;
+            return make_float2(a.x * pr - a.y * pi + br * qr - bi * qi, a.x * pi + a.y * pr + br * qi + bi * qr);
+        },
+        [&](int m, float2 z) {
+            const int x = (2 * m + N / 2) & (N - 1);
+            __stcs(dst + x, make_float2(z.x * scale, 0.f));
+            __stcs(dst + x + 1, make_float2(z.y * scale, 0.f));
+        });
+}
+
 template <class K>
 int prepare(K kernel, size_t smem) {
     if (smem > 48 * 1024) {
@@ -411,6 +507,30 @@ int cols_n(float2 *src, float2 *dst, int n_images, const unsigned int *wsum, boo
     if (st) return st;
     k<<<blocks, S::COLS * S::P, smem, s>>>(src, dst, wsum);
     return check_launch("fft cols");
+}
+
+template <int N>
+int cols_half_n(float2 *grids, int n_images, cudaStream_t s) {
+    using S = ColShape<N>;
+    const size_t smem = sizeof(float2) * ((size_t)S::COLS * S::STRIDE);
+    const unsigned blocks = (unsigned)((size_t)n_images * (half_width_of<N>() / S::COLS));
+    auto k = fft_cols_half_kernel<N>;
+    int st = prepare(k, smem);
+    if (st) return st;
+    k<<<blocks, S::COLS * S::P, smem, s>>>(grids);
+    return check_launch("fft cols (half plane)");
+}
+
+template <int N>
+int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, cudaStream_t s) {
+    using S = C2RShape<N>;
+    const size_t smem = sizeof(float2) * ((size_t)S::ROWS * S::BUF);
+    const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
+    auto k = c2r_rows_kernel<N>;
+    int st = prepare(k, smem);
+    if (st) return st;
+    k<<<blocks, S::ROWS * S::P, smem, s>>>(grids, images, wsum);
+    return check_launch("fft rows (complex to real)");
 }
 
 // ---- src/gpu/gpu_utils.cpp:73-123: fftshift by half swaps, then divide -------------------
@@ -514,6 +634,51 @@ int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsi
         case 2048: return cols_n<2048>(src, dst, n_images, wsum, zero_src, s);
         case 4096: return cols_n<4096>(src, dst, n_images, wsum, zero_src, s);
         default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
+    }
+}
+
+int half_plane_width(int n) {
+    switch (n) {
+        case 32: return half_width_of<32>();
+        case 64: return half_width_of<64>();
+        case 128: return half_width_of<128>();
+        case 256: return half_width_of<256>();
+        case 512: return half_width_of<512>();
+        case 1024: return half_width_of<1024>();
+        case 2048: return half_width_of<2048>();
+        case 4096: return half_width_of<4096>();
+        default: return 0;  // no half-plane path for this side
+    }
+}
+
+int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s) {
+    if (n_images <= 0) return BGI_OK;
+    switch (n) {
+        case 32: return cols_half_n<32>(grids, n_images, s);
+        case 64: return cols_half_n<64>(grids, n_images, s);
+        case 128: return cols_half_n<128>(grids, n_images, s);
+        case 256: return cols_half_n<256>(grids, n_images, s);
+        case 512: return cols_half_n<512>(grids, n_images, s);
+        case 1024: return cols_half_n<1024>(grids, n_images, s);
+        case 2048: return cols_half_n<2048>(grids, n_images, s);
+        case 4096: return cols_half_n<4096>(grids, n_images, s);
+        default: return set_error(BGI_ERR_UNSUPPORTED, "half-plane image side %d", n);
+    }
+}
+
+int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
+                    cudaStream_t s) {
+    if (n_images <= 0) return BGI_OK;
+    switch (n) {
+        case 32: return c2r_n<32>(grids, images, n_images, wsum, s);
+        case 64: return c2r_n<64>(grids, images, n_images, wsum, s);
+        case 128: return c2r_n<128>(grids, images, n_images, wsum, s);
+        case 256: return c2r_n<256>(grids, images, n_images, wsum, s);
+        case 512: return c2r_n<512>(grids, images, n_images, wsum, s);
+        case 1024: return c2r_n<1024>(grids, images, n_images, wsum, s);
+        case 2048: return c2r_n<2048>(grids, images, n_images, wsum, s);
+        case 4096: return c2r_n<4096>(grids, images, n_images, wsum, s);
+        default: return set_error(BGI_ERR_UNSUPPORTED, "half-plane image side %d", n);
     }
 }
 

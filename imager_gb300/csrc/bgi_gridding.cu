@@ -21,7 +21,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kCPT = 4;  // images per thread
 
-template <int POL, bool COUNTERS>
+template <int POL, bool COUNTERS, bool HALF>
 __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
     __shared__ ChannelConst s_cc[kCPT];
     __shared__ unsigned int s_count[kCPT];
@@ -88,8 +88,20 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
                 z = rotate(z, phasor_df(d_hi, d_lo, cc.f_hi, cc.f_lo));
             }
             int ui, vi;
-            if (!isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
-                uv_pixels(uu[j], vv[j], cc, p.du, p.dv, p.min_uv, min_uv_active, &ui, &vi)) {
+            const bool gridded = !isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
+                                 uv_pixels(uu[j], vv[j], cc, p.du, p.dv, p.min_uv, min_uv_active, &ui, &vi);
+            if (HALF && gridded) {
+                // half-plane grid: keep each of the two points whose u index is <= N/2 (the
+                // caller guarantees |u|,|v| pixels < N, so both cells exist and are each
+                // other's mirror)
+                const int w = p.half_width;
+                float2 *grid = p.grids + (size_t)local * n * w;
+                const int u1 = wrap_index(ui, n), v1 = wrap_index(vi, n);
+                const int u2 = wrap_index(-ui, n), v2 = wrap_index(-vi, n);
+                if (u1 <= n / 2) atomicAdd(grid + (size_t)v1 * w + u1, z);
+                if (u2 <= n / 2) atomicAdd(grid + (size_t)v2 * w + u2, make_float2(z.x, -z.y));
+                counted += 2;
+            } else if (gridded) {
                 const long long pos = cell_pos(ui, vi, +1, n);
                 const long long pos2 = cell_pos(ui, vi, -1, n);
                 float2 *grid = p.grids + (size_t)local * npix;
@@ -125,8 +137,9 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
 
 template <int POL>
 void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
-    if (q.counter_mode >= 0) grid_kernel<POL, true><<<grid, kThreads, 0, s>>>(q);
-    else grid_kernel<POL, false><<<grid, kThreads, 0, s>>>(q);
+    if (q.half_width > 0) grid_kernel<POL, false, true><<<grid, kThreads, 0, s>>>(q);
+    else if (q.counter_mode >= 0) grid_kernel<POL, true, false><<<grid, kThreads, 0, s>>>(q);
+    else grid_kernel<POL, false, false><<<grid, kThreads, 0, s>>>(q);
 }
 
 }  // namespace

@@ -35,6 +35,7 @@ struct GridParams {
     int img_begin, img_count;  // images [img_begin, img_begin + img_count) of the block
     int img_base;              // grids/wsum index = img - img_base
     int counter_mode;          // -1 none, 0 first interval, 1 per image
+    int half_width;            // 0: full N x N grids; W > 0: half-plane grids [N][W], u <= N/2
     int apply_geom, apply_cable;
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
@@ -52,6 +53,16 @@ int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsu
 // (needs src != dst).  Final stores stream past L2.
 int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsigned int *wsum,
                        bool zero_src, cudaStream_t s);
+// Half-plane imaging (real images of Hermitian grids): grids [img][N][W] hold columns
+// u = 0..N/2 (W = half_plane_width(N), padding columns stay zero).
+int half_plane_width(int n);
+// Column pass in place on half-plane grids, storing row y at (y + N/2) mod N.
+int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s);
+// Complex-to-real row pass: half-plane rows -> image rows (fftshift of columns and
+// (float)(1/wsum) applied), clearing the grid rows it read.  Images are complex with zero
+// imaginary parts.
+int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
+                    cudaStream_t s);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
                           const float *fnorm, int fnorm_size, cudaStream_t s);
 int launch_vector_sum(const float *data, int64_t image_size, int n_images, float *sums,

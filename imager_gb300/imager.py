@@ -117,10 +117,11 @@ class Imager:
     """Resident-state imager (CPacerImagerHip's members, src/gpu/pacer_imager_hip.h:14-27)."""
 
     def __init__(self, n_pixels: int, oversampling_factor: float = 2.0, pol="XX",
-                 min_uv: float = -math.inf, max_images_per_wave: int = 0, device: int = 0):
+                 min_uv: float = -math.inf, max_images_per_wave: int = 0, device: int = 0,
+                 full_plane: bool = False):
         cfg = capi.Config(int(n_pixels), float(oversampling_factor),
                           POL[pol] if isinstance(pol, str) else int(pol), float(min_uv),
-                          int(max_images_per_wave), int(device))
+                          int(max_images_per_wave), int(device), int(bool(full_plane)))
         h = C.c_void_p()
         call("bgi_create", C.byref(cfg), C.byref(h))
         self._h = h
@@ -153,6 +154,13 @@ class Imager:
         f = np.ascontiguousarray(freqs, np.float64)
         call("bgi_set_frequencies", self._h, len(f), _ptr(f))
         self.n_channels = len(f)
+
+    @property
+    def half_plane(self) -> bool:
+        """Whether image() takes the half-plane (complex-to-real) path for the current state."""
+        st = capi.lib().bgi_half_plane(self._h)
+        capi.check(min(st, 0))
+        return bool(st)
 
     def set_uv_cell(self, delta_u: float, delta_v: float):
         """Use the uv cell of a whole observation (when this handle images one shard of it)."""

@@ -133,6 +133,10 @@ typedef struct bgi_config {
     double min_uv;             /* uv distance cut in wavelengths (strictly greater passes) */
     int max_images_per_wave;   /* images gridded and transformed per launch wave; 0 = auto */
     int device;                /* CUDA device ordinal */
+    int full_plane;            /* 1: always transform the full N x N grid; 0: when every pixel
+                                  coordinate is below N, grid only the half plane u <= N/2 and
+                                  finish with a complex-to-real transform (the grid is
+                                  Hermitian, so the image is real: same images, half the work) */
 } bgi_config;
 
 BGI_API int bgi_create(const bgi_config *cfg, bgi_imager **out);
@@ -148,6 +152,10 @@ BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float
 
 /* Channel frequencies in Hz (host array, copied). */
 BGI_API int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz);
+
+/* 1 when bgi_image would take the half-plane path for the current array, frequencies and
+ * configuration, 0 when it would transform the full plane; negative status on error. */
+BGI_API int bgi_half_plane(const bgi_imager *im);
 
 /* Overrides delta_u and delta_v (metres) of the current array state, e.g. with the values of
  * a whole observation when this handle images one shard of it (gridding_gpu takes them as

@@ -228,21 +228,23 @@ def test_image_averaging_known_answer(im):
 # ------------------------------------------------------------------------------------------
 # whole path (bgi_image)
 # ------------------------------------------------------------------------------------------
-def _imager_for(im, obs, n, pol="XX", min_uv=-1000.0, wave=0):
-    h = im.Imager(n, 2.0, pol, min_uv, max_images_per_wave=wave)
+def _imager_for(im, obs, n, pol="XX", min_uv=-1000.0, wave=0, full_plane=False):
+    h = im.Imager(n, 2.0, pol, min_uv, max_images_per_wave=wave, full_plane=full_plane)
     h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
     h.set_frequencies(obs.freqs)
     return h
 
 
+@pytest.mark.parametrize("full_plane", [False, True])
 @pytest.mark.parametrize("pol", ["XX", "YY", "I", "V"])
 @pytest.mark.parametrize("n,wave", [(64, 0), (128, 2)])
-def test_image_against_oracle(im, pol, n, wave):
+def test_image_against_oracle(im, pol, n, wave, full_plane):
     obs = synth.small(seed=41, n_ant=40, n_intervals=2, n_channels=3, n_pixels=n)
     vis = obs.vis_f32()
     _, _, counters, ref, (du, dv) = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags,
                                                     obs.freqs, n, pol=pol, n_uvw_sets=2)
-    h = _imager_for(im, obs, n, pol, wave=wave)
+    h = _imager_for(im, obs, n, pol, wave=wave, full_plane=full_plane)
+    assert h.half_plane == (not full_plane)
     assert h.uv_cell[:2] == (du, dv)
     out = h.image(dev(vis)).cpu().numpy()
     for i in range(out.shape[0]):
@@ -370,4 +372,21 @@ def test_image_host_many_chunks_equals_device(im):
     sums = h.weight_sums(24)
     assert rel_l2(host_out, dev_out) < 1e-6
     assert np.all(sums == 2 * int((obs.flags == 0).sum()))
+    h.close()
+
+
+def test_half_plane_falls_back_when_pixels_reach_the_side(im):
+    """At 1.5 GHz with oversampling 1 the largest pixel coordinate exceeds N, where the
+    reference's wrap no longer pairs mirror cells; the handle then images the full plane and
+    still matches the oracle."""
+    obs = synth.small(seed=47, n_ant=24, n_intervals=1, n_channels=2, n_pixels=64, f0=1.5e9, df=1e6)
+    h = im.Imager(64, 1.0, "XX", -1000.0)
+    h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+    h.set_frequencies(obs.freqs)
+    assert not h.half_plane
+    out = h.image(dev(obs.vis_f32())).cpu().numpy()
+    _, _, _, ref, _ = O.full_pipeline(obs.vis_f32(), obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, 64,
+                                      osf=1.0)
+    for j in range(2):
+        assert rel_l2(out[0, j], ref[0, j]) < IMAGE_TOL, j
     h.close()
