@@ -529,6 +529,8 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         cudaStream_t ls = streams[l];
         const int cnt = std::min(wave, img_first + count - img0);
         float2 *grid = im->grid[l].ptr;
+        const size_t need = (size_t)cnt * (p.half_width > 0 ? (size_t)n * p.half_width : npix);
+        if (need > im->grid[l].cap) return set_error(BGI_ERR_STATE, "grid scratch too small for a wave");
         unsigned int *ws = im->wsum.ptr + (size_t)img0 * kWsumStride;
         p.grids = grid;
         p.img_begin = img0;

@@ -402,7 +402,10 @@ template <int N>
 __device__ const ZTwData<N> g_z_twiddles = make_z_twiddles<N>();
 
 template <int N>
-constexpr int half_width_of() { return N / 2 + ColShape<N>::COLS; }
+constexpr int half_width_of() {
+    static_assert(N / 2 + ColShape<N>::COLS <= N, "half-plane grid wider than the full grid");
+    return N / 2 + ColShape<N>::COLS;
+}
 
 // Column pass of half-plane grids [img][N][W], in place: tiles of COLS adjacent columns, lanes
 // across the columns (coalesced row segments), transforms stepping together (block barriers);
@@ -639,7 +642,6 @@ int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsi
 
 int half_plane_width(int n) {
     switch (n) {
-        case 32: return half_width_of<32>();
         case 64: return half_width_of<64>();
         case 128: return half_width_of<128>();
         case 256: return half_width_of<256>();
@@ -654,7 +656,6 @@ int half_plane_width(int n) {
 int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s) {
     if (n_images <= 0) return BGI_OK;
     switch (n) {
-        case 32: return cols_half_n<32>(grids, n_images, s);
         case 64: return cols_half_n<64>(grids, n_images, s);
         case 128: return cols_half_n<128>(grids, n_images, s);
         case 256: return cols_half_n<256>(grids, n_images, s);
@@ -670,7 +671,6 @@ int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const un
                     cudaStream_t s) {
     if (n_images <= 0) return BGI_OK;
     switch (n) {
-        case 32: return c2r_n<32>(grids, images, n_images, wsum, s);
         case 64: return c2r_n<64>(grids, images, n_images, wsum, s);
         case 128: return c2r_n<128>(grids, images, n_images, wsum, s);
         case 256: return c2r_n<256>(grids, images, n_images, wsum, s);
