@@ -491,7 +491,8 @@ int prepare_call(bgi_imager *im, int n_images, cudaStream_t s, int *wave_out, in
     return BGI_OK;
 }
 
-GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals, unsigned flags) {
+GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
+                        const void *images) {
     GridParams p{};
     p.vis = vis;
     p.u = im->d_u;
@@ -511,6 +512,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
     p.half_width = im->half_plane() ? half_plane_width(im->cfg.n_pixels) : 0;
+    if (!aligned16(images)) p.half_width = 0;  // the complex-to-real stores are 16 bytes wide
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
     return p;
@@ -581,7 +583,7 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
         }
     }
     int next = 0;
-    BGI_TRY(run_waves(im, block_params(im, vis, n_intervals, flags), reinterpret_cast<float2 *>(images), 0,
+    BGI_TRY(run_waves(im, block_params(im, vis, n_intervals, flags, images), reinterpret_cast<float2 *>(images), 0,
                       n_images, wave, streams, n_lanes, &next));
     if (n_lanes > 1) {
         for (int l = 0; l < n_lanes; ++l) {
@@ -622,7 +624,7 @@ int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsig
     BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_out, im->ev_fork, 0), "fork wait"));
     for (int l = 0; l < n_lanes; ++l)
         BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
-    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags);
+    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr);
     int next = 0;
     for (int c = 0; c < n_chunks; ++c) {
         const int img0 = c * chunk;

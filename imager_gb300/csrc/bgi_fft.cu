@@ -441,7 +441,8 @@ struct C2RShape {
 // The row's N/2 + 1 values are staged in shared memory and cleared in the grid behind the
 // loads; the first pass forms Z[k] from X[k] and X[M-k]; the stores apply the fftshift of
 // columns (x -> (x + N/2) mod N keeps pairs 2m, 2m+1 together) and (float)(1/sum(w)), and
-// write complex pixels with zero imaginary parts, streaming past L2.
+// write each pair of complex pixels (zero imaginary parts) as one 16-byte store streaming past
+// L2: two 8-byte stores would each half-fill their sectors.
 template <int N>
 __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
                                                                                     const unsigned int *wsum) {
@@ -472,9 +473,9 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
             return make_float2(a.x * pr - a.y * pi + br * qr - bi * qi, a.x * pi + a.y * pr + br * qi + bi * qr);
         },
         [&](int m, float2 z) {
+            // pixels x and x+1 as one 16-byte store (images are 16-byte aligned on this path)
             const int x = (2 * m + N / 2) & (N - 1);
-            __stcs(dst + x, make_float2(z.x * scale, 0.f));
-            __stcs(dst + x + 1, make_float2(z.y * scale, 0.f));
+            __stcs(reinterpret_cast<float4 *>(dst + x), make_float4(z.x * scale, 0.f, z.y * scale, 0.f));
         });
 }
 

@@ -60,7 +60,7 @@ int half_plane_width(int n);
 int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s);
 // Complex-to-real row pass: half-plane rows -> image rows (fftshift of columns and
 // (float)(1/wsum) applied), clearing the grid rows it read.  Images are complex with zero
-// imaginary parts.
+// imaginary parts and must be 16-byte aligned.
 int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
                     cudaStream_t s);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
