@@ -162,9 +162,16 @@ struct TwTables {
 // synchronise with __syncwarp; otherwise every thread of the block calls this in lockstep and
 // passes use block barriers.  ALIASED: gstore writes into sm, so the final stores wait until
 // every thread has read its last inputs.
-template <int N, int R, bool WARP, bool ALIASED, class GLoad, class GStore>
+struct NoClear {
+    __device__ __forceinline__ void operator()(int) const {}
+};
+
+// gclear(i), when given, runs for every input element after all of this thread's first-pass
+// loads have been issued (clearing a source behind the loads without serialising them: a store
+// between two loads through possibly aliasing pointers would make each load wait for the last).
+template <int N, int R, bool WARP, bool ALIASED, class GLoad, class GStore, class GClear = NoClear>
 __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *tw, GLoad gload,
-                                              GStore gstore) {
+                                              GStore gstore, GClear gclear = GClear()) {
     using C = FftCfg<N, R>;
     using TT = TwTables<N, R>;
     constexpr int P = C::P;
@@ -173,6 +180,8 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
     float2 a[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) a[m] = gload(t + m * P);
+#pragma unroll
+    for (int m = 0; m < R; ++m) gclear(t + m * P);
     int Ns = 1;
     int toff = 0;
 #pragma unroll
@@ -330,12 +339,10 @@ __global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(f
     float2 *d_row = dst + row * N;
     fft_transform<N, S::R, S::WARP, false>(
         t, buf + slot * C::LEN, tw,
+        [&](int i) { return s_row[i]; }, [&](int i, float2 v) { d_row[i] = v; },
         [&](int i) {
-            float2 v = s_row[i];
             if (ZERO_SRC) s_row[i] = make_float2(0.f, 0.f);
-            return v;
-        },
-        [&](int i, float2 v) { d_row[i] = v; });
+        });
 }
 
 // Column pass on a tile pair: columns [x0, x0+CT) and their fftshift partners [x0+N/2, ...).
@@ -364,11 +371,7 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
     const int dcol = SHIFT_NORM ? ((col + N / 2) & (N - 1)) : col;
     fft_transform<N, S::R, false, false>(
         t, smem + c * S::STRIDE, tw,
-        [&](int i) {
-            float2 v = in[(size_t)i * N + col];
-            if (ZERO_SRC) in[(size_t)i * N + col] = make_float2(0.f, 0.f);
-            return v;
-        },
+        [&](int i) { return in[(size_t)i * N + col]; },
         [&](int i, float2 v) {
             int r = i;
             if (SHIFT_NORM) {
@@ -376,6 +379,9 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
                 v = make_float2(v.x * scale, v.y * scale);
             }
             __stcs(out + (size_t)r * N + dcol, v);
+        },
+        [&](int i) {
+            if (ZERO_SRC) in[(size_t)i * N + col] = make_float2(0.f, 0.f);
         });
 }
 
@@ -456,9 +462,19 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     const size_t img = row / N;
     float2 *src = grids + row * W;
     float2 *buf = smem + slot * S::BUF;
-    for (int k = t; k <= M; k += S::P) {
-        buf[k] = src[k];
-        src[k] = make_float2(0.f, 0.f);
+    constexpr int PER = M / S::P;  // row values per thread, plus X[M] on thread 0
+    float2 r[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) r[q] = src[t + q * S::P];
+    const float2 last = t == 0 ? src[M] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        buf[t + q * S::P] = r[q];
+        src[t + q * S::P] = make_float2(0.f, 0.f);
+    }
+    if (t == 0) {
+        buf[M] = last;
+        src[M] = make_float2(0.f, 0.f);
     }
     fft_sync<S::WARP>();
     const float scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
