@@ -266,7 +266,13 @@ def run_ours(args, rank, world, local_rank):
     images_per_s = world * n_images * args.steps / (ms / 1000.0)
     hbm_peak, peak_kind = measured_peaks()
     # algorithmic bytes per image of each stage
-    alg = {"gridding": B * 32 + 8 * N * N, "fft_rows": 16 * N * N, "fft_cols": 16 * N * N}
+    # algorithmic bytes per image of each stage, for the path the handle took
+    half = im.half_plane
+    if half:
+        hw = N * (N // 2 + 1) * 8  # half-plane grid of one image
+        alg = {"gridding": B * 32 + hw, "fft_pass1": 2 * hw, "fft_pass2": hw + 8 * N * N}
+    else:
+        alg = {"gridding": B * 32 + 8 * N * N, "fft_pass1": 16 * N * N, "fft_pass2": 16 * N * N}
     stage_info = {}
     for k, (tot_ms, launches) in stages.items():
         if launches:
@@ -289,7 +295,8 @@ def run_ours(args, rank, world, local_rank):
             "unit": "GB/s", "frac": stage_info[dom]["achieved_gbs"] / hbm_peak,
             "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
             "traffic": traffic,
-            "algorithmic_bytes_per_image": alg[dom]}
+            "algorithmic_bytes_per_image": alg[dom],
+            "path": "half plane (complex-to-real)" if half else "full plane"}
 
     cpu_rate, cpu_times, cpu_threads = cpu_sample_rate(obs, 16, args.cpu_seconds)
     h2d = vis_np.nbytes

@@ -462,14 +462,16 @@ namespace {
 
 // Per-call set-up on stream s: wave size, grid scratch of the lanes in use (cleared when new or
 // left dirty by a failed call), weight counters of every image cleared.
-int prepare_call(bgi_imager *im, int n_images, cudaStream_t s, int *wave_out, int *lanes_out) {
+int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *wave_out, int *lanes_out) {
     const int n = im->cfg.n_pixels;
     const size_t npix = (size_t)n * n;
     int wave = im->cfg.max_images_per_wave;
     if (wave == 0) {
-        // 32 MiB of grid per lane: two lanes' scratch stays resident in the 129 MB L2
-        const size_t budget = (size_t)32 << 20;
-        wave = (int)std::max<size_t>(1, budget / (npix * sizeof(float2)));
+        // about 26-32 MiB of grid per lane, so that two lanes' scratch stays resident in the
+        // 129 MB L2 (measured best: 16 full-plane or 24 half-plane images at 512^2)
+        const size_t per_image = half ? (size_t)n * half_plane_width(n) * sizeof(float2) : npix * sizeof(float2);
+        const size_t budget = (size_t)(half ? 26 : 32) << 20;
+        wave = (int)std::max<size_t>(1, budget / per_image);
     }
     wave = std::min(wave, n_images);
     const int n_waves = (n_images + wave - 1) / wave;
@@ -572,7 +574,8 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     cudaStream_t s = as_stream(stream);
     const int n_images = n_intervals * im->n_channels;
     int wave = 0, n_lanes = 0;
-    BGI_TRY(prepare_call(im, n_images, s, &wave, &n_lanes));
+    const GridParams p = block_params(im, vis, n_intervals, flags, images);
+    BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
     cudaStream_t streams[bgi_imager::kLanes] = {s, s};
     if (n_lanes > 1) {
         BGI_TRY(im->ensure_lanes());
@@ -583,7 +586,7 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
         }
     }
     int next = 0;
-    BGI_TRY(run_waves(im, block_params(im, vis, n_intervals, flags, images), reinterpret_cast<float2 *>(images), 0,
+    BGI_TRY(run_waves(im, p, reinterpret_cast<float2 *>(images), 0,
                       n_images, wave, streams, n_lanes, &next));
     if (n_lanes > 1) {
         for (int l = 0; l < n_lanes; ++l) {
@@ -611,7 +614,8 @@ int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsig
     BGI_TRY(im->io_vis.ensure(rec_floats * n_images, "image_host vis staging"));
     BGI_TRY(im->io_img.ensure(img_floats * n_images, "image_host image staging"));
     int wave = 0, n_lanes = 0;
-    BGI_TRY(prepare_call(im, n_images, s, &wave, &n_lanes));
+    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr);
+    BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
     BGI_TRY(im->ensure_lanes());
     BGI_TRY(im->ensure_copy_streams());
     // about eight chunks of whole waves
@@ -624,7 +628,6 @@ int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsig
     BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_out, im->ev_fork, 0), "fork wait"));
     for (int l = 0; l < n_lanes; ++l)
         BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
-    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr);
     int next = 0;
     for (int c = 0; c < n_chunks; ++c) {
         const int img0 = c * chunk;

@@ -196,11 +196,13 @@ class Imager:
         call("bgi_set_stage_timing", self._h, int(bool(enable)))
 
     def stage_times(self):
-        """{stage: (total ms, launches)} since the last read, for gridding, fft_rows, fft_cols."""
+        """{stage: (total ms, launches)} since the last read: gridding, the first FFT pass (rows,
+        or the half-plane column pass) and the second (columns with the epilogue, or the
+        complex-to-real row pass)."""
         ms = (C.c_double * 3)()
         n = (C.c_int64 * 3)()
         call("bgi_get_stage_times", self._h, ms, n)
-        return {k: (ms[i], int(n[i])) for i, k in enumerate(("gridding", "fft_rows", "fft_cols"))}
+        return {k: (ms[i], int(n[i])) for i, k in enumerate(("gridding", "fft_pass1", "fft_pass2"))}
 
     def weight_sums(self, n_images: int, stream=None) -> np.ndarray:
         out = np.zeros(n_images, np.uint32)

@@ -200,8 +200,10 @@ BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n
                               double delta_v, int n_pixels, double min_uv, int pol, float *images,
                               void *stream);
 
-/* Stage timing of bgi_image: when enabled, CUDA events are recorded on the call's stream
- * around each launch (gridding, FFT row pass, FFT column pass).  Recording adds no host
+/* Stage timing of bgi_image: when enabled, CUDA events are recorded on the stream of each
+ * launch around it: gridding, the first FFT pass (rows in place, or the half-plane column
+ * pass) and the second (columns with fftshift and normalisation, or the complex-to-real row
+ * pass).  Recording adds no host
  * synchronisation.  bgi_get_stage_times synchronises on the recorded events, writes the summed
  * milliseconds and launch counts of the three stages since the last read, and resets them. */
 BGI_API int bgi_set_stage_timing(bgi_imager *im, int enable);
