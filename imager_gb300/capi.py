@@ -40,6 +40,9 @@ _SIGNATURES = {
     "bgi_apply_cable_lengths_corrections_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp]),
     "bgi_gridding_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _vp, _d, _d, _i, _d, _i, _i,
                               _vp, _vp, _vp]),
+    "bgi_gridding_sorted_workspace": (_i, [_i, _i, _i, C.POINTER(C.c_size_t)]),
+    "bgi_gridding_sorted_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _i,
+                                     _vp, _vp, _vp, C.c_size_t, _vp]),
     "bgi_fft_inverse_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
     "bgi_fft_shift_and_norm_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp]),
     "bgi_vector_sum_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),

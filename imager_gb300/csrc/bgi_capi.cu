@@ -230,23 +230,24 @@ int bgi_apply_cable_lengths_corrections_gpu(float *vis, int n_ant, int n_channel
                         as_stream(stream));
 }
 
-int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
-                     const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
-                     const float *antenna_weights, const double *freqs_hz, double delta_u,
-                     double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
-                     float *counters, float *grids, void *stream) {
-    (void)antenna_weights;
+namespace {
+
+// Checks the arguments shared by both gridders and fills the launch parameters.
+int gridding_params(const char *who, const float *vis, int n_ant, int n_channels, int n_intervals,
+                    const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                    const double *freqs_hz, double delta_u, double delta_v, int n_pixels, double min_uv,
+                    int pol, int counter_mode, float *counters, float *grids, GridParams *out) {
     if (!vis || !u || !v || !baseline_flags || !freqs_hz || !grids || n_ant < 1 ||
         n_channels < 1 || n_intervals < 0 || n_pixels < 1 || n_pixels > 46340)
-        return set_error(BGI_ERR_INVALID, "gridding: bad arguments");
-    if (pol < BGI_POL_XX || pol > BGI_POL_V) return set_error(BGI_ERR_INVALID, "gridding: bad pol %d", pol);
+        return set_error(BGI_ERR_INVALID, "%s: bad arguments", who);
+    if (pol < BGI_POL_XX || pol > BGI_POL_V) return set_error(BGI_ERR_INVALID, "%s: bad pol %d", who, pol);
     if (n_uvw_sets != 1 && n_uvw_sets != n_intervals)
-        return set_error(BGI_ERR_INVALID, "gridding: n_uvw_sets must be 1 or n_intervals");
+        return set_error(BGI_ERR_INVALID, "%s: n_uvw_sets must be 1 or n_intervals", who);
     if (counters && counter_mode != BGI_COUNTERS_FIRST_INTERVAL && counter_mode != BGI_COUNTERS_PER_IMAGE)
-        return set_error(BGI_ERR_INVALID, "gridding: bad counter_mode %d", counter_mode);
-    if (!(delta_u > 0) || !(delta_v > 0)) return set_error(BGI_ERR_INVALID, "gridding: delta_u/v must be > 0");
-    if (!aligned16(vis)) return set_error(BGI_ERR_INVALID, "gridding: vis must be 16-byte aligned");
-    if ((reinterpret_cast<uintptr_t>(grids) & 7u) != 0) return set_error(BGI_ERR_INVALID, "gridding: grids must be 8-byte aligned");
+        return set_error(BGI_ERR_INVALID, "%s: bad counter_mode %d", who, counter_mode);
+    if (!(delta_u > 0) || !(delta_v > 0)) return set_error(BGI_ERR_INVALID, "%s: delta_u/v must be > 0", who);
+    if (!aligned16(vis)) return set_error(BGI_ERR_INVALID, "%s: vis must be 16-byte aligned", who);
+    if ((reinterpret_cast<uintptr_t>(grids) & 7u) != 0) return set_error(BGI_ERR_INVALID, "%s: grids must be 8-byte aligned", who);
     GridParams p{};
     p.vis = vis;
     p.u = u;
@@ -268,7 +269,45 @@ int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_interval
     p.img_count = n_channels * n_intervals;
     p.img_base = 0;
     p.counter_mode = counters ? counter_mode : -1;
+    *out = p;
+    return BGI_OK;
+}
+
+}  // namespace
+
+int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
+                     const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                     const float *antenna_weights, const double *freqs_hz, double delta_u,
+                     double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
+                     float *counters, float *grids, void *stream) {
+    (void)antenna_weights;
+    GridParams p;
+    BGI_TRY(gridding_params("gridding", vis, n_ant, n_channels, n_intervals, u, v, n_uvw_sets, baseline_flags,
+                            freqs_hz, delta_u, delta_v, n_pixels, min_uv, pol, counter_mode, counters, grids, &p));
     return launch_gridding(p, as_stream(stream));
+}
+
+int bgi_gridding_sorted_workspace(int n_ant, int n_pixels, int n_images, size_t *bytes) {
+    if (!bytes || n_ant < 1 || n_ant > kSortedMaxAnt || n_pixels < 1 || n_pixels > 46340 || n_images < 1)
+        return set_error(BGI_ERR_INVALID, "gridding_sorted_workspace: bad arguments");
+    *bytes = sorted_workspace_bytes(baselines_of(n_ant), n_pixels, n_images);
+    return BGI_OK;
+}
+
+int bgi_gridding_sorted_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
+                            const float *u, const float *v, int n_uvw_sets, const int *baseline_flags,
+                            const double *freqs_hz, double delta_u, double delta_v, int n_pixels,
+                            double min_uv, int pol, int counter_mode, float *counters, float *grids,
+                            void *workspace, size_t workspace_bytes, void *stream) {
+    if (n_ant > kSortedMaxAnt)
+        return set_error(BGI_ERR_INVALID, "gridding_sorted: at most %d antennas", kSortedMaxAnt);
+    if (!workspace || !aligned16(workspace))
+        return set_error(BGI_ERR_INVALID, "gridding_sorted: workspace must be a 16-byte aligned device buffer");
+    GridParams p;
+    BGI_TRY(gridding_params("gridding_sorted", vis, n_ant, n_channels, n_intervals, u, v, n_uvw_sets,
+                            baseline_flags, freqs_hz, delta_u, delta_v, n_pixels, min_uv, pol, counter_mode,
+                            counters, grids, &p));
+    return launch_gridding_sorted(p, workspace, workspace_bytes, as_stream(stream));
 }
 
 int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_images,

@@ -40,6 +40,14 @@ struct GridParams {
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
 
+// ---- deterministic gridding (bgi_sorted.cu) ------------------------------------------------
+// Point indices 2*b(+1) are 32-bit: at most 46,340 antennas (about 1.07e9 baselines).
+constexpr int kSortedMaxAnt = 46340;
+size_t sorted_workspace_bytes(long long n_baselines, int n_pixels, int n_images);
+// Same parameters as launch_gridding (full-plane grids only, half_width 0); the workspace is
+// reused chunk by chunk, so any size of at least one image's share works.
+int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaStream_t s);
+
 // ---- FFT and image epilogues (bgi_fft.cu) --------------------------------------------------
 bool fft_size_supported(int n);
 // Row pass: src rows -> dst rows (inverse DFT along x); zero_src clears src after reading.

@@ -1,0 +1,341 @@
+// Deterministic gridding by sort and segmented reduction.
+//
+// The atomic gridder adds the points of a cell in whatever order the GPU schedules them, so its
+// float sums differ in the last bits from run to run.  This variant sums every cell in a fixed
+// order -- the reference CPU loop's order, baseline by baseline, each visibility before its
+// conjugate (src/pacer_imager.cpp:297-408) -- so its grids are reproducible and bit-identical
+// to the CPU gridding given the same visibilities.  Per chunk of images:
+//
+//   keys:    one thread per (image, baseline): the two points' cells (or "none") and values,
+//            and a per-cell point count (integer atomics: order-free);
+//   scan:    exclusive prefix sum of the counts of each image, giving each cell's segment;
+//   place:   each point writes its index into its cell's segment (slot order arbitrary);
+//   reduce:  one thread per cell orders its segment by point index and adds the values to the
+//            cell in that order, starting from the grid's current value (as the CPU's +=).
+//
+// Workspace (caller provided, bgi_gridding_sorted_workspace gives the size): per image
+// 2B point keys, values and segment entries, and three N*N integer arrays.
+#include <algorithm>
+
+#include "bgi_internal.h"
+
+namespace bgi {
+namespace {
+
+constexpr unsigned kNoCell = 0xffffffffu;
+constexpr int kThreads = 256;
+
+struct SortedWs {
+    unsigned *key;      // [chunk][2B] cell of each point, kNoCell when not gridded
+    float2 *val;        // [chunk][2B]
+    unsigned *seg;      // [chunk][2B] point indices grouped by cell
+    unsigned *cnt;      // [chunk][N*N] points per cell
+    unsigned *start;    // [chunk][N*N] first segment slot of each cell
+    unsigned *cursor;   // [chunk][N*N] slots used so far
+    unsigned *n_long;   // [chunk] cells whose segment is longer than kShortSeg
+    unsigned *longs;    // [chunk][long_cap(B)] those cells
+};
+
+// Segments up to this length are ordered by the thread of their cell; longer ones (rare: many
+// short baselines in one cell) are handed to one block each.
+constexpr unsigned kShortSeg = 32;
+constexpr int kLongThreads = 512;
+constexpr int kLongBlocks = 8;  // blocks per image sharing its long cells
+constexpr int kTile = 1024;
+
+__host__ __device__ inline size_t long_cap(long long nb) { return (size_t)(2 * nb) / (kShortSeg + 1) + 1; }
+
+size_t per_image_bytes(long long nb, int n) {
+    const size_t pts = 2 * (size_t)nb, cells = (size_t)n * n;
+    return pts * (sizeof(unsigned) + sizeof(float2) + sizeof(unsigned)) + 3 * cells * sizeof(unsigned) +
+           (1 + long_cap(nb)) * sizeof(unsigned) + 8 * 256;  // 8 arrays, each start rounded up to 256 B
+}
+
+SortedWs carve(void *ws, int chunk, long long nb, int n) {
+    const size_t pts = 2 * (size_t)nb * chunk, cells = (size_t)n * n * chunk;
+    char *p = static_cast<char *>(ws);
+    auto take = [&](size_t bytes) {
+        char *q = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return q;
+    };
+    SortedWs w;
+    w.val = reinterpret_cast<float2 *>(take(pts * sizeof(float2)));
+    w.key = reinterpret_cast<unsigned *>(take(pts * sizeof(unsigned)));
+    w.seg = reinterpret_cast<unsigned *>(take(pts * sizeof(unsigned)));
+    w.cnt = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
+    w.start = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
+    w.cursor = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
+    w.n_long = reinterpret_cast<unsigned *>(take(chunk * sizeof(unsigned)));
+    w.longs = reinterpret_cast<unsigned *>(take(chunk * long_cap(nb) * sizeof(unsigned)));
+    return w;
+}
+
+// keys: grid x = baselines, y = images of the chunk
+__global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int chunk_first, SortedWs w) {
+    __shared__ ChannelConst s_cc;
+    const int img = chunk_first + blockIdx.y;
+    const int local = blockIdx.y;
+    const int ch = img % p.n_channels, t = img / p.n_channels;
+    if (threadIdx.x == 0) s_cc = make_channel_const(p.freqs[ch], p.du, p.dv);
+    __syncthreads();
+    const long long nb = p.n_baselines;
+    const long long b = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const bool in_range = b < nb;
+    const size_t set = p.n_uvw_sets > 1 ? (size_t)t * nb : 0;
+    const int n = p.n_pixels;
+    unsigned k1 = kNoCell, k2 = kNoCell;
+    float2 z = make_float2(0.f, 0.f);
+    if (in_range && p.flags[b] <= 0) {
+        const float2 *rec = reinterpret_cast<const float2 *>(p.vis) + ((size_t)img * nb + b) * 4;
+        float2 a = make_float2(0.f, 0.f), bb = a;
+        switch (p.pol) {
+            case BGI_POL_XX: load_pols<BGI_POL_XX>(rec, a, bb); z = combine_pols<BGI_POL_XX>(a, bb); break;
+            case BGI_POL_YY: load_pols<BGI_POL_YY>(rec, a, bb); z = combine_pols<BGI_POL_YY>(a, bb); break;
+            case BGI_POL_I: load_pols<BGI_POL_I>(rec, a, bb); z = combine_pols<BGI_POL_I>(a, bb); break;
+            default: load_pols<BGI_POL_V>(rec, a, bb); z = combine_pols<BGI_POL_V>(a, bb); break;
+        }
+        if (p.apply_geom || p.apply_cable) {
+            float d_hi, d_lo;
+            const float wv = p.apply_geom ? p.w[set + b] : 0.f;
+            const float2 dl = p.apply_cable ? p.dl[b] : make_float2(0.f, 0.f);
+            delay_df(wv, dl.x, dl.y, d_hi, d_lo);
+            z = rotate(z, phasor_df(d_hi, d_lo, s_cc.f_hi, s_cc.f_lo));
+        }
+        int ui, vi;
+        if (!isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
+            uv_pixels(p.u[set + b], p.v[set + b], s_cc, p.du, p.dv, p.min_uv, p.min_uv >= 0.0, &ui, &vi)) {
+            const long long pos = cell_pos(ui, vi, +1, n), pos2 = cell_pos(ui, vi, -1, n);
+            unsigned *cnt = w.cnt + (size_t)local * n * n;
+            if (pos >= 0) {
+                k1 = (unsigned)pos;
+                atomicAdd(cnt + pos, 1u);
+            }
+            if (pos2 >= 0) {
+                k2 = (unsigned)pos2;
+                atomicAdd(cnt + pos2, 1u);
+            }
+        }
+    }
+    if (p.wsum) {
+        const unsigned counted = (k1 != kNoCell) + (k2 != kNoCell);
+        const unsigned total = __reduce_add_sync(0xffffffffu, counted);
+        if ((threadIdx.x & 31) == 0 && total)
+            atomicAdd(p.wsum + (size_t)(img - p.img_base) * kWsumStride, total);
+    }
+    if (!in_range) return;
+    const size_t q = (size_t)local * 2 * nb + 2 * b;
+    w.key[q] = k1;
+    w.key[q + 1] = k2;
+    w.val[q] = z;
+    w.val[q + 1] = make_float2(z.x, -z.y);
+}
+
+// scan: one block per image, exclusive prefix sum of its N*N counts (each thread owns a
+// contiguous run of cells).
+__global__ void __launch_bounds__(1024) scan_kernel(SortedWs w, int n) {
+    __shared__ unsigned s_part[1024];
+    const size_t cells = (size_t)n * n;
+    const unsigned *cnt = w.cnt + blockIdx.x * cells;
+    unsigned *start = w.start + blockIdx.x * cells;
+    const size_t per = (cells + blockDim.x - 1) / blockDim.x;
+    const size_t c0 = threadIdx.x * per, c1 = c0 + per < cells ? c0 + per : cells;
+    unsigned sum = 0;
+    for (size_t c = c0; c < c1; ++c) sum += cnt[c];
+    s_part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {  // inclusive Hillis-Steele scan
+        unsigned v = threadIdx.x >= (unsigned)off ? s_part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        s_part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = s_part[threadIdx.x] - sum;  // exclusive prefix of this thread's run
+    for (size_t c = c0; c < c1; ++c) {
+        start[c] = run;
+        run += cnt[c];
+    }
+}
+
+// place: one thread per point
+__global__ void __launch_bounds__(kThreads) place_kernel(SortedWs w, long long n_points, int n) {
+    const long long q = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const int local = blockIdx.y;
+    if (q >= n_points) return;
+    const size_t base = (size_t)local * n_points;
+    const unsigned key = w.key[base + q];
+    if (key == kNoCell) return;
+    const size_t cbase = (size_t)local * n * n;
+    const unsigned slot = atomicAdd(w.cursor + cbase + key, 1u);
+    w.seg[base + w.start[cbase + key] + slot] = (unsigned)q;
+}
+
+// reduce: one thread per cell; orders the cell's point indices (insertion sort: segments are
+// short) and adds the values in that order to the cell's current value.
+__global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, int chunk_first, SortedWs w,
+                                                          long long n_points) {
+    const int n = p.n_pixels;
+    const long long cells = (long long)n * n;
+    const long long c = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const int local = blockIdx.y;
+    if (c >= cells) return;
+    const size_t cbase = (size_t)local * cells;
+    const unsigned len = w.cnt[cbase + c];
+    if (len == 0) return;
+    if (len > kShortSeg) {
+        const unsigned slot = atomicAdd(w.n_long + local, 1u);
+        w.longs[(size_t)local * long_cap(n_points / 2) + slot] = (unsigned)c;
+        return;
+    }
+    unsigned *seg = w.seg + (size_t)local * n_points + w.start[cbase + c];
+    for (unsigned i = 1; i < len; ++i) {
+        const unsigned v = seg[i];
+        unsigned j = i;
+        while (j > 0 && seg[j - 1] > v) {
+            seg[j] = seg[j - 1];
+            --j;
+        }
+        seg[j] = v;
+    }
+    const int img = chunk_first + local;
+    float2 *cell = p.grids + (size_t)(img - p.img_base) * cells + c;
+    float2 acc = *cell;
+    const float2 *val = w.val + (size_t)local * n_points;
+    for (unsigned i = 0; i < len; ++i) {
+        const float2 v = val[seg[i]];
+        acc.x = __fadd_rn(acc.x, v.x);
+        acc.y = __fadd_rn(acc.y, v.y);
+    }
+    *cell = acc;
+    if (p.counter_mode == BGI_COUNTERS_PER_IMAGE || (p.counter_mode == BGI_COUNTERS_FIRST_INTERVAL && img < p.n_channels)) {
+        float *cnt = p.counters + (size_t)img * cells + c;
+        float f = *cnt;
+        for (unsigned i = 0; i < len; ++i) f = __fadd_rn(f, 1.0f);
+        *cnt = f;
+    }
+}
+
+// long segments: one block per cell.  Each point index is placed at its rank (the number of
+// smaller indices in the segment, counted against shared-memory tiles) in the cell's range of
+// the key array, which is free after placement; then the values are staged in tiles and thread
+// 0 adds them in that order.
+__global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, int chunk_first, SortedWs w,
+                                                            long long n_points) {
+    __shared__ unsigned s_idx[kTile];
+    __shared__ float2 s_val[kTile];
+    const int n = p.n_pixels;
+    const size_t cells = (size_t)n * n;
+    const int local = blockIdx.y;
+    const int img = chunk_first + local;
+    const unsigned n_long = w.n_long[local];
+    for (unsigned li = blockIdx.x; li < n_long; li += gridDim.x) {
+        const unsigned c = w.longs[(size_t)local * long_cap(n_points / 2) + li];
+        const size_t cbase = (size_t)local * cells;
+        const unsigned len = w.cnt[cbase + c];
+        const unsigned st = w.start[cbase + c];
+        const unsigned *seg = w.seg + (size_t)local * n_points + st;
+        unsigned *ordered = w.key + (size_t)local * n_points + st;
+        for (unsigned i0 = 0; i0 < len; i0 += kLongThreads) {
+            const bool mine_valid = i0 + threadIdx.x < len;
+            const unsigned mine = mine_valid ? seg[i0 + threadIdx.x] : 0u;
+            unsigned rank = 0;
+            for (unsigned j0 = 0; j0 < len; j0 += kTile) {
+                const unsigned m = min((unsigned)kTile, len - j0);
+                __syncthreads();
+                for (unsigned t = threadIdx.x; t < m; t += kLongThreads) s_idx[t] = seg[j0 + t];
+                __syncthreads();
+                for (unsigned t = 0; t < m; ++t) rank += s_idx[t] < mine;
+            }
+            if (mine_valid) ordered[rank] = mine;
+        }
+        __syncthreads();
+        float2 *cell = p.grids + (size_t)(img - p.img_base) * cells + c;
+        float2 acc = make_float2(0.f, 0.f);
+        if (threadIdx.x == 0) acc = *cell;
+        const float2 *val = w.val + (size_t)local * n_points;
+        for (unsigned j0 = 0; j0 < len; j0 += kTile) {
+            const unsigned m = min((unsigned)kTile, len - j0);
+            __syncthreads();
+            for (unsigned t = threadIdx.x; t < m; t += kLongThreads) s_val[t] = val[ordered[j0 + t]];
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (unsigned t = 0; t < m; ++t) {
+                    acc.x = __fadd_rn(acc.x, s_val[t].x);
+                    acc.y = __fadd_rn(acc.y, s_val[t].y);
+                }
+            }
+        }
+        if (threadIdx.x == 0) {
+            *cell = acc;
+            if (p.counter_mode == BGI_COUNTERS_PER_IMAGE ||
+                (p.counter_mode == BGI_COUNTERS_FIRST_INTERVAL && img < p.n_channels)) {
+                float *cnt = p.counters + (size_t)img * cells + c;
+                float f = *cnt;
+                for (unsigned i = 0; i < len; ++i) f = __fadd_rn(f, 1.0f);
+                *cnt = f;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+size_t sorted_workspace_bytes(long long n_baselines, int n_pixels, int n_images) {
+    return per_image_bytes(n_baselines, n_pixels) * (size_t)std::max(1, n_images);
+}
+
+int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaStream_t s) {
+    if (p.img_count <= 0 || p.n_baselines <= 0) return BGI_OK;
+    const int n = p.n_pixels;
+    const size_t per = per_image_bytes(p.n_baselines, n);
+    const int chunk = (int)std::min<size_t>((size_t)p.img_count, ws_bytes / per);
+    if (chunk < 1 || !ws) return set_error(BGI_ERR_INVALID, "gridding_sorted: workspace of %zu bytes is below %zu", ws_bytes, per);
+    const long long n_points = 2 * p.n_baselines;
+    const unsigned bx_b = (unsigned)((p.n_baselines + kThreads - 1) / kThreads);
+    const unsigned bx_p = (unsigned)((n_points + kThreads - 1) / kThreads);
+    const unsigned bx_c = (unsigned)(((long long)n * n + kThreads - 1) / kThreads);
+    for (int img0 = p.img_begin; img0 < p.img_begin + p.img_count; img0 += chunk) {
+        const int cnt = std::min(chunk, p.img_begin + p.img_count - img0);
+        SortedWs w = carve(ws, cnt, p.n_baselines, n);
+        const size_t cell_bytes = sizeof(unsigned) * (size_t)n * n * cnt;
+        int st = check_cuda(cudaMemsetAsync(w.cnt, 0, cell_bytes, s), "gridding_sorted: clear counts");
+        if (st) return st;
+        st = check_cuda(cudaMemsetAsync(w.cursor, 0, cell_bytes, s), "gridding_sorted: clear cursors");
+        if (st) return st;
+        st = check_cuda(cudaMemsetAsync(w.n_long, 0, sizeof(unsigned) * cnt, s), "gridding_sorted: clear long list");
+        if (st) return st;
+        for (int done = 0; done < cnt; done += 65535) {
+            const int k = std::min(65535, cnt - done);
+            SortedWs wd = w;
+            wd.key += (size_t)done * n_points;
+            wd.val += (size_t)done * n_points;
+            wd.cnt += (size_t)done * n * n;
+            keys_kernel<<<dim3(bx_b, k), kThreads, 0, s>>>(p, img0 + done, wd);
+            if ((st = check_launch("gridding_sorted keys"))) return st;
+        }
+        scan_kernel<<<cnt, 1024, 0, s>>>(w, n);
+        if ((st = check_launch("gridding_sorted scan"))) return st;
+        for (int done = 0; done < cnt; done += 65535) {
+            const int k = std::min(65535, cnt - done);
+            SortedWs wd = w;
+            wd.key += (size_t)done * n_points;
+            wd.val += (size_t)done * n_points;
+            wd.seg += (size_t)done * n_points;
+            wd.cnt += (size_t)done * n * n;
+            wd.start += (size_t)done * n * n;
+            wd.cursor += (size_t)done * n * n;
+            place_kernel<<<dim3(bx_p, k), kThreads, 0, s>>>(wd, n_points, n);
+            if ((st = check_launch("gridding_sorted place"))) return st;
+            wd.n_long += done;
+            wd.longs += (size_t)done * long_cap(p.n_baselines);
+            reduce_kernel<<<dim3(bx_c, k), kThreads, 0, s>>>(p, img0 + done, wd, n_points);
+            if ((st = check_launch("gridding_sorted reduce"))) return st;
+            long_kernel<<<dim3(kLongBlocks, k), kLongThreads, 0, s>>>(p, img0 + done, wd, n_points);
+            if ((st = check_launch("gridding_sorted long segments"))) return st;
+        }
+    }
+    return BGI_OK;
+}
+
+}  // namespace bgi

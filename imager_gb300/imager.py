@@ -88,6 +88,29 @@ def gridding(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv, pol, g
          _ptr(grids), _stream(stream))
 
 
+def gridding_sorted_workspace_bytes(n_ant, n_pixels, n_images):
+    """Device bytes bgi_gridding_sorted_gpu needs to grid n_images images in one chunk."""
+    out = C.c_size_t(0)
+    call("bgi_gridding_sorted_workspace", int(n_ant), int(n_pixels), int(n_images), C.byref(out))
+    return int(out.value)
+
+
+def gridding_sorted(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv, pol, grids, counters=None,
+                    counter_mode=capi.COUNTERS_PER_IMAGE, n_uvw_sets=1, workspace=None, stream=None):
+    """Deterministic gridding: gridding()'s result with every cell summed in the CPU loop's order
+    (src/pacer_imager.cpp:297-408), bit-identical run to run.  workspace: a uint8 CUDA tensor;
+    by default one sized for all images is allocated."""
+    T, Cn, B = _vis_dims(vis)
+    n_ant = _n_ant(B)
+    if workspace is None:
+        workspace = torch.empty(gridding_sorted_workspace_bytes(n_ant, n_pixels, max(1, T * Cn)),
+                                dtype=torch.uint8, device=vis.device)
+    call("bgi_gridding_sorted_gpu", _ptr(vis), n_ant, Cn, T, _ptr(u), _ptr(v), n_uvw_sets, _ptr(flags),
+         _ptr(freqs), float(delta_u), float(delta_v), int(n_pixels), float(min_uv),
+         POL[pol] if isinstance(pol, str) else int(pol), int(counter_mode), _ptr(counters),
+         _ptr(grids), _ptr(workspace), workspace.numel(), _stream(stream))
+
+
 def fft_inverse(grids, images, stream=None):
     """gpufftExecC2C(..., BACKWARD) replacement: unnormalised inverse 2D FFT, out of place."""
     n = int(grids.shape[-1])

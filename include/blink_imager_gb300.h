@@ -100,6 +100,22 @@ BGI_API int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_
                      double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
                      float *counters, float *grids, void *stream);
 
+/* Deterministic gridding: the same inputs, checks and cell indices as bgi_gridding_gpu, but
+ * every cell sums its points in the CPU gridding loop's order (baseline by baseline, each
+ * visibility before its conjugate: src/pacer_imager.cpp:297-408), so grids are reproducible
+ * run to run and bit-identical to that loop's FP32 sums.  No reference GPU counterpart (the
+ * reference's gridding_kernel adds with float atomics in scheduling order).  The caller
+ * provides a 16-byte aligned device workspace; bgi_gridding_sorted_workspace gives the bytes
+ * needed to grid n_images images in one chunk (a smaller workspace of at least one image's
+ * share is used chunk by chunk).  At most 46,340 antennas. */
+BGI_API int bgi_gridding_sorted_workspace(int n_ant, int n_pixels, int n_images, size_t *bytes);
+BGI_API int bgi_gridding_sorted_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
+                            const float *u, const float *v, int n_uvw_sets,
+                            const int *baseline_flags, const double *freqs_hz, double delta_u,
+                            double delta_v, int n_pixels, double min_uv, int pol,
+                            int counter_mode, float *counters, float *grids, void *workspace,
+                            size_t workspace_bytes, void *stream);
+
 /* gpufftPlanMany + gpufftExecC2C(..., BACKWARD) (src/gpu/pacer_imager_hip.cpp:83-99): batched
  * unnormalised inverse 2D FFT, out of place, our own kernels.  n_pixels: power of two,
  * 16..4096. */

@@ -59,3 +59,20 @@ def test_create_rejects_bad_config(lib):
     # null handle calls
     assert lib.bgi_image(None, C.c_void_p(16), 1, 0, C.c_void_p(16), None) == capi.ERR_INVALID
     assert lib.bgi_destroy(None) == capi.OK
+
+
+def test_sorted_workspace_size(lib):
+    n = C.c_size_t(0)
+    assert lib.bgi_gridding_sorted_workspace(256, 512, 1, C.byref(n)) == capi.OK
+    one = n.value
+    nb = 256 * 257 // 2
+    # per image: key, value and segment entry per point (2 per baseline), 3 counts per cell
+    assert one >= 2 * nb * 16 + 3 * 512 * 512 * 4
+    assert lib.bgi_gridding_sorted_workspace(256, 512, 10, C.byref(n)) == capi.OK
+    assert n.value == 10 * one
+    assert lib.bgi_gridding_sorted_workspace(0, 512, 1, C.byref(n)) == capi.ERR_INVALID
+    assert lib.bgi_gridding_sorted_workspace(256, 512, 1, None) == capi.ERR_INVALID
+    # a workspace that is not 16-byte aligned is refused before any launch
+    assert lib.bgi_gridding_sorted_gpu(C.c_void_p(16), 4, 1, 1, C.c_void_p(16), C.c_void_p(16), 1,
+                                       C.c_void_p(16), C.c_void_p(16), 1.0, 1.0, 64, -1.0, 0, 1, None,
+                                       C.c_void_p(16), C.c_void_p(24), 1 << 20, None) == capi.ERR_INVALID
