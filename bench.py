@@ -226,6 +226,35 @@ def run_ours(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
+    # variants of the same step, timed the same way over fewer steps
+    variants = {}
+    if args.variants:
+        def time_steps(h, k):
+            for _ in range(2):
+                h.image(vis, flags=flags, out=out)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(k):
+                h.image(vis, flags=flags, out=out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / k
+
+        k = max(3, min(args.steps, 20))
+        im.set_deterministic(True)
+        v_ms = time_steps(im, k)
+        im.set_deterministic(False)
+        variants["deterministic_sorted_gridding"] = {"images_per_s": world * n_images / (v_ms / 1000.0),
+                                                     "ms_per_step": v_ms, "steps": k, "plane": "full"}
+        full = Imager(N, 2.0, "XX", -1000.0, max_images_per_wave=args.wave, full_plane=True)
+        full.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+        full.set_frequencies(obs.freqs)
+        v_ms = time_steps(full, k)
+        full.close()
+        variants["full_plane_atomic_gridding"] = {"images_per_s": world * n_images / (v_ms / 1000.0),
+                                                  "ms_per_step": v_ms, "steps": k, "plane": "full"}
+
     # end to end through the host-buffer entry point: pinned input, pinned output
     vis_h = torch.from_numpy(vis_np).pin_memory()
     out_h = torch.empty((T, Cn, N, N), dtype=torch.complex64).pin_memory()
@@ -322,6 +351,7 @@ def run_ours(args, rank, world, local_rank):
                                    "normalise, shift (oracle/ restatement, OpenMP)"},
         "clocks": clocks.summary(t0, t3),
         "gpu_launches": sum(v[1] for v in stages.values()),
+        "variants": variants,
         "parity_sample_rel_l2": max(errs),
     }
     print(json.dumps(line), flush=True)
@@ -338,6 +368,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--wave", type=int, default=0, help="images per launch wave (0 = auto)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-variants", dest="variants", action="store_false",
+                    help="skip timing the deterministic and full-plane variants")
     ap.add_argument("--intervals", type=int, default=10,
                     help="intervals per block (10 = the measured workload; fewer only for profiling)")
     args = ap.parse_args()

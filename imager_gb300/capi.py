@@ -58,6 +58,7 @@ _SIGNATURES = {
     "bgi_image_host": (_i, [_vp, _vp, _i, _u, _vp, _vp]),
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
+    "bgi_set_deterministic": (_i, [_vp, _i]),
     "bgi_set_stage_timing": (_i, [_vp, _i]),
     "bgi_get_stage_times": (_i, [_vp, C.POINTER(_d), C.POINTER(_i64)]),
 }

@@ -129,6 +129,10 @@ struct bgi_imager {
     bool grid_dirty[kLanes] = {false, false};
     cudaStream_t lane[kLanes] = {nullptr, nullptr};
     cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {nullptr, nullptr};
+    // Deterministic mode: gridding by sort and ordered per-cell sums (full plane), with a
+    // workspace per lane for one wave.
+    bool deterministic = false;
+    DevBuf<unsigned char> sorted_ws[kLanes];
     DevBuf<unsigned int> wsum;    // per-image weight counts of the last call
     DevBuf<float> io_vis, io_img; // device staging of bgi_image_host
     int last_images = 0;
@@ -379,6 +383,7 @@ int bgi_destroy(bgi_imager *im) {
         if (im->lane[l]) cudaStreamDestroy(im->lane[l]);
         if (im->ev_join[l]) cudaEventDestroy(im->ev_join[l]);
         im->grid[l].release();
+        im->sorted_ws[l].release();
     }
     if (im->ev_fork) cudaEventDestroy(im->ev_fork);
     for (cudaEvent_t e : im->ev_in) cudaEventDestroy(e);
@@ -523,6 +528,8 @@ int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *w
                                "grid scratch clear"));
             im->grid_dirty[l] = false;
         }
+        if (im->deterministic)
+            BGI_TRY(im->sorted_ws[l].ensure(sorted_workspace_bytes(im->n_baselines, n, wave), "gridding workspace"));
     }
     BGI_TRY(im->wsum.ensure((size_t)n_images * kWsumStride, "weight sums"));
     BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * kWsumStride * n_images, s),
@@ -552,7 +559,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.n_pixels = im->cfg.n_pixels;
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
-    p.half_width = im->half_plane() ? half_plane_width(im->cfg.n_pixels) : 0;
+    p.half_width = im->half_plane() && !im->deterministic ? half_plane_width(im->cfg.n_pixels) : 0;
     if (!aligned16(images)) p.half_width = 0;  // the complex-to-real stores are 16 bytes wide
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
@@ -582,7 +589,12 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         p.wsum = ws;  // indexed img - img_base
         im->grid_dirty[l] = true;
         BGI_TRY(im->mark(ls));
-        BGI_TRY(launch_gridding(p, ls));
+        if (im->deterministic) {
+            p.grids_zero = 1;  // the wave scratch is zero between waves
+            BGI_TRY(launch_gridding_sorted(p, im->sorted_ws[l].ptr, im->sorted_ws[l].cap, ls));
+        }
+        else
+            BGI_TRY(launch_gridding(p, ls));
         BGI_TRY(im->mark(ls));
         if (p.half_width > 0) {
             BGI_TRY(launch_fft_cols_half(grid, n, cnt, ls));                   // in place, rows shifted
@@ -703,6 +715,12 @@ int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void
                                          sizeof(uint32_t) * kWsumStride, sizeof(uint32_t), n_images,
                                          cudaMemcpyDeviceToHost, s), "last_weight_sums copy"));
     return check_cuda(cudaStreamSynchronize(s), "last_weight_sums sync");
+}
+
+int bgi_set_deterministic(bgi_imager *im, int enable) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_deterministic: null handle");
+    im->deterministic = enable != 0;
+    return BGI_OK;
 }
 
 int bgi_set_stage_timing(bgi_imager *im, int enable) {

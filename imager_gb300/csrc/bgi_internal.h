@@ -37,6 +37,8 @@ struct GridParams {
     int counter_mode;          // -1 none, 0 first interval, 1 per image
     int half_width;            // 0: full N x N grids; W > 0: half-plane grids [N][W], u <= N/2
     int apply_geom, apply_cable;
+    int grids_zero;            // 1: grids hold zeros on entry (the ordered gridder then writes
+                               // cells instead of reading them first)
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
 

@@ -30,7 +30,8 @@ struct SortedWs {
     float2 *val;        // [chunk][2B]
     unsigned *seg;      // [chunk][2B] point indices grouped by cell
     unsigned *cnt;      // [chunk][N*N] points per cell
-    unsigned *start;    // [chunk][N*N] first segment slot of each cell
+    unsigned *start;    // [chunk][N*N] first segment slot of each cell within its tile
+    unsigned *tile_off; // [chunk][tiles(N)] first segment slot of each tile of kScanTile cells
     unsigned *cursor;   // [chunk][N*N] slots used so far
     unsigned *n_long;   // [chunk] cells whose segment is longer than kShortSeg
     unsigned *longs;    // [chunk][long_cap(B)] those cells
@@ -42,13 +43,22 @@ constexpr unsigned kShortSeg = 32;
 constexpr int kLongThreads = 512;
 constexpr int kLongBlocks = 8;  // blocks per image sharing its long cells
 constexpr int kTile = 1024;
+// The per-image prefix sum runs over tiles of 4096 cells (256 threads x 16 cells), then over
+// the tiles' totals.
+constexpr int kScanTile = 4096;
+constexpr int kScanPer = kScanTile / kThreads;
+
+__host__ __device__ inline size_t scan_tiles(int n) { return ((size_t)n * n + kScanTile - 1) / kScanTile; }
+__device__ __forceinline__ unsigned seg_start(const SortedWs &w, int local, int n, size_t c) {
+    return w.tile_off[(size_t)local * scan_tiles(n) + c / kScanTile] + w.start[(size_t)local * n * n + c];
+}
 
 __host__ __device__ inline size_t long_cap(long long nb) { return (size_t)(2 * nb) / (kShortSeg + 1) + 1; }
 
 size_t per_image_bytes(long long nb, int n) {
     const size_t pts = 2 * (size_t)nb, cells = (size_t)n * n;
     return pts * (sizeof(unsigned) + sizeof(float2) + sizeof(unsigned)) + 3 * cells * sizeof(unsigned) +
-           (1 + long_cap(nb)) * sizeof(unsigned) + 8 * 256;  // 8 arrays, each start rounded up to 256 B
+           (1 + long_cap(nb) + scan_tiles(n)) * sizeof(unsigned) + 9 * 256;  // 9 arrays, each start rounded up to 256 B
 }
 
 SortedWs carve(void *ws, int chunk, long long nb, int n) {
@@ -66,6 +76,7 @@ SortedWs carve(void *ws, int chunk, long long nb, int n) {
     w.cnt = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
     w.start = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
     w.cursor = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
+    w.tile_off = reinterpret_cast<unsigned *>(take(chunk * scan_tiles(n) * sizeof(unsigned)));
     w.n_long = reinterpret_cast<unsigned *>(take(chunk * sizeof(unsigned)));
     w.longs = reinterpret_cast<unsigned *>(take(chunk * long_cap(nb) * sizeof(unsigned)));
     return w;
@@ -131,29 +142,97 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
     w.val[q + 1] = make_float2(z.x, -z.y);
 }
 
-// scan: one block per image, exclusive prefix sum of its N*N counts (each thread owns a
-// contiguous run of cells).
-__global__ void __launch_bounds__(1024) scan_kernel(SortedWs w, int n) {
-    __shared__ unsigned s_part[1024];
+// scan, first level: grid (tiles, images); each thread owns 16 consecutive cells (read and
+// written as 16-byte vectors when the image's cell count is a multiple of 4).  Writes each
+// cell's exclusive prefix within its tile and the tile's total.
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads) scan_tiles_kernel(SortedWs w, int n) {
+    __shared__ unsigned s_warp[kThreads / 32];
     const size_t cells = (size_t)n * n;
-    const unsigned *cnt = w.cnt + blockIdx.x * cells;
-    unsigned *start = w.start + blockIdx.x * cells;
-    const size_t per = (cells + blockDim.x - 1) / blockDim.x;
-    const size_t c0 = threadIdx.x * per, c1 = c0 + per < cells ? c0 + per : cells;
+    const int local = blockIdx.y;
+    const size_t c0 = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPer;
+    const unsigned *cnt = w.cnt + (size_t)local * cells;
+    unsigned *start = w.start + (size_t)local * cells;
+    unsigned v[kScanPer];
+    if (VEC) {
+#pragma unroll
+        for (int j = 0; j < kScanPer; j += 4) {
+            uint4 q = make_uint4(0u, 0u, 0u, 0u);
+            if (c0 + j < cells) q = *reinterpret_cast<const uint4 *>(cnt + c0 + j);
+            v[j] = q.x;
+            v[j + 1] = q.y;
+            v[j + 2] = q.z;
+            v[j + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanPer; ++j) v[j] = c0 + j < cells ? cnt[c0 + j] : 0u;
+    }
     unsigned sum = 0;
-    for (size_t c = c0; c < c1; ++c) sum += cnt[c];
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) sum += v[j];
+    // block-wide exclusive scan of the thread sums
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned incl = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned x = lane < kThreads / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += t;
+        }
+        if (lane < kThreads / 32) s_warp[lane] = x;  // inclusive warp totals
+    }
+    __syncthreads();
+    unsigned run = incl - sum + (wid > 0 ? s_warp[wid - 1] : 0u);
+    unsigned out[kScanPer];
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) {
+        out[j] = run;
+        run += v[j];
+    }
+    if (VEC) {
+#pragma unroll
+        for (int j = 0; j < kScanPer; j += 4)
+            if (c0 + j < cells) *reinterpret_cast<uint4 *>(start + c0 + j) = make_uint4(out[j], out[j + 1], out[j + 2], out[j + 3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanPer; ++j)
+            if (c0 + j < cells) start[c0 + j] = out[j];
+    }
+    if (threadIdx.x == kThreads - 1) w.tile_off[(size_t)local * scan_tiles(n) + blockIdx.x] = run;
+}
+
+// scan, second level: one block per image turns its tile totals into exclusive offsets (each
+// thread owns a contiguous run of tiles).
+__global__ void __launch_bounds__(1024) scan_offsets_kernel(SortedWs w, int n) {
+    __shared__ unsigned s_part[1024];
+    const size_t tiles = scan_tiles(n);
+    unsigned *off = w.tile_off + (size_t)blockIdx.x * tiles;
+    const size_t per = (tiles + blockDim.x - 1) / blockDim.x;
+    const size_t t0 = threadIdx.x * per, t1 = t0 + per < tiles ? t0 + per : tiles;
+    unsigned sum = 0;
+    for (size_t t = t0; t < t1; ++t) sum += off[t];
     s_part[threadIdx.x] = sum;
     __syncthreads();
-    for (int off = 1; off < (int)blockDim.x; off <<= 1) {  // inclusive Hillis-Steele scan
-        unsigned v = threadIdx.x >= (unsigned)off ? s_part[threadIdx.x - off] : 0u;
+    for (int d = 1; d < (int)blockDim.x; d <<= 1) {  // inclusive Hillis-Steele scan
+        const unsigned x = threadIdx.x >= (unsigned)d ? s_part[threadIdx.x - d] : 0u;
         __syncthreads();
-        s_part[threadIdx.x] += v;
+        s_part[threadIdx.x] += x;
         __syncthreads();
     }
-    unsigned run = s_part[threadIdx.x] - sum;  // exclusive prefix of this thread's run
-    for (size_t c = c0; c < c1; ++c) {
-        start[c] = run;
-        run += cnt[c];
+    unsigned run = s_part[threadIdx.x] - sum;
+    for (size_t t = t0; t < t1; ++t) {
+        const unsigned x = off[t];
+        off[t] = run;
+        run += x;
     }
 }
 
@@ -167,11 +246,42 @@ __global__ void __launch_bounds__(kThreads) place_kernel(SortedWs w, long long n
     if (key == kNoCell) return;
     const size_t cbase = (size_t)local * n * n;
     const unsigned slot = atomicAdd(w.cursor + cbase + key, 1u);
-    w.seg[base + w.start[cbase + key] + slot] = (unsigned)q;
+    w.seg[base + seg_start(w, local, n, key) + slot] = (unsigned)q;
 }
 
-// reduce: one thread per cell; orders the cell's point indices (insertion sort: segments are
-// short) and adds the values in that order to the cell's current value.
+// Orders a segment of at most K point indices in registers (adjacent compare-exchanges of an
+// unrolled insertion sort; the padding sorts last), gathers the values, and adds them to acc in
+// index order.
+template <int K>
+__device__ __forceinline__ void sum_segment_in_registers(const unsigned *seg, unsigned len, const float2 *val,
+                                                         float2 &acc) {
+    unsigned idx[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) idx[j] = (unsigned)j < len ? seg[j] : 0xffffffffu;
+#pragma unroll
+    for (int i = 1; i < K; ++i) {
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+            const unsigned lo = min(idx[j - 1], idx[j]), hi = max(idx[j - 1], idx[j]);
+            idx[j - 1] = lo;
+            idx[j] = hi;
+        }
+    }
+    float2 v[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) v[j] = (unsigned)j < len ? val[idx[j]] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        if ((unsigned)j < len) {
+            acc.x = __fadd_rn(acc.x, v[j].x);
+            acc.y = __fadd_rn(acc.y, v[j].y);
+        }
+    }
+}
+
+// reduce: one thread per cell; orders the cell's point indices (in registers up to 16 points,
+// by insertion in the segment up to kShortSeg) and adds the values in that order to the cell's
+// current value.
 __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, int chunk_first, SortedWs w,
                                                           long long n_points) {
     const int n = p.n_pixels;
@@ -187,24 +297,34 @@ __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, in
         w.longs[(size_t)local * long_cap(n_points / 2) + slot] = (unsigned)c;
         return;
     }
-    unsigned *seg = w.seg + (size_t)local * n_points + w.start[cbase + c];
-    for (unsigned i = 1; i < len; ++i) {
-        const unsigned v = seg[i];
-        unsigned j = i;
-        while (j > 0 && seg[j - 1] > v) {
-            seg[j] = seg[j - 1];
-            --j;
-        }
-        seg[j] = v;
-    }
     const int img = chunk_first + local;
     float2 *cell = p.grids + (size_t)(img - p.img_base) * cells + c;
-    float2 acc = *cell;
+    float2 acc = p.grids_zero ? make_float2(0.f, 0.f) : *cell;
+    unsigned *seg = w.seg + (size_t)local * n_points + seg_start(w, local, n, c);
     const float2 *val = w.val + (size_t)local * n_points;
-    for (unsigned i = 0; i < len; ++i) {
-        const float2 v = val[seg[i]];
+    if (len == 1) {
+        const float2 v = val[seg[0]];
         acc.x = __fadd_rn(acc.x, v.x);
         acc.y = __fadd_rn(acc.y, v.y);
+    } else if (len <= 4) {
+        sum_segment_in_registers<4>(seg, len, val, acc);
+    } else if (len <= 16) {
+        sum_segment_in_registers<16>(seg, len, val, acc);
+    } else {
+        for (unsigned i = 1; i < len; ++i) {
+            const unsigned v = seg[i];
+            unsigned j = i;
+            while (j > 0 && seg[j - 1] > v) {
+                seg[j] = seg[j - 1];
+                --j;
+            }
+            seg[j] = v;
+        }
+        for (unsigned i = 0; i < len; ++i) {
+            const float2 v = val[seg[i]];
+            acc.x = __fadd_rn(acc.x, v.x);
+            acc.y = __fadd_rn(acc.y, v.y);
+        }
     }
     *cell = acc;
     if (p.counter_mode == BGI_COUNTERS_PER_IMAGE || (p.counter_mode == BGI_COUNTERS_FIRST_INTERVAL && img < p.n_channels)) {
@@ -232,7 +352,7 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, 
         const unsigned c = w.longs[(size_t)local * long_cap(n_points / 2) + li];
         const size_t cbase = (size_t)local * cells;
         const unsigned len = w.cnt[cbase + c];
-        const unsigned st = w.start[cbase + c];
+        const unsigned st = seg_start(w, local, n, c);
         const unsigned *seg = w.seg + (size_t)local * n_points + st;
         unsigned *ordered = w.key + (size_t)local * n_points + st;
         for (unsigned i0 = 0; i0 < len; i0 += kLongThreads) {
@@ -251,7 +371,7 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, 
         __syncthreads();
         float2 *cell = p.grids + (size_t)(img - p.img_base) * cells + c;
         float2 acc = make_float2(0.f, 0.f);
-        if (threadIdx.x == 0) acc = *cell;
+        if (threadIdx.x == 0 && !p.grids_zero) acc = *cell;
         const float2 *val = w.val + (size_t)local * n_points;
         for (unsigned j0 = 0; j0 < len; j0 += kTile) {
             const unsigned m = min((unsigned)kTile, len - j0);
@@ -314,8 +434,20 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
             keys_kernel<<<dim3(bx_b, k), kThreads, 0, s>>>(p, img0 + done, wd);
             if ((st = check_launch("gridding_sorted keys"))) return st;
         }
-        scan_kernel<<<cnt, 1024, 0, s>>>(w, n);
-        if ((st = check_launch("gridding_sorted scan"))) return st;
+        for (int done = 0; done < cnt; done += 65535) {
+            const int k = std::min(65535, cnt - done);
+            SortedWs wd = w;
+            wd.cnt += (size_t)done * n * n;
+            wd.start += (size_t)done * n * n;
+            wd.tile_off += (size_t)done * scan_tiles(n);
+            if ((size_t)n * n % 4 == 0)
+                scan_tiles_kernel<true><<<dim3((unsigned)scan_tiles(n), k), kThreads, 0, s>>>(wd, n);
+            else
+                scan_tiles_kernel<false><<<dim3((unsigned)scan_tiles(n), k), kThreads, 0, s>>>(wd, n);
+            if ((st = check_launch("gridding_sorted scan tiles"))) return st;
+        }
+        scan_offsets_kernel<<<cnt, 1024, 0, s>>>(w, n);
+        if ((st = check_launch("gridding_sorted scan offsets"))) return st;
         for (int done = 0; done < cnt; done += 65535) {
             const int k = std::min(65535, cnt - done);
             SortedWs wd = w;
@@ -325,6 +457,7 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
             wd.cnt += (size_t)done * n * n;
             wd.start += (size_t)done * n * n;
             wd.cursor += (size_t)done * n * n;
+            wd.tile_off += (size_t)done * scan_tiles(n);
             place_kernel<<<dim3(bx_p, k), kThreads, 0, s>>>(wd, n_points, n);
             if ((st = check_launch("gridding_sorted place"))) return st;
             wd.n_long += done;

@@ -215,6 +215,10 @@ class Imager:
         call("bgi_image_host", self._h, _ptr(vis), T, int(flags), _ptr(out), _stream(stream))
         return out
 
+    def set_deterministic(self, enable: bool = True):
+        """Grid by sort and ordered per-cell sums (full plane): the same image bits on every run."""
+        call("bgi_set_deterministic", self._h, int(bool(enable)))
+
     def set_stage_timing(self, enable: bool = True):
         call("bgi_set_stage_timing", self._h, int(bool(enable)))
 

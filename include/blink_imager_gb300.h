@@ -216,6 +216,11 @@ BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n
                               double delta_v, int n_pixels, double min_uv, int pol, float *images,
                               void *stream);
 
+/* Deterministic mode (default off): bgi_image and bgi_image_host grid with the ordered
+ * per-cell sums of bgi_gridding_sorted_gpu on the full plane, so every image is the same bits
+ * on every run and whatever else shares the call.  No reference counterpart. */
+BGI_API int bgi_set_deterministic(bgi_imager *im, int enable);
+
 /* Stage timing of bgi_image: when enabled, CUDA events are recorded on the stream of each
  * launch around it: gridding, the first FFT pass (rows in place, or the half-plane column
  * pass) and the second (columns with fftshift and normalisation, or the complex-to-real row

@@ -156,3 +156,34 @@ def test_sorted_workspace_errors(im):
     odd = torch.empty(per + 64, dtype=torch.uint8, device="cuda")[8:]
     with pytest.raises(capi.BgiError):
         im.gridding_sorted(*args, workspace=odd)
+
+
+def test_deterministic_imager(im):
+    """bgi_image in deterministic mode: the images match the oracle within the image
+    tolerance, and are the same bits across runs, wave sizes and the host entry point."""
+    n = 128
+    obs = synth.small(seed=43, n_ant=40, n_intervals=2, n_channels=3, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, counters, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n,
+                                             pol="I", n_uvw_sets=2)
+    outs = []
+    for wave in (0, 1, 4):
+        h = im.Imager(n, 2.0, "I", -1000.0, max_images_per_wave=wave)
+        h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+        h.set_frequencies(obs.freqs)
+        h.set_deterministic(True)
+        a = h.image(dev(vis)).cpu().numpy()
+        b = h.image(dev(vis)).cpu().numpy()
+        assert np.array_equal(_bits(a), _bits(b))
+        c = h.image_host(np.ascontiguousarray(vis))
+        assert np.array_equal(_bits(a), _bits(c))
+        assert np.array_equal(h.weight_sums(6), counters.reshape(6, -1).sum(1).astype(np.uint32))
+        h.close()
+        outs.append(a)
+    for a in outs[1:]:
+        assert np.array_equal(_bits(a), _bits(outs[0]))
+    a = outs[0]
+    for i in range(a.shape[0]):
+        for j in range(a.shape[1]):
+            d = np.asarray(a[i, j], np.complex128) - ref[i, j]
+            assert np.linalg.norm(d) / np.linalg.norm(ref[i, j]) < 1e-4, (i, j)
