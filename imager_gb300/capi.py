@@ -18,6 +18,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_STATE = 0, -1, -2, -3
 POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 COUNTERS_FIRST_INTERVAL, COUNTERS_PER_IMAGE = 0, 1
 APPLY_GEOMETRIC, APPLY_CABLE = 0x1, 0x2
+VIS_FORMAT = {"c64": 0, "s16": 1, "bf16": 2, "fp16": 3}
 
 
 class BgiError(RuntimeError):
@@ -44,6 +45,10 @@ _SIGNATURES = {
     "bgi_gridding_sorted_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _i,
                                      _vp, _vp, _vp, C.c_size_t, _vp]),
     "bgi_fft_inverse_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
+    "bgi_compressed_size": (_i, [_i, _i, _i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "bgi_compress_visibilities": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "bgi_image_compressed": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp]),
+    "bgi_image_compressed_host": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp]),
     "bgi_fft_shift_and_norm_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp]),
     "bgi_vector_sum_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),

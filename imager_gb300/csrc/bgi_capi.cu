@@ -135,6 +135,7 @@ struct bgi_imager {
     DevBuf<unsigned char> sorted_ws[kLanes];
     DevBuf<unsigned int> wsum;    // per-image weight counts of the last call
     DevBuf<float> io_vis, io_img; // device staging of bgi_image_host
+    DevBuf<float> io_scales;      // block scales staged by bgi_image_compressed_host
     int last_images = 0;
 
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
@@ -392,6 +393,7 @@ int bgi_destroy(bgi_imager *im) {
     if (im->copy_out) cudaStreamDestroy(im->copy_out);
     im->wsum.release();
     im->io_vis.release();
+    im->io_scales.release();
     im->io_img.release();
     delete im;
     return BGI_OK;
@@ -540,9 +542,12 @@ int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *w
 }
 
 GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
-                        const void *images) {
+                        const void *images, int format = BGI_VIS_C64, const float *scales = nullptr) {
     GridParams p{};
     p.vis = vis;
+    p.vis_format = format;
+    p.vis_scales = scales;
+    p.vis_blocks = vis_blocks(im->n_baselines);
     p.u = im->d_u;
     p.v = im->d_v;
     p.w = im->d_w;
@@ -615,17 +620,25 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
 
 extern "C" {
 
-int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
-              void *stream) {
+}  // extern "C"
+
+namespace {
+
+int image_impl(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals, unsigned flags,
+               float *images, void *stream) {
     BGI_TRY(image_checks(im, n_intervals, flags));
-    if (!vis || !images) return set_error(BGI_ERR_INVALID, "image: null buffer");
-    if (!aligned16(vis) || (reinterpret_cast<uintptr_t>(images) & 7u) != 0)
-        return set_error(BGI_ERR_INVALID, "image: vis must be 16-byte and images 8-byte aligned");
+    const float *vis = static_cast<const float *>(data);
+    if (!vis || !images || (format != BGI_VIS_C64 && !scales)) return set_error(BGI_ERR_INVALID, "image: null buffer");
+    const uintptr_t need = format == BGI_VIS_C64 ? 15u : 3u;
+    if ((reinterpret_cast<uintptr_t>(vis) & need) != 0 || (reinterpret_cast<uintptr_t>(scales) & 3u) != 0 ||
+        (reinterpret_cast<uintptr_t>(images) & 7u) != 0)
+        return set_error(BGI_ERR_INVALID, "image: visibilities must be 16-byte (complex64) or 4-byte (16-bit) "
+                                          "aligned, scales 4-byte and images 8-byte aligned");
     BGI_TRY(im->activate());
     cudaStream_t s = as_stream(stream);
     const int n_images = n_intervals * im->n_channels;
     int wave = 0, n_lanes = 0;
-    const GridParams p = block_params(im, vis, n_intervals, flags, images);
+    const GridParams p = block_params(im, vis, n_intervals, flags, images, format, scales);
     BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
     cudaStream_t streams[bgi_imager::kLanes] = {s, s};
     if (n_lanes > 1) {
@@ -649,26 +662,86 @@ int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags,
     return BGI_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images, void *stream) {
+    return image_impl(im, BGI_VIS_C64, vis, nullptr, n_intervals, flags, images, stream);
+}
+
+int bgi_image_compressed(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals,
+                         unsigned flags, float *images, void *stream) {
+    if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
+        return set_error(BGI_ERR_INVALID, "image_compressed: bad format %d", format);
+    return image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+}
+
+int bgi_compressed_size(int n_ant, int n_channels, int n_intervals, size_t *data_bytes, size_t *scale_bytes) {
+    if (n_ant < 1 || n_channels < 1 || n_intervals < 0 || !data_bytes || !scale_bytes)
+        return set_error(BGI_ERR_INVALID, "compressed_size: bad arguments");
+    const size_t imgs = (size_t)n_channels * n_intervals;
+    const long long nb = baselines_of(n_ant);
+    *data_bytes = imgs * 4 * (size_t)nb * sizeof(uint32_t);
+    *scale_bytes = imgs * 4 * (size_t)vis_blocks(nb) * sizeof(float);
+    return BGI_OK;
+}
+
+int bgi_compress_visibilities(const float *vis, int n_ant, int n_channels, int n_intervals, int format, void *data,
+                              float *scales, void *stream) {
+    if (!vis || !data || !scales || n_ant < 1 || n_channels < 1 || n_intervals < 0)
+        return set_error(BGI_ERR_INVALID, "compress: bad arguments");
+    if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
+        return set_error(BGI_ERR_INVALID, "compress: bad format %d", format);
+    if (!aligned16(vis) || (reinterpret_cast<uintptr_t>(data) & 3u) != 0 || (reinterpret_cast<uintptr_t>(scales) & 3u) != 0)
+        return set_error(BGI_ERR_INVALID, "compress: vis must be 16-byte, data and scales 4-byte aligned");
+    return launch_compress(vis, baselines_of(n_ant), (long long)n_channels * n_intervals, format, data, scales,
+                           as_stream(stream));
+}
+
+}  // extern "C"
+
+namespace {
+
+// Pol planes of a block-scaled block that a pol needs (planes XX=0, XY=1, YX=2, YY=3).
+int planes_for(int pol, int out[2]) {
+    switch (pol) {
+        case BGI_POL_XX: out[0] = 0; return 1;
+        case BGI_POL_YY: out[0] = 3; return 1;
+        case BGI_POL_I: out[0] = 0, out[1] = 3; return 2;
+        default: out[0] = 1, out[1] = 2; return 2;
+    }
+}
+
 // Host buffers: the block is cut into chunks of whole waves; each chunk's visibilities go up on
-// a copy stream, its waves run on the lanes as soon as they have landed, and its images come
-// back on a second copy stream as soon as they are done, so uploads, imaging and downloads of
+// a copy stream (for the block-scaled formats only the pol planes the image needs, and their
+// scales), its waves run on the lanes as soon as they have landed, and its images come back on
+// a second copy stream as soon as they are done, so uploads, imaging and downloads of
 // different chunks overlap.
-int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsigned flags,
-                   float *images_host, void *stream) {
+int image_host_impl(bgi_imager *im, int format, const void *vis_host, const float *scales_host, int n_intervals,
+                    unsigned flags, float *images_host, void *stream) {
     BGI_TRY(image_checks(im, n_intervals, flags));
-    if (!vis_host || !images_host) return set_error(BGI_ERR_INVALID, "image_host: null buffer");
+    if (!vis_host || !images_host || (format != BGI_VIS_C64 && !scales_host))
+        return set_error(BGI_ERR_INVALID, "image_host: null buffer");
     BGI_TRY(im->activate());
     cudaStream_t s = as_stream(stream);
     const int n_images = n_intervals * im->n_channels;
-    const size_t rec_floats = (size_t)im->n_baselines * 8;  // one image's visibility records
+    const long long nb = im->n_baselines, nblk = vis_blocks(nb);
+    const bool planar = format != BGI_VIS_C64;
+    const size_t rec_floats = (size_t)nb * (planar ? 4 : 8);  // one image's stored visibilities
+    const size_t sc_floats = planar ? (size_t)4 * nblk : 0;
     const size_t img_floats = (size_t)im->cfg.n_pixels * im->cfg.n_pixels * 2;
     BGI_TRY(im->io_vis.ensure(rec_floats * n_images, "image_host vis staging"));
+    if (planar) BGI_TRY(im->io_scales.ensure(sc_floats * n_images, "image_host scale staging"));
     BGI_TRY(im->io_img.ensure(img_floats * n_images, "image_host image staging"));
     int wave = 0, n_lanes = 0;
-    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr);
+    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, format,
+                                      planar ? im->io_scales.ptr : nullptr);
     BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
     BGI_TRY(im->ensure_lanes());
     BGI_TRY(im->ensure_copy_streams());
+    int planes[2] = {0, 0};
+    const int n_planes = planar ? planes_for(im->cfg.pol, planes) : 0;
     // about eight chunks of whole waves
     const int waves_total = (n_images + wave - 1) / wave;
     const int chunk = wave * std::max(1, (waves_total + 7) / 8);
@@ -680,12 +753,28 @@ int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsig
     for (int l = 0; l < n_lanes; ++l)
         BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_fork, 0), "fork wait"));
     int next = 0;
+    const float *src = static_cast<const float *>(vis_host);
     for (int c = 0; c < n_chunks; ++c) {
         const int img0 = c * chunk;
         const int cnt = std::min(chunk, n_images - img0);
-        BGI_TRY(check_cuda(cudaMemcpyAsync(im->io_vis.ptr + rec_floats * img0, vis_host + rec_floats * img0,
-                                           sizeof(float) * rec_floats * cnt, cudaMemcpyHostToDevice, im->copy_in),
-                           "image_host H2D"));
+        if (!planar) {
+            BGI_TRY(check_cuda(cudaMemcpyAsync(im->io_vis.ptr + rec_floats * img0, src + rec_floats * img0,
+                                               sizeof(float) * rec_floats * cnt, cudaMemcpyHostToDevice, im->copy_in),
+                               "image_host H2D"));
+        } else {
+            for (int q = 0; q < n_planes; ++q) {
+                const size_t off = rec_floats * img0 + (size_t)planes[q] * nb;
+                BGI_TRY(check_cuda(cudaMemcpy2DAsync(im->io_vis.ptr + off, sizeof(float) * rec_floats, src + off,
+                                                     sizeof(float) * rec_floats, sizeof(float) * nb, cnt,
+                                                     cudaMemcpyHostToDevice, im->copy_in),
+                                   "image_host H2D planes"));
+                const size_t soff = sc_floats * img0 + (size_t)planes[q] * nblk;
+                BGI_TRY(check_cuda(cudaMemcpy2DAsync(im->io_scales.ptr + soff, sizeof(float) * sc_floats,
+                                                     scales_host + soff, sizeof(float) * sc_floats,
+                                                     sizeof(float) * nblk, cnt, cudaMemcpyHostToDevice, im->copy_in),
+                                   "image_host H2D scales"));
+            }
+        }
         BGI_TRY(check_cuda(cudaEventRecord(im->ev_in[c], im->copy_in), "chunk in record"));
         for (int l = 0; l < n_lanes; ++l)
             BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_in[c], 0), "chunk in wait"));
@@ -704,6 +793,22 @@ int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsig
     BGI_TRY(check_cuda(cudaStreamWaitEvent(s, im->ev_join[0], 0), "join wait"));
     im->last_images = n_images;
     return check_cuda(cudaStreamSynchronize(s), "image_host sync");
+}
+
+}  // namespace
+
+extern "C" {
+
+int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsigned flags,
+                   float *images_host, void *stream) {
+    return image_host_impl(im, BGI_VIS_C64, vis_host, nullptr, n_intervals, flags, images_host, stream);
+}
+
+int bgi_image_compressed_host(bgi_imager *im, int format, const void *data_host, const float *scales_host,
+                              int n_intervals, unsigned flags, float *images_host, void *stream) {
+    if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
+        return set_error(BGI_ERR_INVALID, "image_compressed_host: bad format %d", format);
+    return image_host_impl(im, format, data_host, scales_host, n_intervals, flags, images_host, stream);
 }
 
 int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream) {

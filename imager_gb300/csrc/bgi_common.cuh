@@ -1,6 +1,7 @@
 // Shared device helpers of the BLINK GB300 imaging kernels.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -9,7 +10,10 @@
 namespace bgi {
 
 constexpr double kVelLight = 299792458.0;  // src/pacer_imager_defs.h:12-13
-constexpr float kMaxVis = 1e12f;           // src/pacer_imager_defs.h:21 (1e12 is exact in float)
+// src/pacer_imager_defs.h:21: a component passes when |x| < 1e12, compared in double.  1e12 is
+// not a float; the float test |x| < 1000000061440 (the first float above 1e12) passes exactly
+// the same values (the largest float below 1e12 is 999999995904).
+constexpr float kMaxVis = 1000000061440.0f;
 
 // ------------------------------------------------------------------------------------------
 // Host-side error reporting (thread-local message, status codes of blink_imager_gb300.h)
@@ -131,6 +135,48 @@ __device__ __forceinline__ void load_pols(const float2 *rec, float2 &a, float2 &
     else if (POL == BGI_POL_YY) a = __ldcs(rec + 3);
     else if (POL == BGI_POL_I) { a = __ldcs(rec); b = __ldcs(rec + 3); }
     else { a = __ldcs(rec + 1); b = __ldcs(rec + 2); }
+}
+
+// ---- block-scaled 16-bit visibilities ------------------------------------------------------
+constexpr int kVisBlock = 128;  // baselines per scale block of a pol plane
+
+// one stored complex value (re in the low half, im in the high half) times its block scale
+template <int FMT>
+__device__ __forceinline__ float2 decode_vis(uint32_t e, float scale) {
+    const uint16_t r = (uint16_t)(e & 0xffffu), i = (uint16_t)(e >> 16);
+    float x, y;
+    if (FMT == BGI_VIS_S16) {
+        x = r == 0x8000u ? __int_as_float(0x7fc00000) : (float)(int16_t)r;
+        y = i == 0x8000u ? __int_as_float(0x7fc00000) : (float)(int16_t)i;
+    } else if (FMT == BGI_VIS_BF16) {
+        x = __uint_as_float((uint32_t)r << 16);
+        y = __uint_as_float((uint32_t)i << 16);
+    } else {
+        x = __half2float(__ushort_as_half(r));
+        y = __half2float(__ushort_as_half(i));
+    }
+    return make_float2(__fmul_rn(x, scale), __fmul_rn(y, scale));
+}
+
+// Loads the pols that POL needs (as load_pols) from pol planes: data [img][4][B] of uint32,
+// scales [img][4][NB].
+template <int POL, int FMT>
+__device__ __forceinline__ void load_pols_planar(const uint32_t *data, const float *scales, size_t img,
+                                                 long long nb, long long nblk, long long b, float2 &a,
+                                                 float2 &bb) {
+    const uint32_t *d = data + img * 4 * nb + b;
+    const float *sc = scales + img * 4 * nblk + b / kVisBlock;
+    if (POL == BGI_POL_XX) {
+        a = decode_vis<FMT>(__ldcs(d), __ldg(sc));
+    } else if (POL == BGI_POL_YY) {
+        a = decode_vis<FMT>(__ldcs(d + 3 * nb), __ldg(sc + 3 * nblk));
+    } else if (POL == BGI_POL_I) {
+        a = decode_vis<FMT>(__ldcs(d), __ldg(sc));
+        bb = decode_vis<FMT>(__ldcs(d + 3 * nb), __ldg(sc + 3 * nblk));
+    } else {
+        a = decode_vis<FMT>(__ldcs(d + nb), __ldg(sc + nblk));
+        bb = decode_vis<FMT>(__ldcs(d + 2 * nb), __ldg(sc + 2 * nblk));
+    }
 }
 
 template <int POL>

@@ -21,7 +21,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kCPT = 4;  // images per thread
 
-template <int POL, bool COUNTERS, bool HALF>
+template <int POL, bool COUNTERS, bool HALF, int FMT>
 __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
     __shared__ ChannelConst s_cc[kCPT];
     __shared__ unsigned int s_count[kCPT];
@@ -50,7 +50,11 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
             if (j < n_here) {
                 const size_t img = (size_t)img_first + j;
                 const size_t off = (p.n_uvw_sets > 1 ? (size_t)t * nb : 0) + b;
-                load_pols<POL>(reinterpret_cast<const float2 *>(p.vis) + (img * nb + b) * 4, pa[j], pb[j]);
+                if (FMT == BGI_VIS_C64)
+                    load_pols<POL>(reinterpret_cast<const float2 *>(p.vis) + (img * nb + b) * 4, pa[j], pb[j]);
+                else
+                    load_pols_planar<POL, FMT>(reinterpret_cast<const uint32_t *>(p.vis), p.vis_scales, img, nb,
+                                               p.vis_blocks, b, pa[j], pb[j]);
                 uu[j] = p.u[off];
                 vv[j] = p.v[off];
                 if (p.apply_geom) ww[j] = p.w[off];
@@ -135,17 +139,30 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
     }
 }
 
+template <int POL, int FMT>
+void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
+    if (q.half_width > 0) grid_kernel<POL, false, true, FMT><<<grid, kThreads, 0, s>>>(q);
+    else grid_kernel<POL, false, false, FMT><<<grid, kThreads, 0, s>>>(q);
+}
+
 template <int POL>
 void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
-    if (q.half_width > 0) grid_kernel<POL, false, true><<<grid, kThreads, 0, s>>>(q);
-    else if (q.counter_mode >= 0) grid_kernel<POL, true, false><<<grid, kThreads, 0, s>>>(q);
-    else grid_kernel<POL, false, false><<<grid, kThreads, 0, s>>>(q);
+    switch (q.vis_format) {
+        case BGI_VIS_S16: launch_fmt<POL, BGI_VIS_S16>(grid, q, s); break;
+        case BGI_VIS_BF16: launch_fmt<POL, BGI_VIS_BF16>(grid, q, s); break;
+        case BGI_VIS_FP16: launch_fmt<POL, BGI_VIS_FP16>(grid, q, s); break;
+        default:
+            if (q.counter_mode >= 0) grid_kernel<POL, true, false, BGI_VIS_C64><<<grid, kThreads, 0, s>>>(q);
+            else launch_fmt<POL, BGI_VIS_C64>(grid, q, s);
+    }
 }
 
 }  // namespace
 
 int launch_gridding(const GridParams &p, cudaStream_t s) {
     if (p.img_count <= 0 || p.n_baselines <= 0) return BGI_OK;
+    if (p.vis_format != BGI_VIS_C64 && p.counter_mode >= 0)
+        return set_error(BGI_ERR_UNSUPPORTED, "gridding: counter grids need complex64 visibilities");
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;
     const int max_groups = 65535;
     for (int done = 0; done < p.img_count; done += max_groups * kCPT) {

@@ -21,7 +21,10 @@ int launch_cable(float *vis, int n_ant, int n_channels, int n_intervals, const d
 
 // ---- gridding (bgi_gridding.cu) ------------------------------------------------------------
 struct GridParams {
-    const float *vis;        // [T][C][B][4][2]
+    const float *vis;        // [T][C][B][4][2] (BGI_VIS_C64), or uint32 pol planes [T][C][4][B]
+    const float *vis_scales; // block-scaled formats: [T][C][4][vis_blocks]
+    long long vis_blocks;    // scale blocks per pol plane, ceil(B / 128)
+    int vis_format;          // enum bgi_vis_format
     const float *u, *v, *w;  // [n_uvw_sets][B]
     const float2 *dl;        // [B] L[a2]-L[a1] (cable delay) as a float pair (hi, lo), or null
     const int *flags;        // [B]
@@ -41,6 +44,11 @@ struct GridParams {
                                // cells instead of reading them first)
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
+
+// ---- block-scaled 16-bit visibilities (bgi_compress.cu) -------------------------------------
+long long vis_blocks(long long n_baselines);
+int launch_compress(const float *vis, long long n_baselines, long long n_images, int format, void *data,
+                    float *scales, cudaStream_t s);
 
 // ---- deterministic gridding (bgi_sorted.cu) ------------------------------------------------
 // Point indices 2*b(+1) are 32-bit: at most 46,340 antennas (about 1.07e9 baselines).

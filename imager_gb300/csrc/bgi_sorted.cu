@@ -82,6 +82,20 @@ SortedWs carve(void *ws, int chunk, long long nb, int n) {
     return w;
 }
 
+// the selected pol of one visibility, in any storage format
+template <int POL>
+__device__ __forceinline__ float2 load_selected(const GridParams &p, size_t img, long long nb, long long b) {
+    float2 a = make_float2(0.f, 0.f), bb = a;
+    const uint32_t *planes = reinterpret_cast<const uint32_t *>(p.vis);
+    switch (p.vis_format) {
+        case BGI_VIS_S16: load_pols_planar<POL, BGI_VIS_S16>(planes, p.vis_scales, img, nb, p.vis_blocks, b, a, bb); break;
+        case BGI_VIS_BF16: load_pols_planar<POL, BGI_VIS_BF16>(planes, p.vis_scales, img, nb, p.vis_blocks, b, a, bb); break;
+        case BGI_VIS_FP16: load_pols_planar<POL, BGI_VIS_FP16>(planes, p.vis_scales, img, nb, p.vis_blocks, b, a, bb); break;
+        default: load_pols<POL>(reinterpret_cast<const float2 *>(p.vis) + (img * nb + b) * 4, a, bb);
+    }
+    return combine_pols<POL>(a, bb);
+}
+
 // keys: grid x = baselines, y = images of the chunk
 __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int chunk_first, SortedWs w) {
     __shared__ ChannelConst s_cc;
@@ -98,13 +112,11 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
     unsigned k1 = kNoCell, k2 = kNoCell;
     float2 z = make_float2(0.f, 0.f);
     if (in_range && p.flags[b] <= 0) {
-        const float2 *rec = reinterpret_cast<const float2 *>(p.vis) + ((size_t)img * nb + b) * 4;
-        float2 a = make_float2(0.f, 0.f), bb = a;
         switch (p.pol) {
-            case BGI_POL_XX: load_pols<BGI_POL_XX>(rec, a, bb); z = combine_pols<BGI_POL_XX>(a, bb); break;
-            case BGI_POL_YY: load_pols<BGI_POL_YY>(rec, a, bb); z = combine_pols<BGI_POL_YY>(a, bb); break;
-            case BGI_POL_I: load_pols<BGI_POL_I>(rec, a, bb); z = combine_pols<BGI_POL_I>(a, bb); break;
-            default: load_pols<BGI_POL_V>(rec, a, bb); z = combine_pols<BGI_POL_V>(a, bb); break;
+            case BGI_POL_XX: z = load_selected<BGI_POL_XX>(p, img, nb, b); break;
+            case BGI_POL_YY: z = load_selected<BGI_POL_YY>(p, img, nb, b); break;
+            case BGI_POL_I: z = load_selected<BGI_POL_I>(p, img, nb, b); break;
+            default: z = load_selected<BGI_POL_V>(p, img, nb, b); break;
         }
         if (p.apply_geom || p.apply_cable) {
             float d_hi, d_lo;

@@ -13,7 +13,7 @@ import numpy as np
 import torch
 
 from . import capi
-from .capi import APPLY_CABLE, APPLY_GEOMETRIC, POL, call
+from .capi import APPLY_CABLE, APPLY_GEOMETRIC, POL, VIS_FORMAT, call
 
 __all__ = ["Imager", "apply_geometric_corrections", "apply_cable_corrections", "gridding",
            "fft_inverse", "fft_shift_and_norm", "vector_sum", "image_averaging",
@@ -109,6 +109,19 @@ def gridding_sorted(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv,
          _ptr(freqs), float(delta_u), float(delta_v), int(n_pixels), float(min_uv),
          POL[pol] if isinstance(pol, str) else int(pol), int(counter_mode), _ptr(counters),
          _ptr(grids), _ptr(workspace), workspace.numel(), _stream(stream))
+
+
+def compress_visibilities(vis, fmt="s16", stream=None):
+    """Block-scaled 16-bit storage of device visibilities complex64 [T][C][B][4] (or float32
+    [T][C][B][4][2]): returns (data uint16 [T][C][4][B][2], scales float32 [T][C][4][ceil(B/128)])
+    on the same device."""
+    T, Cn, B = _vis_dims(vis)
+    nblk = (B + 127) // 128
+    data = torch.empty((T, Cn, 4, B, 2), dtype=torch.int16, device=vis.device)
+    scales = torch.empty((T, Cn, 4, nblk), dtype=torch.float32, device=vis.device)
+    call("bgi_compress_visibilities", _ptr(vis), _n_ant(B), Cn, T, VIS_FORMAT[fmt], _ptr(data), _ptr(scales),
+         _stream(stream))
+    return data, scales
 
 
 def fft_inverse(grids, images, stream=None):
@@ -213,6 +226,28 @@ class Imager:
         if out is None:
             out = np.empty((T, Cn, n, n), np.complex64)
         call("bgi_image_host", self._h, _ptr(vis), T, int(flags), _ptr(out), _stream(stream))
+        return out
+
+    def image_compressed(self, data, scales, fmt="s16", flags: int = APPLY_GEOMETRIC | APPLY_CABLE, out=None,
+                         stream=None) -> torch.Tensor:
+        """Dirty images of block-scaled 16-bit device visibilities (compress_visibilities)."""
+        T, Cn = int(data.shape[0]), int(data.shape[1])
+        n = self.n_pixels
+        if out is None:
+            out = torch.empty((T, Cn, n, n), dtype=torch.complex64, device=data.device)
+        call("bgi_image_compressed", self._h, VIS_FORMAT[fmt], _ptr(data), _ptr(scales), T, int(flags), _ptr(out),
+             _stream(stream))
+        return out
+
+    def image_compressed_host(self, data, scales, fmt="s16", flags: int = APPLY_GEOMETRIC | APPLY_CABLE,
+                              out=None, stream=None):
+        """Host buffers in and out; uploads only the pol planes the handle's pol needs."""
+        T, Cn = int(data.shape[0]), int(data.shape[1])
+        n = self.n_pixels
+        if out is None:
+            out = np.empty((T, Cn, n, n), np.complex64)
+        call("bgi_image_compressed_host", self._h, VIS_FORMAT[fmt], _ptr(data), _ptr(scales), T, int(flags),
+             _ptr(out), _stream(stream))
         return out
 
     def set_deterministic(self, enable: bool = True):

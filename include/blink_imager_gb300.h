@@ -57,6 +57,19 @@ enum bgi_status {
  * (src/gridding.hpp:4). */
 enum bgi_pol { BGI_POL_XX = 0, BGI_POL_YY = 1, BGI_POL_I = 2, BGI_POL_V = 3 };
 
+/* Visibility storage.  BGI_VIS_C64 is the reference's layout, float[T][C][B][4 pols][re,im]
+ * (pols XX, XY, YX, YY).  The block-scaled 16-bit formats (no reference counterpart) store
+ * pol planes, data uint16[T][C][4][B][re,im], with one float scale per block of 128 baselines
+ * of a plane (256 components): scales float[T][C][4][ceil(B/128)], value = element * scale.
+ * A component that is NaN or has |x| >= 1e12 (skipped by the gridding) is stored as invalid
+ * and read back as NaN; m is the largest |x| of a block's valid components (0 if none).
+ *   BGI_VIS_S16:  scale = m / 32767, element = rint(x / scale) as int16 (+-32767), invalid
+ *                 -32768.  Error <= scale / 2 per component (relative L2 about 3e-5).
+ *   BGI_VIS_BF16: scale = m (1 if m == 0), element = bfloat16(x / scale), nearest even;
+ *                 relative error up to 2^-9 per component (about 2e-3 relative L2).
+ *   BGI_VIS_FP16: as BF16 with IEEE binary16 elements; up to 2^-12 relative (about 2e-4). */
+enum bgi_vis_format { BGI_VIS_C64 = 0, BGI_VIS_S16 = 1, BGI_VIS_BF16 = 2, BGI_VIS_FP16 = 3 };
+
 /* Counter layout for bgi_gridding_gpu. */
 enum bgi_counter_mode {
     /* counters float[C][N][N], counted for interval 0 only (src/gpu/gridding_gpu.cpp:107,117) */
@@ -193,6 +206,23 @@ BGI_API int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigne
  * synchronises the stream before returning. */
 BGI_API int bgi_image_host(bgi_imager *im, const float *vis_host, int n_intervals, unsigned flags,
                    float *images_host, void *stream);
+
+/* Block-scaled 16-bit visibilities (enum bgi_vis_format; no reference counterpart).
+ * bgi_compressed_size gives the bytes of a block's data and scales; bgi_compress_visibilities
+ * encodes complex64 visibilities float[T][C][B][4][2] (device) into them, bit for bit as the
+ * format states.  bgi_image_compressed / bgi_image_compressed_host image such a block as
+ * bgi_image / bgi_image_host do (corrections, if flagged, applied to the decoded values); the
+ * gridding reads only the pol planes the handle's pol needs, and the host variant uploads only
+ * those planes and their scales.  Device data must be 4-byte aligned. */
+BGI_API int bgi_compressed_size(int n_ant, int n_channels, int n_intervals, size_t *data_bytes,
+                                size_t *scale_bytes);
+BGI_API int bgi_compress_visibilities(const float *vis, int n_ant, int n_channels, int n_intervals,
+                                      int format, void *data, float *scales, void *stream);
+BGI_API int bgi_image_compressed(bgi_imager *im, int format, const void *data, const float *scales,
+                                 int n_intervals, unsigned flags, float *images, void *stream);
+BGI_API int bgi_image_compressed_host(bgi_imager *im, int format, const void *data_host,
+                                      const float *scales_host, int n_intervals, unsigned flags,
+                                      float *images_host, void *stream);
 
 /* Per-image weight sums (number of gridded points) of the last bgi_image call on this
  * handle, as uint32[n_images]; copies to host and synchronises the stream. */

@@ -117,6 +117,15 @@ void bgo_image_average(const float *images, int64_t image_size, int n_images, fl
 
 int bgo_max_threads(void);
 
+/* Block-scaled 16-bit visibility storage of the GB300 imager (no reference counterpart; the
+ * format is stated in blink_compress.c).  format: BGO_VIS_S16, BGO_VIS_BF16 or BGO_VIS_FP16. */
+enum { BGO_VIS_C64 = 0, BGO_VIS_S16 = 1, BGO_VIS_BF16 = 2, BGO_VIS_FP16 = 3 };
+int64_t bgo_compressed_blocks(int64_t n_baselines);
+void bgo_compress(const float *vis, int64_t n_images, int64_t n_baselines, int format,
+                  uint16_t *data, float *scales);
+void bgo_decompress(const uint16_t *data, const float *scales, int64_t n_images,
+                    int64_t n_baselines, int format, float *vis);
+
 #ifdef __cplusplus
 }
 #endif

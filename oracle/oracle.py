@@ -25,6 +25,8 @@ POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
+VIS_FORMAT = {"c64": 0, "s16": 1, "bf16": 2, "fp16": 3}
 
 _lib = None
 _ref = None
@@ -66,6 +68,9 @@ def library():
             "bgo_vector_sum": (None, [_f32p, i64, i32, _f64p]),
             "bgo_image_average": (None, [_f32p, i64, i32, _f32p]),
             "bgo_max_threads": (i32, []),
+            "bgo_compressed_blocks": (i64, [i64]),
+            "bgo_compress": (None, [_f32p, i64, i64, i32, _u16p, _f32p]),
+            "bgo_decompress": (None, [_u16p, _f32p, i64, i64, i32, _f32p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -234,3 +239,25 @@ def full_pipeline(vis_raw, u, v, w, cable, flags, freqs, n_pixels, osf=2.0, min_
                                   n_uvw_sets=n_uvw_sets)
     images = image_f64(grids, counters)
     return vis, grids, counters, images, (du, dv)
+
+
+def compress(vis, fmt="s16"):
+    """Block-scaled 16-bit storage of vis float32 [T][C][B][4][2] (blink_compress.c): returns
+    (data uint16 [T][C][4][B][2], scales float32 [T][C][4][ceil(B/128)])."""
+    vis = np.ascontiguousarray(vis, np.float32)
+    T, Cn, nb = vis.shape[:3]
+    nblk = int(library().bgo_compressed_blocks(nb))
+    data = np.empty((T, Cn, 4, nb, 2), np.uint16)
+    scales = np.empty((T, Cn, 4, nblk), np.float32)
+    library().bgo_compress(vis.reshape(-1), T * Cn, nb, VIS_FORMAT[fmt], data.reshape(-1), scales.reshape(-1))
+    return data, scales
+
+
+def decompress(data, scales, fmt="s16"):
+    """Inverse of compress(): float32 visibilities [T][C][B][4][2]."""
+    data = np.ascontiguousarray(data, np.uint16)
+    scales = np.ascontiguousarray(scales, np.float32)
+    T, Cn, _, nb = data.shape[:4]
+    vis = np.empty((T, Cn, nb, 4, 2), np.float32)
+    library().bgo_decompress(data.reshape(-1), scales.reshape(-1), T * Cn, nb, VIS_FORMAT[fmt], vis.reshape(-1))
+    return vis

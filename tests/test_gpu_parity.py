@@ -136,6 +136,24 @@ def test_gridding_rounding_ties_and_wraps(im):
         _check_grids(g, g_ref)
 
 
+def test_gridding_max_vis_edge(im):
+    """|x| < 1e12 is decided in double by the reference (src/pacer_imager.cpp:329): the float
+    just below 1e12 is gridded, the float just above is skipped."""
+    obs = synth.small(seed=9, n_ant=16, n_intervals=1, n_channels=2, n_pixels=64)
+    vis = obs.vis_f32().copy()
+    below, above = np.float32(999999995904.0), np.float32(1000000061440.0)
+    vis[0, 0, 22, 0, 0] = below      # baselines 22-25: antenna 6 with antennas 1-4
+    vis[0, 0, 23, 0, 1] = -below
+    vis[0, 1, 24, 0, 0] = above
+    vis[0, 1, 25, 0, 1] = -above
+    umax, vmax = O.uv_max(obs.u, obs.v, obs.flags)
+    du, dv = O.delta_uv(2.0, umax, 64), O.delta_uv(2.0, vmax, 64)
+    g_ref, c_ref, n_ref = O.gridding(vis, obs.u, obs.v, obs.flags, obs.freqs, du, dv, 64)
+    g, c = _grid_gpu(im, vis, obs.u, obs.v, obs.flags, obs.freqs, du, dv, 64, -1000.0, "XX", 1)
+    assert np.array_equal(c, c_ref)
+    assert (np.abs(g) >= 9e11).sum() >= 2  # the two components just below 1e12 were gridded
+
+
 def test_gridding_against_reference_golden(im):
     """bgi_gridding_gpu on the reference's corrected visibilities reproduces the reference's
     counters exactly and its grids to summation order, including the 48-pixel case."""

@@ -119,3 +119,55 @@ def test_cell_index_edges(oracle_lib):
     assert O.cell_index(5.0, 0.0, 1.0, 1.0, lam, -1.0, 64, +1) == 3
     assert O.cell_index(-5.0, 0.0, 1.0, 1.0, lam, -1.0, 64, +1) == 64 - 3
     del c
+
+
+def test_compress_encoders_round_to_nearest_even(oracle_lib):
+    """The storage oracle's 16-bit encoders (oracle/blink_compress.c) agree with numpy's
+    binary16 and torch's bfloat16 conversions (both round to nearest even): a block whose
+    largest component is 1.0 stores x / 1.0 = x."""
+    O = oracle_lib
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    n = 128 * 64
+    x = (rng.standard_normal(n * 8) * 10.0 ** rng.integers(-9, 1, n * 8)).astype(np.float32)
+    x = np.clip(x, -0.999, 0.999)
+    x[:16] = np.float32([6.1035156e-05, 6.097555e-05, 5.9604645e-08, 2.9802322e-08, 2.9802326e-08,
+                         8.9406967e-08, 0.5, -0.5, 1e-30, -1e-30, 0.0, -0.0, 0.33333334, 2.0 ** -14,
+                         2.0 ** -24 * 1.5, 2.0 ** -24 * 2.5])
+    vis = x.reshape(1, 1, n, 4, 2).copy()
+    vis[0, 0, ::128, :, 0] = 1.0  # every block's max is exactly 1
+    for fmt in ("fp16", "bf16"):
+        data, scales = O.compress(vis, fmt)
+        assert np.all(scales == 1.0)
+        planar = np.ascontiguousarray(vis[0, 0].transpose(1, 0, 2))  # [4][B][2]
+        if fmt == "fp16":
+            want = planar.astype(np.float16).view(np.uint16)
+        else:
+            want = torch.from_numpy(planar).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
+        assert np.array_equal(data[0, 0], want), fmt
+        back = O.decompress(data, scales, fmt)
+        ref = want.view(np.float16).astype(np.float32) if fmt == "fp16" else \
+            torch.from_numpy(want.view(np.int16)).view(torch.bfloat16).float().numpy()
+        assert np.array_equal(back[0, 0].transpose(1, 0, 2), ref), fmt
+
+
+def test_compress_s16_known_answers(oracle_lib):
+    """S16: scale = max/32767, elements rint(x/scale) clamped, invalid components -32768
+    and decoded as NaN, an all-zero block has scale 0."""
+    O = oracle_lib
+    vis = np.zeros((1, 1, 130, 4, 2), np.float32)
+    vis[0, 0, 0, 0] = (3.0, -1.5)
+    vis[0, 0, 1, 0] = (np.nan, 0.75)
+    vis[0, 0, 2, 0] = (2e12, 1.0)
+    vis[0, 0, 129, 0] = (-4.0, 0.0)   # second block of the XX plane
+    data, scales = O.compress(vis, "s16")
+    assert scales.shape == (1, 1, 4, 2)
+    assert scales[0, 0, 0, 0] == np.float32(3.0) / np.float32(32767.0)
+    assert scales[0, 0, 1, 0] == 0.0 and scales[0, 0, 0, 1] == np.float32(4.0) / np.float32(32767.0)
+    e = data[0, 0, 0].view(np.int16)
+    assert e[0, 0] == 32767 and e[0, 1] in (-16384, -16383)
+    assert e[1, 0] == -32768 and e[2, 0] == -32768
+    assert e[129, 0] == -32767
+    back = O.decompress(data, scales, "s16")
+    assert np.isnan(back[0, 0, 1, 0, 0]) and np.isnan(back[0, 0, 2, 0, 0])
+    assert back[0, 0, 0, 0, 0] == np.float32(32767) * scales[0, 0, 0, 0]
