@@ -2,13 +2,18 @@
 """Benchmark of the GB300 BLINK dirty-imaging path; prints one JSON line on rank 0.
 
 Workload (one step): a block of 256 antennas (32,896 baselines incl. autos), 64 channels over
-150-180 MHz x 10 intervals of 1 s with Earth-rotated zenith UVW, complex64 4-pol
-visibilities (673 MB), imaged to 640 dirty images of 512x512 (pol XX, oversampling 2, natural
-weighting): geometric + cable corrections, nearest-neighbour gridding, inverse 2D FFT,
-fftshift and normalisation.  Inputs are seeded synthetic data with that shape (no public data
-set exists for this path).
+150-180 MHz x 10 intervals of 1 s with Earth-rotated zenith UVW, 4-pol visibilities, imaged to
+640 dirty images of 512x512 (pol XX, oversampling 2, natural weighting): geometric + cable
+corrections, nearest-neighbour gridding, inverse 2D FFT, fftshift and normalisation.  Inputs are
+seeded synthetic data with that shape (no public data set exists for this path).
 
-  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+The timed step images the block from its stored form (--storage): by default 16-bit block
+floating point (int16 pol planes with one FP32 scale per 128 baselines, encoded once before
+timing, as stored data), checked against the FP64 oracle of the original complex64
+visibilities; complex64 storage, bf16/fp16 storage, the deterministic gridder, the full-plane
+path and the reference's plain FP32 call sequence are timed beside it as variants.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--storage s16|c64|bf16|fp16]
 
 `--impl reference` times the reference's CPU imaging path (the C restatement in oracle/, run
 with every host thread) on bounded samples of the same workload.  Under torchrun each rank
@@ -169,9 +174,115 @@ def run_reference(args, rank, world):
 # ------------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------------
+SAMPLES = ((0, 0), (-1, 63), (4, 31))  # (interval, channel) of the images checked each run
+
+
+def sample_references(obs, du, dv, T):
+    """FP64 oracle images of the sample images from the original complex64 visibilities."""
+    from oracle import oracle as O
+    O.build()
+    vis_np = obs.vis_f32()
+    refs = {}
+    for t, c in SAMPLES:
+        t = t % T
+        corr = np.ascontiguousarray(vis_np[t:t + 1, c:c + 1])
+        O.apply_geometric(corr, np.ascontiguousarray(obs.w[t:t + 1]), obs.freqs[c:c + 1])
+        O.apply_cable(corr, obs.cable, obs.freqs[c:c + 1])
+        g, cnt, _ = O.gridding(corr, obs.u[t:t + 1], obs.v[t:t + 1], obs.flags, obs.freqs[c:c + 1], du, dv,
+                               obs.n_pixels)
+        refs[(t, c)] = O.image_f64(g, cnt)[0, 0]
+    return refs
+
+
+def image_errors(out, refs):
+    """Per sample image: relative L2, max |err| / max |ref| and RMS err / RMS ref; the worst of each."""
+    worst = {"rel_l2": 0.0, "max_err_rel": 0.0, "rms_err_rel": 0.0}
+    for (t, c), ref in refs.items():
+        got = out[t, c].cpu().numpy().astype(np.complex128)
+        d = np.abs(got - ref)
+        worst["rel_l2"] = max(worst["rel_l2"], float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        worst["max_err_rel"] = max(worst["max_err_rel"], float(d.max() / np.abs(ref).max()))
+        worst["rms_err_rel"] = max(worst["rms_err_rel"], float(np.sqrt((d ** 2).mean() / (np.abs(ref) ** 2).mean())))
+    return worst
+
+
+L2_FLUSH_BYTES = 512 << 20  # written between timed steps: four times the 129 MB L2
+
+
+class L2Flush:
+    def __init__(self):
+        import torch
+        self.buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.buf.zero_()
+
+
+def timed_steps(step, k, stream, flush, pre=None):
+    """Total ms of k steps, each bracketed by its own CUDA events on `stream` with the L2 flushed
+    before it (outside the events); `pre()`, when given, runs before the flush (outside too)."""
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    for e0, e1 in evs:
+        if pre:
+            pre()
+        flush()
+        e0.record(stream)
+        step()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return sum(e0.elapsed_time(e1) for e0, e1 in evs)
+
+
+def time_steps(step, k, stream, flush, pre=None):
+    """ms per step of `step()` over k steps after two untimed ones."""
+    import torch
+    for _ in range(2):
+        if pre:
+            pre()
+        step()
+    torch.cuda.synchronize()
+    return timed_steps(step, k, stream, flush, pre) / k
+
+
+def plain_dropin_step(obs, vis, du, dv, out):
+    """The reference GPU imager's call sequence (src/gpu/pacer_imager_hip.cpp:36-146) through
+    the free functions: corrections in place, grids and counters zeroed, atomic gridding with
+    per-channel counters, unfused inverse FFT into the images, counter sums, fftshift and
+    normalisation -- FP32 and complex64 throughout, full plane, no fusion."""
+    import torch
+    from imager_gb300 import capi
+    from imager_gb300 import imager as IM
+    T, Cn, B = vis.shape[:3]
+    N = obs.n_pixels
+    work = torch.empty_like(vis)
+    w, cable, freqs = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (obs.w, obs.cable, obs.freqs))
+    u, v, flags = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (obs.u, obs.v, obs.flags))
+    grids = torch.empty((T, Cn, N, N), dtype=torch.complex64, device="cuda")
+    counters = torch.empty((Cn, N, N), dtype=torch.float32, device="cuda")
+    fnorm = torch.empty(Cn, dtype=torch.float32, device="cuda")
+
+    def step():
+        IM.apply_geometric_corrections(work, w, freqs, n_uvw_sets=T)
+        IM.apply_cable_corrections(work, cable, freqs)
+        grids.zero_()
+        counters.zero_()
+        IM.gridding(work, u, v, flags, freqs, du, dv, N, -1000.0, "XX", grids, counters,
+                    counter_mode=capi.COUNTERS_FIRST_INTERVAL, n_uvw_sets=T)
+        IM.fft_inverse(grids, out)
+        IM.vector_sum(counters, N * N, Cn, fnorm)
+        IM.fft_shift_and_norm(out, fnorm)
+
+    def fresh():  # the reference corrects each block's visibilities in place once
+        work.copy_(vis)
+
+    return step, fresh
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from imager_gb300 import capi, synth
+    from imager_gb300 import imager as IM
     from imager_gb300.imager import APPLY_CABLE, APPLY_GEOMETRIC, Imager
 
     torch.cuda.set_device(local_rank)
@@ -187,14 +298,25 @@ def run_ours(args, rank, world, local_rank):
     vis_np = obs.vis_f32()
     vis = torch.from_numpy(vis_np).cuda()
     out = torch.empty((T, Cn, N, N), dtype=torch.complex64, device="cuda")
+    fmt = args.storage
+    # stored visibilities: the block arrives in the storage format (encoded once, untimed)
+    stored = {f: IM.compress_visibilities(vis, f) for f in ("s16", "bf16", "fp16")}
+    torch.cuda.synchronize()
     im = Imager(N, 2.0, "XX", -1000.0, max_images_per_wave=args.wave)
     im.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
     im.set_frequencies(obs.freqs)
     flags = APPLY_GEOMETRIC | APPLY_CABLE
     stream = torch.cuda.current_stream()
 
+    def step_for(h, f):
+        if f == "c64":
+            return lambda: h.image(vis, flags=flags, out=out)
+        d, sc = stored[f]
+        return lambda: h.image_compressed(d, sc, f, flags=flags, out=out)
+
+    step = step_for(im, fmt)
     for _ in range(args.warmup):
-        im.image(vis, flags=flags, out=out)
+        step()
     torch.cuda.synchronize()
     sums = im.weight_sums(n_images)
     gridded_vis = int(sums.sum()) // 2  # each gridded visibility lands at two cells
@@ -204,21 +326,20 @@ def run_ours(args, rank, world, local_rank):
     clocks = ClockSampler(uuid if len(uuid.replace("GPU-", "")) == 36 else "")
     clocks.start()
     time.sleep(0.3)
-    im.set_stage_timing(True)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush = L2Flush()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.monotonic()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        im.image(vis, flags=flags, out=out)
-    ev1.record(stream)
-    torch.cuda.synchronize()
+    ms = timed_steps(step, args.steps, stream, flush)
     t1 = time.monotonic()
     if dist:
         dist.barrier()
-    ms = ev0.elapsed_time(ev1)
+    # per-stage device times from a separate pass (the stage events cost a few percent, so the
+    # timed steps above run without them)
+    stage_steps = max(3, min(args.steps, 20))
+    im.set_stage_timing(True)
+    timed_steps(step, stage_steps, stream, flush)
     stages = im.stage_times()
     im.set_stage_timing(False)
     if dist:
@@ -226,45 +347,83 @@ def run_ours(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
-    # variants of the same step, timed the same way over fewer steps
+    du, dv, _, _ = im.uv_cell
+    refs = sample_references(obs, du, dv, T) if rank == 0 else {}
+    errs = image_errors(out, refs) if rank == 0 else {}
+
+    # variants of the same step, timed the same way over fewer steps, with their sample errors
     variants = {}
     if args.variants:
-        def time_steps(h, k):
-            for _ in range(2):
-                h.image(vis, flags=flags, out=out)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(k):
-                h.image(vis, flags=flags, out=out)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            return e0.elapsed_time(e1) / k
-
         k = max(3, min(args.steps, 20))
+        for f in ("c64", "s16", "bf16", "fp16"):
+            if f == fmt:
+                continue
+            v_ms = time_steps(step_for(im, f), k, stream, flush)
+            variants[f"storage_{f}"] = {"images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms,
+                                        "steps": k, **({"errors_vs_fp64": image_errors(out, refs)} if rank == 0 else {})}
         im.set_deterministic(True)
-        v_ms = time_steps(im, k)
+        v_ms = time_steps(step, k, stream, flush)
         im.set_deterministic(False)
         variants["deterministic_sorted_gridding"] = {"images_per_s": world * n_images / (v_ms / 1000.0),
-                                                     "ms_per_step": v_ms, "steps": k, "plane": "full"}
+                                                     "ms_per_step": v_ms, "steps": k, "plane": "full",
+                                                     "storage": fmt}
         full = Imager(N, 2.0, "XX", -1000.0, max_images_per_wave=args.wave, full_plane=True)
         full.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
         full.set_frequencies(obs.freqs)
-        v_ms = time_steps(full, k)
+        v_ms = time_steps(step_for(full, fmt), k, stream, flush)
         full.close()
         variants["full_plane_atomic_gridding"] = {"images_per_s": world * n_images / (v_ms / 1000.0),
-                                                  "ms_per_step": v_ms, "steps": k, "plane": "full"}
+                                                  "ms_per_step": v_ms, "steps": k, "plane": "full", "storage": fmt}
+        out_r = torch.empty((T, Cn, N, N), dtype=torch.float32, device="cuda")
+        d, sc = stored[fmt] if fmt != "c64" else (None, None)
+        real_step = (lambda: im.image(vis, flags=flags | IM.OUTPUT_REAL, out=out_r)) if fmt == "c64" else \
+            (lambda: im.image_compressed(d, sc, fmt, flags=flags | IM.OUTPUT_REAL, out=out_r))
+        v_ms = time_steps(real_step, k, stream, flush)
+        variants["real_output"] = {"images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms,
+                                   "steps": k, "storage": fmt,
+                                   "what": "BGI_OUTPUT_REAL: float images (the real part) from the last FFT pass",
+                                   **({"errors_vs_fp64": image_errors(out_r.to(torch.complex64), refs)}
+                                      if rank == 0 else {})}
+        del out_r
+        plain_step, plain_fresh = plain_dropin_step(obs, vis, du, dv, out)
+        v_ms = time_steps(plain_step, k, stream, flush, pre=plain_fresh)
+        refs0 = {key: r for key, r in refs.items() if key[0] == 0}  # per-channel norm equals per-image at t=0
+        variants["plain_fp32_dropin"] = {
+            "images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms, "steps": k,
+            "what": "reference GPU call order through the free functions: corrections in place, gridding "
+                    "with counters, unfused FFT, vector sum, fftshift+norm; complex64/FP32, full plane",
+            **({"errors_vs_fp64_interval0": image_errors(out, refs0)} if rank == 0 else {})}
 
     # end to end through the host-buffer entry point: pinned input, pinned output
-    vis_h = torch.from_numpy(vis_np).pin_memory()
     out_h = torch.empty((T, Cn, N, N), dtype=torch.complex64).pin_memory()
+    if fmt == "c64":
+        vis_h = torch.from_numpy(vis_np).pin_memory()
+        e2e_step = lambda: im.image_host(vis_h, flags=flags, out=out_h)  # noqa: E731
+        h2d = vis_np.nbytes
+    else:
+        d_h = stored[fmt][0].cpu().pin_memory()
+        s_h = stored[fmt][1].cpu().pin_memory()
+        e2e_step = lambda: im.image_compressed_host(d_h, s_h, fmt, flags=flags, out=out_h)  # noqa: E731
+        n_planes = 1  # pol XX reads one plane
+        h2d = n_images * n_planes * (B * 4 + int(s_h.shape[-1]) * 4)
     e2e_steps = max(3, min(args.steps, 20))
-    im.image_host(vis_h, flags=flags, out=out_h)
+    e2e_step()
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     for _ in range(e2e_steps):
-        im.image_host(vis_h, flags=flags, out=out_h)
+        e2e_step()
     e2e_s = (time.perf_counter() - t2) / e2e_steps
+    if args.variants:  # the same through the host entry point with real images coming back
+        out_hr = torch.empty((T, Cn, N, N), dtype=torch.float32).pin_memory()
+        e2e_real = (lambda: im.image_host(vis_h, flags=flags | IM.OUTPUT_REAL, out=out_hr)) if fmt == "c64" else \
+            (lambda: im.image_compressed_host(d_h, s_h, fmt, flags=flags | IM.OUTPUT_REAL, out=out_hr))
+        e2e_real()
+        t4 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_real()
+        e2e_real_s = (time.perf_counter() - t4) / e2e_steps
+        variants["e2e_real_output"] = {"images_per_s": world * n_images / e2e_real_s, "h2d_bytes_per_step": h2d,
+                                       "d2h_bytes_per_step": n_images * N * N * 4}
     t3 = time.monotonic()
     clocks.stop()
     if dist:
@@ -276,37 +435,24 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
         return 0
 
-    # parity spot check of the timed output: three images against the FP64 oracle
-    from oracle import oracle as O
-    O.build()
-    du, dv, _, _ = im.uv_cell
-    tl = T - 1
-    corr = np.ascontiguousarray(vis_np[[0, tl]][:, [0, 63]])
-    O.apply_geometric(corr, np.ascontiguousarray(obs.w[[0, tl]]), obs.freqs[[0, 63]], n_uvw_sets=2)
-    O.apply_cable(corr, obs.cable, obs.freqs[[0, 63]])
-    errs = []
-    for k, (t, c) in enumerate(((0, 0), (tl, 63))):
-        g, cnt, _ = O.gridding(corr[k:k + 1, k:k + 1], obs.u[t:t + 1], obs.v[t:t + 1], obs.flags,
-                               obs.freqs[c:c + 1], du, dv, N)
-        ref = O.image_f64(g, cnt)[0, 0]
-        got = out[t, c].cpu().numpy().astype(np.complex128)
-        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
-
     images_per_s = world * n_images * args.steps / (ms / 1000.0)
     hbm_peak, peak_kind = measured_peaks()
     # algorithmic bytes per image of each stage
     # algorithmic bytes per image of each stage, for the path the handle took
+    # stored visibility bytes per image that the gridding must read: the complex64 record, or
+    # for the 16-bit formats the one pol plane XX needs and its block scales
+    vis_bytes = B * 32 if fmt == "c64" else B * 4 + int(stored[fmt][1].shape[-1]) * 4
     half = im.half_plane
     if half:
         hw = N * (N // 2 + 1) * 8  # half-plane grid of one image
-        alg = {"gridding": B * 32 + hw, "fft_pass1": 2 * hw, "fft_pass2": hw + 8 * N * N}
+        alg = {"gridding": vis_bytes + hw, "fft_pass1": 2 * hw, "fft_pass2": hw + 8 * N * N}
     else:
-        alg = {"gridding": B * 32 + 8 * N * N, "fft_pass1": 16 * N * N, "fft_pass2": 16 * N * N}
+        alg = {"gridding": vis_bytes + 8 * N * N, "fft_pass1": 16 * N * N, "fft_pass2": 16 * N * N}
     stage_info = {}
     for k, (tot_ms, launches) in stages.items():
         if launches:
             per_launch_ms = tot_ms / launches
-            imgs_per_launch = n_images * args.steps / launches
+            imgs_per_launch = n_images * stage_steps / launches
             gbs = alg[k] * imgs_per_launch / (per_launch_ms / 1000.0) / 1e9
             stage_info[k] = {"ms_per_launch": per_launch_ms, "launches": launches,
                              "images_per_launch": imgs_per_launch, "achieved_gbs": gbs,
@@ -316,8 +462,9 @@ def run_ours(args, rank, world, local_rank):
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
             tr = json.load(f)
-        if dom in tr.get("bytes_per_image", {}):
-            traffic = tr["bytes_per_image"][dom] * stage_info[dom]["images_per_launch"]
+        per_image = tr.get("bytes_per_image", {}).get(fmt, {})
+        if dom in per_image:
+            traffic = per_image[dom] * stage_info[dom]["images_per_launch"]
     except Exception:
         traffic = None
     roof = {"kernel": dom, "bound": "hbm", "achieved": stage_info[dom]["achieved_gbs"], "peak": hbm_peak,
@@ -328,21 +475,28 @@ def run_ours(args, rank, world, local_rank):
             "path": "half plane (complex-to-real)" if half else "full plane"}
 
     cpu_rate, cpu_times, cpu_threads = cpu_sample_rate(obs, 16, args.cpu_seconds)
-    h2d = vis_np.nbytes
     d2h = n_images * N * N * 8
+    plain = variants.get("plain_fp32_dropin", {}).get("images_per_s")
     line = {
         "metric": METRIC, "value": images_per_s, "unit": "images/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "storage": {"c64": "complex64 (the reference's layout)",
+                    "s16": "16-bit block floating point: int16 pol planes, one FP32 scale per 128 baselines",
+                    "bf16": "bfloat16 pol planes, one FP32 scale per 128 baselines",
+                    "fp16": "binary16 pol planes, one FP32 scale per 128 baselines"}[fmt],
+        "vs_plain_fp32_dropin": images_per_s / plain if plain else None,
         "data": "synthetic (seeded; shapes and distributions of the workload)",
         "config": {"workload": WORKLOAD if T == 10 else WORKLOAD.replace("10 intervals", f"{T} intervals"),
                    "images_per_step": n_images, "n_pixels": N, "baselines": B,
                    "wave_images": args.wave or "auto",
-                   "l2": "inputs (673 MB visibilities) and outputs (1.34 GB images) larger than L2 (129 MB)",
+                   "l2": "flushed before every timed step (512 MB written outside the step's events)",
+                   "bytes_per_step": {"stored_visibilities_read": n_images * vis_bytes, "images_written": d2h},
                    "parallelism": "one block per GPU, no collective" if world > 1 else "single GPU"},
         "vis_per_s": world * gridded_vis * args.steps / (ms / 1000.0),
         "e2e": {"value": world * n_images / e2e_s, "unit": "images/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "api": "bgi_image_host (pinned host buffers)"},
+                "d2h_bytes_per_step": d2h,
+                "api": ("bgi_image_host" if fmt == "c64" else "bgi_image_compressed_host") + " (pinned host buffers)"},
         "roofline": roof,
         "stages": stage_info,
         "cpu_baseline": {"value": cpu_rate, "unit": "images/s", "cores": cpu_threads, "kind": "port",
@@ -350,9 +504,11 @@ def run_ours(args, rank, world, local_rank):
                                    f"{len(cpu_times)} repetitions: corrections, gridding, FP32 FFT, "
                                    "normalise, shift (oracle/ restatement, OpenMP)"},
         "clocks": clocks.summary(t0, t3),
-        "gpu_launches": sum(v[1] for v in stages.values()),
+        "gpu_launches": sum(v[1] for v in stages.values()) * args.steps // stage_steps,
         "variants": variants,
-        "parity_sample_rel_l2": max(errs),
+        "parity_sample_rel_l2": errs["rel_l2"],
+        "errors_vs_fp64": {**errs, "images": [f"interval {t % T}, channel {c}" for t, c in SAMPLES],
+                           "oracle": "FP64 oracle of the original complex64 visibilities"},
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -368,6 +524,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--wave", type=int, default=0, help="images per launch wave (0 = auto)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--storage", choices=["s16", "bf16", "fp16", "c64"], default="s16",
+                    help="visibility storage of the timed step (s16: 16-bit block floating point)")
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip timing the deterministic and full-plane variants")
     ap.add_argument("--intervals", type=int, default=10,

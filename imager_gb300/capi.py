@@ -17,7 +17,7 @@ HEADER = os.path.join(_build.ROOT, "include", "blink_imager_gb300.h")
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_STATE = 0, -1, -2, -3, -4, -5
 POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 COUNTERS_FIRST_INTERVAL, COUNTERS_PER_IMAGE = 0, 1
-APPLY_GEOMETRIC, APPLY_CABLE = 0x1, 0x2
+APPLY_GEOMETRIC, APPLY_CABLE, OUTPUT_REAL = 0x1, 0x2, 0x4
 VIS_FORMAT = {"c64": 0, "s16": 1, "bf16": 2, "fp16": 3}
 
 

@@ -496,7 +496,8 @@ static int image_checks(bgi_imager *im, int n_intervals, unsigned flags) {
     if (n_intervals < 1) return set_error(BGI_ERR_INVALID, "image: n_intervals must be >= 1");
     if (im->n_uvw_sets != 1 && im->n_uvw_sets != n_intervals)
         return set_error(BGI_ERR_INVALID, "image: array has %d UVW sets for %d intervals", im->n_uvw_sets, n_intervals);
-    if (flags & ~(BGI_APPLY_GEOMETRIC | BGI_APPLY_CABLE)) return set_error(BGI_ERR_INVALID, "image: unknown flags");
+    if (flags & ~(BGI_APPLY_GEOMETRIC | BGI_APPLY_CABLE | BGI_OUTPUT_REAL))
+        return set_error(BGI_ERR_INVALID, "image: unknown flags");
     if (!(im->delta_u > 0) || !(im->delta_v > 0))
         return set_error(BGI_ERR_STATE, "image: u_max/v_max is zero (no unflagged baseline?)");
     return BGI_OK;
@@ -565,17 +566,23 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
     p.half_width = im->half_plane() && !im->deterministic ? half_plane_width(im->cfg.n_pixels) : 0;
-    if (!aligned16(images)) p.half_width = 0;  // the complex-to-real stores are 16 bytes wide
+    // the complex-to-real pass stores pixel pairs: 16 bytes of complex or 8 bytes of real pixels
+    if ((reinterpret_cast<uintptr_t>(images) & ((flags & BGI_OUTPUT_REAL) ? 7u : 15u)) != 0) p.half_width = 0;
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
     return p;
+}
+
+// First pixel of image img: complex images are npix float2 apart, real images npix floats.
+float2 *image_ptr(float2 *out, int img, size_t npix, bool real) {
+    return real ? reinterpret_cast<float2 *>(reinterpret_cast<float *>(out) + (size_t)img * npix) : out + (size_t)img * npix;
 }
 
 // Images [img_first, img_first + count) of a block, in waves of `wave` images that alternate on
 // streams[0..n_streams) starting at stream *next.  Per wave: gridding into the stream's grid
 // scratch, the row pass in place, the column pass into the images (clearing the scratch).
 int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int count, int wave,
-              cudaStream_t *streams, int n_streams, int *next) {
+              cudaStream_t *streams, int n_streams, int *next, bool real) {
     const int n = im->cfg.n_pixels;
     const size_t npix = (size_t)n * n;
     for (int img0 = img_first; img0 < img_first + count; img0 += wave) {
@@ -604,11 +611,11 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         if (p.half_width > 0) {
             BGI_TRY(launch_fft_cols_half(grid, n, cnt, ls));                   // in place, rows shifted
             BGI_TRY(im->mark(ls));
-            BGI_TRY(launch_c2r_rows(grid, out + (size_t)img0 * npix, n, cnt, ws, ls));  // clears the scratch
+            BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, ls, real));  // clears the scratch
         } else {
             BGI_TRY(launch_fft_rows(grid, grid, n, cnt, false, ls));  // in place in the scratch
             BGI_TRY(im->mark(ls));
-            BGI_TRY(launch_fft_cols_to(grid, out + (size_t)img0 * npix, n, cnt, ws, true, ls));  // clears the scratch
+            BGI_TRY(launch_fft_cols_to(grid, image_ptr(out, img0, npix, real), n, cnt, ws, true, ls, real));  // clears the scratch
         }
         BGI_TRY(im->mark(ls));
         im->grid_dirty[l] = false;
@@ -651,7 +658,7 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     }
     int next = 0;
     BGI_TRY(run_waves(im, p, reinterpret_cast<float2 *>(images), 0,
-                      n_images, wave, streams, n_lanes, &next));
+                      n_images, wave, streams, n_lanes, &next, (flags & BGI_OUTPUT_REAL) != 0));
     if (n_lanes > 1) {
         for (int l = 0; l < n_lanes; ++l) {
             BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[l], im->lane[l]), "join record"));
@@ -730,7 +737,8 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     const bool planar = format != BGI_VIS_C64;
     const size_t rec_floats = (size_t)nb * (planar ? 4 : 8);  // one image's stored visibilities
     const size_t sc_floats = planar ? (size_t)4 * nblk : 0;
-    const size_t img_floats = (size_t)im->cfg.n_pixels * im->cfg.n_pixels * 2;
+    const bool real = (flags & BGI_OUTPUT_REAL) != 0;
+    const size_t img_floats = (size_t)im->cfg.n_pixels * im->cfg.n_pixels * (real ? 1 : 2);
     BGI_TRY(im->io_vis.ensure(rec_floats * n_images, "image_host vis staging"));
     if (planar) BGI_TRY(im->io_scales.ensure(sc_floats * n_images, "image_host scale staging"));
     BGI_TRY(im->io_img.ensure(img_floats * n_images, "image_host image staging"));
@@ -779,7 +787,7 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
         for (int l = 0; l < n_lanes; ++l)
             BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_in[c], 0), "chunk in wait"));
         BGI_TRY(run_waves(im, p, reinterpret_cast<float2 *>(im->io_img.ptr), img0, cnt, wave, im->lane, n_lanes,
-                          &next));
+                          &next, real));
         for (int l = 0; l < n_lanes; ++l) {
             BGI_TRY(check_cuda(cudaEventRecord(im->ev_done[c * bgi_imager::kLanes + l], im->lane[l]), "chunk done"));
             BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_out, im->ev_done[c * bgi_imager::kLanes + l], 0),

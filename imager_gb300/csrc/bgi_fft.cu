@@ -352,10 +352,12 @@ __global__ void __launch_bounds__(Shape<N>::ROWS *Shape<N>::P) fft_rows_kernel(f
 // happen in the first pass, before any store, and no other block touches these columns, so the
 // pass may run in place (src == dst) even with the fftshift.  With SHIFT_NORM the stores apply
 // the fftshift and multiply by (float)(1/sum(w)); with ZERO_SRC the loads clear src behind them
-// (src != dst), and the final stores stream past L2.
-template <int N, bool SHIFT_NORM, bool ZERO_SRC>
+// (src != dst), and the final stores stream past L2.  With REAL (epilogue only) dst holds real
+// images float[N][N] and only the real parts are stored.
+template <int N, bool SHIFT_NORM, bool ZERO_SRC, bool REAL = false>
 __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_kernel(float2 *src, float2 *dst,
                                                                                     const unsigned int *wsum) {
+    static_assert(!REAL || SHIFT_NORM, "real output is written by the epilogue");
     using S = ColShape<N>;
     constexpr int COLS = S::COLS, CT = COLS / 2, TILES = (N / 2) / CT;
     extern __shared__ float2 smem[];
@@ -378,7 +380,10 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
                 r = (i + N / 2) & (N - 1);
                 v = make_float2(v.x * scale, v.y * scale);
             }
-            __stcs(out + (size_t)r * N + dcol, v);
+            if (REAL)
+                __stcs(reinterpret_cast<float *>(dst) + img * (size_t)N * N + (size_t)r * N + dcol, v.x);
+            else
+                __stcs(out + (size_t)r * N + dcol, v);
         },
         [&](int i) {
             if (ZERO_SRC) in[(size_t)i * N + col] = make_float2(0.f, 0.f);
@@ -448,8 +453,9 @@ struct C2RShape {
 // loads; the first pass forms Z[k] from X[k] and X[M-k]; the stores apply the fftshift of
 // columns (x -> (x + N/2) mod N keeps pairs 2m, 2m+1 together) and (float)(1/sum(w)), and
 // write each pair of complex pixels (zero imaginary parts) as one 16-byte store streaming past
-// L2: two 8-byte stores would each half-fill their sectors.
-template <int N>
+// L2: two 8-byte stores would each half-fill their sectors.  With REAL the images are float
+// [N][N] and each pixel pair is one 8-byte store.
+template <int N, bool REAL>
 __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
                                                                                     const unsigned int *wsum) {
     using S = C2RShape<N>;
@@ -491,7 +497,11 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
         [&](int m, float2 z) {
             // pixels x and x+1 as one 16-byte store (images are 16-byte aligned on this path)
             const int x = (2 * m + N / 2) & (N - 1);
-            __stcs(reinterpret_cast<float4 *>(dst + x), make_float4(z.x * scale, 0.f, z.y * scale, 0.f));
+            if (REAL)
+                __stcs(reinterpret_cast<float2 *>(reinterpret_cast<float *>(images) + row * N + x),
+                       make_float2(z.x * scale, z.y * scale));
+            else
+                __stcs(reinterpret_cast<float4 *>(dst + x), make_float4(z.x * scale, 0.f, z.y * scale, 0.f));
         });
 }
 
@@ -517,12 +527,14 @@ int rows_n(const float2 *src, float2 *dst, int n_images, bool zero_src, cudaStre
 }
 
 template <int N>
-int cols_n(float2 *src, float2 *dst, int n_images, const unsigned int *wsum, bool zero_src, cudaStream_t s) {
+int cols_n(float2 *src, float2 *dst, int n_images, const unsigned int *wsum, bool zero_src, bool real,
+           cudaStream_t s) {
     using S = ColShape<N>;
     const size_t smem = sizeof(float2) * ((size_t)S::COLS * S::STRIDE);
     const unsigned blocks = (unsigned)((size_t)n_images * (N / 2) / (S::COLS / 2));
-    auto k = wsum ? (zero_src ? fft_cols_kernel<N, true, true> : fft_cols_kernel<N, true, false>)
-                  : (zero_src ? fft_cols_kernel<N, false, true> : fft_cols_kernel<N, false, false>);
+    auto k = real ? fft_cols_kernel<N, true, true, true>
+                  : wsum ? (zero_src ? fft_cols_kernel<N, true, true> : fft_cols_kernel<N, true, false>)
+                         : (zero_src ? fft_cols_kernel<N, false, true> : fft_cols_kernel<N, false, false>);
     int st = prepare(k, smem);
     if (st) return st;
     k<<<blocks, S::COLS * S::P, smem, s>>>(src, dst, wsum);
@@ -542,11 +554,11 @@ int cols_half_n(float2 *grids, int n_images, cudaStream_t s) {
 }
 
 template <int N>
-int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, cudaStream_t s) {
+int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, bool real, cudaStream_t s) {
     using S = C2RShape<N>;
     const size_t smem = sizeof(float2) * ((size_t)S::ROWS * S::BUF);
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
-    auto k = c2r_rows_kernel<N>;
+    auto k = real ? c2r_rows_kernel<N, true> : c2r_rows_kernel<N, false>;
     int st = prepare(k, smem);
     if (st) return st;
     k<<<blocks, S::ROWS * S::P, smem, s>>>(grids, images, wsum);
@@ -640,19 +652,20 @@ int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsu
 }
 
 int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsigned int *wsum,
-                       bool zero_src, cudaStream_t s) {
+                       bool zero_src, cudaStream_t s, bool real) {
     if (n_images <= 0) return BGI_OK;
     if (zero_src && src == dst) return set_error(BGI_ERR_INVALID, "fft cols: clearing the source needs src != dst");
+    if (real && (!wsum || !zero_src)) return set_error(BGI_ERR_INVALID, "fft cols: real output is the epilogue's");
     switch (n) {
-        case 16: return cols_n<16>(src, dst, n_images, wsum, zero_src, s);
-        case 32: return cols_n<32>(src, dst, n_images, wsum, zero_src, s);
-        case 64: return cols_n<64>(src, dst, n_images, wsum, zero_src, s);
-        case 128: return cols_n<128>(src, dst, n_images, wsum, zero_src, s);
-        case 256: return cols_n<256>(src, dst, n_images, wsum, zero_src, s);
-        case 512: return cols_n<512>(src, dst, n_images, wsum, zero_src, s);
-        case 1024: return cols_n<1024>(src, dst, n_images, wsum, zero_src, s);
-        case 2048: return cols_n<2048>(src, dst, n_images, wsum, zero_src, s);
-        case 4096: return cols_n<4096>(src, dst, n_images, wsum, zero_src, s);
+        case 16: return cols_n<16>(src, dst, n_images, wsum, zero_src, real, s);
+        case 32: return cols_n<32>(src, dst, n_images, wsum, zero_src, real, s);
+        case 64: return cols_n<64>(src, dst, n_images, wsum, zero_src, real, s);
+        case 128: return cols_n<128>(src, dst, n_images, wsum, zero_src, real, s);
+        case 256: return cols_n<256>(src, dst, n_images, wsum, zero_src, real, s);
+        case 512: return cols_n<512>(src, dst, n_images, wsum, zero_src, real, s);
+        case 1024: return cols_n<1024>(src, dst, n_images, wsum, zero_src, real, s);
+        case 2048: return cols_n<2048>(src, dst, n_images, wsum, zero_src, real, s);
+        case 4096: return cols_n<4096>(src, dst, n_images, wsum, zero_src, real, s);
         default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
     }
 }
@@ -685,16 +698,16 @@ int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s) {
 }
 
 int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool real) {
     if (n_images <= 0) return BGI_OK;
     switch (n) {
-        case 64: return c2r_n<64>(grids, images, n_images, wsum, s);
-        case 128: return c2r_n<128>(grids, images, n_images, wsum, s);
-        case 256: return c2r_n<256>(grids, images, n_images, wsum, s);
-        case 512: return c2r_n<512>(grids, images, n_images, wsum, s);
-        case 1024: return c2r_n<1024>(grids, images, n_images, wsum, s);
-        case 2048: return c2r_n<2048>(grids, images, n_images, wsum, s);
-        case 4096: return c2r_n<4096>(grids, images, n_images, wsum, s);
+        case 64: return c2r_n<64>(grids, images, n_images, wsum, real, s);
+        case 128: return c2r_n<128>(grids, images, n_images, wsum, real, s);
+        case 256: return c2r_n<256>(grids, images, n_images, wsum, real, s);
+        case 512: return c2r_n<512>(grids, images, n_images, wsum, real, s);
+        case 1024: return c2r_n<1024>(grids, images, n_images, wsum, real, s);
+        case 2048: return c2r_n<2048>(grids, images, n_images, wsum, real, s);
+        case 4096: return c2r_n<4096>(grids, images, n_images, wsum, real, s);
         default: return set_error(BGI_ERR_UNSUPPORTED, "half-plane image side %d", n);
     }
 }

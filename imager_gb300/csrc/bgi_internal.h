@@ -69,8 +69,9 @@ int launch_fft_cols(float2 *images, int n, int n_images, const unsigned int *wsu
                     cudaStream_t s);
 // Column pass from src into dst (src == dst: in place); zero_src clears src behind the loads
 // (needs src != dst).  Final stores stream past L2.
+// real: dst holds real images float[N][N] (needs wsum and zero_src).
 int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsigned int *wsum,
-                       bool zero_src, cudaStream_t s);
+                       bool zero_src, cudaStream_t s, bool real = false);
 // Half-plane imaging (real images of Hermitian grids): grids [img][N][W] hold columns
 // u = 0..N/2 (W = half_plane_width(N), padding columns stay zero).
 int half_plane_width(int n);
@@ -79,8 +80,9 @@ int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s);
 // Complex-to-real row pass: half-plane rows -> image rows (fftshift of columns and
 // (float)(1/wsum) applied), clearing the grid rows it read.  Images are complex with zero
 // imaginary parts and must be 16-byte aligned.
+// real: images are float[N][N] (8-byte aligned) instead of complex.
 int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
-                    cudaStream_t s);
+                    cudaStream_t s, bool real = false);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
                           const float *fnorm, int fnorm_size, cudaStream_t s);
 int launch_vector_sum(const float *data, int64_t image_size, int n_images, float *sums,

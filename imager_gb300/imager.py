@@ -13,7 +13,7 @@ import numpy as np
 import torch
 
 from . import capi
-from .capi import APPLY_CABLE, APPLY_GEOMETRIC, POL, VIS_FORMAT, call
+from .capi import APPLY_CABLE, APPLY_GEOMETRIC, OUTPUT_REAL, POL, VIS_FORMAT, call
 
 __all__ = ["Imager", "apply_geometric_corrections", "apply_cable_corrections", "gridding",
            "fft_inverse", "fft_shift_and_norm", "vector_sum", "image_averaging",
@@ -45,6 +45,10 @@ def _n_ant(n_baselines: int) -> int:
     if n * (n + 1) // 2 != n_baselines:
         raise ValueError(f"{n_baselines} is not a triangular baseline count")
     return n
+
+
+def _out_dtype(flags):
+    return torch.float32 if flags & OUTPUT_REAL else torch.complex64
 
 
 def _vis_dims(vis: torch.Tensor):
@@ -214,7 +218,7 @@ class Imager:
         T, Cn, _ = _vis_dims(vis)
         n = self.n_pixels
         if out is None:
-            out = torch.empty((T, Cn, n, n), dtype=torch.complex64, device=vis.device)
+            out = torch.empty((T, Cn, n, n), dtype=_out_dtype(flags), device=vis.device)
         call("bgi_image", self._h, _ptr(vis), T, int(flags), _ptr(out), _stream(stream))
         return out
 
@@ -224,7 +228,7 @@ class Imager:
         Cn = int(vis.shape[1])
         n = self.n_pixels
         if out is None:
-            out = np.empty((T, Cn, n, n), np.complex64)
+            out = np.empty((T, Cn, n, n), np.float32 if flags & OUTPUT_REAL else np.complex64)
         call("bgi_image_host", self._h, _ptr(vis), T, int(flags), _ptr(out), _stream(stream))
         return out
 
@@ -234,7 +238,7 @@ class Imager:
         T, Cn = int(data.shape[0]), int(data.shape[1])
         n = self.n_pixels
         if out is None:
-            out = torch.empty((T, Cn, n, n), dtype=torch.complex64, device=data.device)
+            out = torch.empty((T, Cn, n, n), dtype=_out_dtype(flags), device=data.device)
         call("bgi_image_compressed", self._h, VIS_FORMAT[fmt], _ptr(data), _ptr(scales), T, int(flags), _ptr(out),
              _stream(stream))
         return out
@@ -245,7 +249,7 @@ class Imager:
         T, Cn = int(data.shape[0]), int(data.shape[1])
         n = self.n_pixels
         if out is None:
-            out = np.empty((T, Cn, n, n), np.complex64)
+            out = np.empty((T, Cn, n, n), np.float32 if flags & OUTPUT_REAL else np.complex64)
         call("bgi_image_compressed_host", self._h, VIS_FORMAT[fmt], _ptr(data), _ptr(scales), T, int(flags),
              _ptr(out), _stream(stream))
         return out

@@ -81,6 +81,11 @@ enum bgi_counter_mode {
 /* Flags of bgi_image / bgi_image_host. */
 #define BGI_APPLY_GEOMETRIC 0x1u /* ApplyGeometricCorrections (src/pacer_imager.cpp:463-464) */
 #define BGI_APPLY_CABLE 0x2u     /* ApplyCableCorrections (src/pacer_imager.cpp:466-473) */
+/* Real images float[T][C][N][N] instead of complex64 images: the real part, the part the
+ * reference's image averaging reads (src/utils.cpp:4-22), written by the last FFT pass with
+ * half the output bytes.  (On the half-plane path the images are real by construction; on the
+ * full plane the imaginary parts, rounding noise of a Hermitian grid, are dropped.) */
+#define BGI_OUTPUT_REAL 0x4u
 
 BGI_API const char *bgi_last_error(void);
 BGI_API int bgi_version(void); /* 100 * major + minor */

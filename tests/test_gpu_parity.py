@@ -408,3 +408,33 @@ def test_half_plane_falls_back_when_pixels_reach_the_side(im):
     for j in range(2):
         assert rel_l2(out[0, j], ref[0, j]) < IMAGE_TOL, j
     h.close()
+
+
+@pytest.mark.parametrize("full_plane", [False, True])
+@pytest.mark.parametrize("pol", ["XX", "I"])
+def test_image_real_output(im, full_plane, pol):
+    """BGI_OUTPUT_REAL: float images equal to the real part of the complex images (bit for bit
+    in deterministic mode), within the image tolerance of the oracle's real part, on device and
+    host buffers."""
+    n = 128
+    obs = synth.small(seed=53, n_ant=40, n_intervals=2, n_channels=3, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, _, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n, pol=pol,
+                                      n_uvw_sets=2)
+    h = _imager_for(im, obs, n, pol, full_plane=full_plane)
+    h.set_deterministic(True)
+    fl = im.APPLY_GEOMETRIC | im.APPLY_CABLE
+    cplx = h.image(dev(vis), flags=fl).cpu().numpy()
+    real = h.image(dev(vis), flags=fl | im.OUTPUT_REAL)
+    assert real.dtype == torch.float32 and tuple(real.shape) == (2, 3, n, n)
+    real = real.cpu().numpy()
+    assert np.array_equal(real.view(np.uint32), np.ascontiguousarray(cplx.real).view(np.uint32))
+    for i in range(2):
+        for j in range(3):
+            assert rel_l2(real[i, j], ref[i, j].real) < IMAGE_TOL, (i, j)
+    host = h.image_host(np.ascontiguousarray(vis), flags=fl | im.OUTPUT_REAL)
+    assert host.dtype == np.float32 and np.array_equal(host.view(np.uint32), real.view(np.uint32))
+    h.set_deterministic(False)
+    fast = h.image(dev(vis), flags=fl | im.OUTPUT_REAL).cpu().numpy()  # atomic gridder
+    assert rel_l2(fast, real) < 1e-6
+    h.close()
