@@ -64,6 +64,8 @@ _SIGNATURES = {
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
     "bgi_set_deterministic": (_i, [_vp, _i]),
+    "bgi_device_fault": (_i, [_i, C.POINTER(C.c_uint), _i]),
+    "bgi_selftest_wait_timeout": (_i, [_i, _vp]),
     "bgi_set_stage_timing": (_i, [_vp, _i]),
     "bgi_get_stage_times": (_i, [_vp, C.POINTER(_d), C.POINTER(_i64)]),
 }

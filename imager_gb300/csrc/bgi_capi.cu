@@ -119,6 +119,8 @@ struct bgi_imager {
     }
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
+    DevBuf<ChannelConst> d_cc; // per-channel gridding constants for the current delta_u/v
+    bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
     double *d_freqs = nullptr;
     // Two lanes (streams) image alternate waves, each with its own grid scratch, so one wave's
@@ -386,6 +388,7 @@ int bgi_destroy(bgi_imager *im) {
         im->grid[l].release();
         im->sorted_ws[l].release();
     }
+    im->d_cc.release();
     if (im->ev_fork) cudaEventDestroy(im->ev_fork);
     for (cudaEvent_t e : im->ev_in) cudaEventDestroy(e);
     for (cudaEvent_t e : im->ev_done) cudaEventDestroy(e);
@@ -441,6 +444,7 @@ int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, con
     im->u_max = um;
     im->v_max = vm;
     // src/pacer_imager.cpp:497-499: float oversampling factor promoted to double
+    im->cc_valid = false;
     im->delta_u = (double)im->cfg.oversampling_factor * um / im->cfg.n_pixels;
     im->delta_v = (double)im->cfg.oversampling_factor * vm / im->cfg.n_pixels;
     return BGI_OK;
@@ -458,6 +462,7 @@ int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz) 
                        "set_frequencies copy"));
     im->n_channels = n_channels;
     im->freq_max = *std::max_element(freqs_hz, freqs_hz + n_channels);
+    im->cc_valid = false;
     return BGI_OK;
 }
 
@@ -473,6 +478,7 @@ int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v) {
     if (im->n_ant == 0) return set_error(BGI_ERR_STATE, "set_uv_cell: array not set");
     if (!(delta_u > 0) || !(delta_v > 0) || !std::isfinite(delta_u) || !std::isfinite(delta_v))
         return set_error(BGI_ERR_INVALID, "set_uv_cell: delta_u/v must be finite and > 0");
+    im->cc_valid = false;
     im->delta_u = delta_u;
     im->delta_v = delta_v;
     return BGI_OK;
@@ -534,6 +540,11 @@ int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *w
         if (im->deterministic)
             BGI_TRY(im->sorted_ws[l].ensure(sorted_workspace_bytes(im->n_baselines, n, wave), "gridding workspace"));
     }
+    if (!im->cc_valid) {
+        BGI_TRY(im->d_cc.ensure((size_t)im->n_channels, "channel constants"));
+        BGI_TRY(launch_channel_consts(im->d_freqs, im->n_channels, im->delta_u, im->delta_v, im->d_cc.ptr, s));
+        im->cc_valid = true;
+    }
     BGI_TRY(im->wsum.ensure((size_t)n_images * kWsumStride, "weight sums"));
     BGI_TRY(check_cuda(cudaMemsetAsync(im->wsum.ptr, 0, sizeof(unsigned int) * kWsumStride * n_images, s),
                        "weight sums clear"));
@@ -555,6 +566,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.dl = im->d_dl;
     p.flags = im->d_flags;
     p.freqs = im->d_freqs;
+    p.chan_consts = nullptr;  // set after prepare_call builds the table
     p.du = im->delta_u;
     p.dv = im->delta_v;
     p.min_uv = im->cfg.min_uv;
@@ -645,8 +657,9 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     cudaStream_t s = as_stream(stream);
     const int n_images = n_intervals * im->n_channels;
     int wave = 0, n_lanes = 0;
-    const GridParams p = block_params(im, vis, n_intervals, flags, images, format, scales);
+    GridParams p = block_params(im, vis, n_intervals, flags, images, format, scales);
     BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
+    p.chan_consts = im->d_cc.ptr;
     cudaStream_t streams[bgi_imager::kLanes] = {s, s};
     if (n_lanes > 1) {
         BGI_TRY(im->ensure_lanes());
@@ -743,9 +756,10 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     if (planar) BGI_TRY(im->io_scales.ensure(sc_floats * n_images, "image_host scale staging"));
     BGI_TRY(im->io_img.ensure(img_floats * n_images, "image_host image staging"));
     int wave = 0, n_lanes = 0;
-    const GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, format,
+    GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, format,
                                       planar ? im->io_scales.ptr : nullptr);
     BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
+    p.chan_consts = im->d_cc.ptr;
     BGI_TRY(im->ensure_lanes());
     BGI_TRY(im->ensure_copy_streams());
     int planes[2] = {0, 0};
@@ -800,7 +814,11 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[0], im->copy_out), "join record"));
     BGI_TRY(check_cuda(cudaStreamWaitEvent(s, im->ev_join[0], 0), "join wait"));
     im->last_images = n_images;
-    return check_cuda(cudaStreamSynchronize(s), "image_host sync");
+    BGI_TRY(check_cuda(cudaStreamSynchronize(s), "image_host sync"));
+    unsigned int fault = 0;
+    BGI_TRY(read_device_fault(&fault, false));
+    if (fault) return set_error(BGI_ERR_CUDA, "image_host: device fault word 0x%x (a bounded wait gave up)", fault);
+    return BGI_OK;
 }
 
 }  // namespace
@@ -828,6 +846,25 @@ int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void
                                          sizeof(uint32_t) * kWsumStride, sizeof(uint32_t), n_images,
                                          cudaMemcpyDeviceToHost, s), "last_weight_sums copy"));
     return check_cuda(cudaStreamSynchronize(s), "last_weight_sums sync");
+}
+
+int bgi_device_fault(int device, unsigned int *fault_bits, int clear) {
+    if (!fault_bits) return set_error(BGI_ERR_INVALID, "device_fault: null output");
+    int prev = 0;
+    BGI_TRY(check_cuda(cudaGetDevice(&prev), "get device"));
+    BGI_TRY(check_cuda(cudaSetDevice(device), "set device"));
+    const int st = read_device_fault(fault_bits, clear != 0);
+    cudaSetDevice(prev);
+    return st;
+}
+
+int bgi_selftest_wait_timeout(int device, void *stream) {
+    int prev = 0;
+    BGI_TRY(check_cuda(cudaGetDevice(&prev), "get device"));
+    BGI_TRY(check_cuda(cudaSetDevice(device), "set device"));
+    const int st = launch_wait_timeout_selftest(as_stream(stream));
+    cudaSetDevice(prev);
+    return st;
 }
 
 int bgi_set_deterministic(bgi_imager *im, int enable) {

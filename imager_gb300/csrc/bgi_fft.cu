@@ -16,6 +16,7 @@
 //                partner at x + N/2, so shifted stores never race with another block's loads.
 //                In the fused path the stores apply the fftshift and the 1/sum(weights)
 //                normalisation (src/pacer_imager.cpp:171-179).
+#include "bgi_async.cuh"
 #include "bgi_internal.h"
 
 namespace bgi {
@@ -449,40 +450,58 @@ struct C2RShape {
 };
 
 // Complex-to-real pass: half-plane row y (already at its fftshifted position) -> image row y.
-// The row's N/2 + 1 values are staged in shared memory and cleared in the grid behind the
-// loads; the first pass forms Z[k] from X[k] and X[M-k]; the stores apply the fftshift of
-// columns (x -> (x + N/2) mod N keeps pairs 2m, 2m+1 together) and (float)(1/sum(w)), and
-// write each pair of complex pixels (zero imaginary parts) as one 16-byte store streaming past
-// L2: two 8-byte stores would each half-fill their sectors.  With REAL the images are float
-// [N][N] and each pixel pair is one 8-byte store.
+// One thread stages the block's rows (N/2 + 1 values each, rounded up to 16 bytes) in shared
+// memory with bulk asynchronous copies completing on an mbarrier, then clears them in the grid
+// with bulk stores from a zero row once they have landed; the first pass forms Z[k] from X[k]
+// and X[M-k]; the stores apply the fftshift of columns (x -> (x + N/2) mod N keeps pairs
+// 2m, 2m+1 together) and (float)(1/sum(w)), and write each pair of complex pixels (zero
+// imaginary parts) as one 16-byte store streaming past L2: two 8-byte stores would each
+// half-fill their sectors.  With REAL the images are float [N][N] and each pixel pair is one
+// 8-byte store.
+template <int N>
+constexpr unsigned c2r_row_bytes() {
+    return (unsigned)(((N / 2 + 1) * sizeof(float2) + 15) & ~(size_t)15);
+}
+
 template <int N, bool REAL>
 __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
                                                                                     const unsigned int *wsum) {
     using S = C2RShape<N>;
     constexpr int M = S::M, W = half_width_of<N>();
-    extern __shared__ float2 smem[];
+    constexpr unsigned ROW_BYTES = c2r_row_bytes<N>();
+    static_assert(ROW_BYTES <= S::BUF * sizeof(float2), "staged row larger than its buffer");
+    static_assert(ROW_BYTES <= W * sizeof(float2) && (W * sizeof(float2)) % 16 == 0, "rows copied whole");
+    static_assert((S::BUF * sizeof(float2)) % 16 == 0, "row buffers 16-byte aligned");
+    extern __shared__ __align__(16) float2 smem[];
+    float2 *zeros = smem + S::ROWS * S::BUF;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(zeros + ROW_BYTES / sizeof(float2));
     const float2 *tw = twiddles<M, S::R>();
     const float2 *wz = reinterpret_cast<const float2 *>(g_z_twiddles<N>.v);
     const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
-    const size_t row = (size_t)blockIdx.x * S::ROWS + slot;
+    const size_t row0 = (size_t)blockIdx.x * S::ROWS;
+    const size_t row = row0 + slot;
     const size_t img = row / N;
-    float2 *src = grids + row * W;
     float2 *buf = smem + slot * S::BUF;
-    constexpr int PER = M / S::P;  // row values per thread, plus X[M] on thread 0
-    float2 r[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) r[q] = src[t + q * S::P];
-    const float2 last = t == 0 ? src[M] : make_float2(0.f, 0.f);
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        buf[t + q * S::P] = r[q];
-        src[t + q * S::P] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
     }
-    if (t == 0) {
-        buf[M] = last;
-        src[M] = make_float2(0.f, 0.f);
+    for (int i = threadIdx.x; i < (int)(ROW_BYTES / 16); i += blockDim.x)
+        reinterpret_cast<float4 *>(zeros)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(bar, S::ROWS * ROW_BYTES);
+        for (int r = 0; r < S::ROWS; ++r) bulk_load(smem + r * S::BUF, grids + (row0 + r) * W, ROW_BYTES, bar);
     }
-    fft_sync<S::WARP>();
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
+        mbar_wait_bounded(bar, 0);  // let copies still in flight land before the block exits
+        return;
+    }
+    if (threadIdx.x == 0) {  // the rows have been read: clear them for the next wave
+        for (int r = 0; r < S::ROWS; ++r) bulk_store(grids + (row0 + r) * W, zeros, ROW_BYTES);
+        bulk_commit();
+    }
     const float scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
     float2 *dst = images + row * N;
     fft_transform<M, S::R, S::WARP, false>(
@@ -503,6 +522,7 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
             else
                 __stcs(reinterpret_cast<float4 *>(dst + x), make_float4(z.x * scale, 0.f, z.y * scale, 0.f));
         });
+    if (threadIdx.x == 0) bulk_wait_all();
 }
 
 template <class K>
@@ -556,7 +576,7 @@ int cols_half_n(float2 *grids, int n_images, cudaStream_t s) {
 template <int N>
 int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, bool real, cudaStream_t s) {
     using S = C2RShape<N>;
-    const size_t smem = sizeof(float2) * ((size_t)S::ROWS * S::BUF);
+    const size_t smem = sizeof(float2) * ((size_t)S::ROWS * S::BUF) + c2r_row_bytes<N>() + sizeof(uint64_t);
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
     auto k = real ? c2r_rows_kernel<N, true> : c2r_rows_kernel<N, false>;
     int st = prepare(k, smem);
@@ -750,6 +770,32 @@ int launch_image_average(const float2 *images, int64_t image_size, int n_images,
     const int64_t blocks = (image_size + 255) / 256;
     average_kernel<<<(unsigned)blocks, 256, 0, s>>>(images, image_size, n_images, out);
     return check_launch("image_averaging");
+}
+
+// ---- device fault word -------------------------------------------------------------------
+namespace {
+// One thread waits on an mbarrier that nothing arrives on: the bounded wait gives up, records
+// the fault and returns (the self-test of the wait limit).
+__global__ void wait_timeout_kernel() {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        mbar_wait_bounded(&bar, 0);
+    }
+}
+}  // namespace
+
+int read_device_fault(unsigned int *bits, bool clear) {
+    int st = check_cuda(cudaMemcpyFromSymbol(bits, g_device_fault, sizeof(unsigned int)), "read device fault");
+    if (st || !clear || !*bits) return st;
+    const unsigned int zero = 0;
+    return check_cuda(cudaMemcpyToSymbol(g_device_fault, &zero, sizeof(unsigned int)), "clear device fault");
+}
+
+int launch_wait_timeout_selftest(cudaStream_t s) {
+    wait_timeout_kernel<<<1, 32, 0, s>>>();
+    return check_launch("wait timeout self-test");
 }
 
 }  // namespace bgi

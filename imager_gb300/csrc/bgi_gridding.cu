@@ -24,7 +24,7 @@ constexpr int kCPT = 4;  // images per thread
 template <int POL, bool COUNTERS, bool HALF, int FMT>
 __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
     __shared__ ChannelConst s_cc[kCPT];
-    __shared__ unsigned int s_count[kCPT];
+    __shared__ unsigned int s_count[kCPT][kThreads / 32];  // per-warp weight counts
     const int img_first = p.img_begin + blockIdx.y * kCPT;
     const int img_end = p.img_begin + p.img_count;
     const int n_here = min(kCPT, img_end - img_first);
@@ -65,13 +65,16 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
             }
         }
     }
-    if (threadIdx.x < n_here) {
-        int ch = ch_first + threadIdx.x;
-        while (ch >= p.n_channels) ch -= p.n_channels;
-        s_cc[threadIdx.x] = make_channel_const(p.freqs[ch], p.du, p.dv);
-        s_count[threadIdx.x] = 0;
+    // channel constants: from the caller's table when there is one (no FP64 work and no block
+    // barrier here), else computed by kCPT threads while the loads are in flight
+    if (!p.chan_consts) {  // uniform across the block
+        if (threadIdx.x < n_here) {
+            int ch = ch_first + threadIdx.x;
+            while (ch >= p.n_channels) ch -= p.n_channels;
+            s_cc[threadIdx.x] = make_channel_const(p.freqs[ch], p.du, p.dv);
+        }
+        __syncthreads();
     }
-    __syncthreads();
 
     const int n = p.n_pixels;
     const long long npix = (long long)n * n;
@@ -84,7 +87,9 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
         const int local = img - p.img_base;
         unsigned int counted = 0;
         if (in_range && flag <= 0) {
-            const ChannelConst &cc = s_cc[j];
+            int chj = ch_first + j;
+            if (chj >= p.n_channels) chj %= p.n_channels;
+            const ChannelConst cc = p.chan_consts ? p.chan_consts[chj] : s_cc[j];
             float2 z = combine_pols<POL>(pa[j], pb[j]);
             if (corr) {
                 float d_hi, d_lo;
@@ -128,14 +133,18 @@ __global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
         }
         if (p.wsum) {
             const unsigned int warp_total = __reduce_add_sync(0xffffffffu, counted);
-            if ((threadIdx.x & 31) == 0 && warp_total) atomicAdd(&s_count[j], warp_total);
+            if ((threadIdx.x & 31) == 0) s_count[j][threadIdx.x >> 5] = warp_total;
         }
     }
     // one global atomic per block and image
     if (p.wsum) {
         __syncthreads();
-        if (threadIdx.x < n_here && s_count[threadIdx.x])
-            atomicAdd(p.wsum + (size_t)(img_first + threadIdx.x - p.img_base) * kWsumStride, s_count[threadIdx.x]);
+        if (threadIdx.x < n_here) {
+            unsigned int total = 0;
+#pragma unroll
+            for (int w = 0; w < kThreads / 32; ++w) total += s_count[threadIdx.x][w];
+            if (total) atomicAdd(p.wsum + (size_t)(img_first + threadIdx.x - p.img_base) * kWsumStride, total);
+        }
     }
 }
 
@@ -157,7 +166,19 @@ void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
     }
 }
 
+__global__ void channel_consts_kernel(const double *freqs, int n_channels, double du, double dv, ChannelConst *table) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n_channels) table[c] = make_channel_const(freqs[c], du, dv);
+}
+
 }  // namespace
+
+int launch_channel_consts(const double *freqs, int n_channels, double du, double dv, ChannelConst *table,
+                          cudaStream_t s) {
+    if (n_channels <= 0) return BGI_OK;
+    channel_consts_kernel<<<(n_channels + 127) / 128, 128, 0, s>>>(freqs, n_channels, du, dv, table);
+    return check_launch("channel constants");
+}
 
 int launch_gridding(const GridParams &p, cudaStream_t s) {
     if (p.img_count <= 0 || p.n_baselines <= 0) return BGI_OK;

@@ -29,6 +29,8 @@ struct GridParams {
     const float2 *dl;        // [B] L[a2]-L[a1] (cable delay) as a float pair (hi, lo), or null
     const int *flags;        // [B]
     const double *freqs;     // [C] Hz
+    const ChannelConst *chan_consts;  // [C] make_channel_const(freqs[c], du, dv), or null (then
+                                      // the gridding kernels compute them)
     float2 *grids;           // images [img - img_base][N*N]
     float *counters;         // optional counter grids
     unsigned int *wsum;      // optional per-image weight counts at wsum[(img - img_base) * kWsumStride]
@@ -44,6 +46,9 @@ struct GridParams {
                                // cells instead of reading them first)
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
+// table[c] = make_channel_const(freqs[c], du, dv) for c < n_channels
+int launch_channel_consts(const double *freqs, int n_channels, double du, double dv, ChannelConst *table,
+                          cudaStream_t s);
 
 // ---- block-scaled 16-bit visibilities (bgi_compress.cu) -------------------------------------
 long long vis_blocks(long long n_baselines);
@@ -89,6 +94,11 @@ int launch_vector_sum(const float *data, int64_t image_size, int n_images, float
                       cudaStream_t s);
 int launch_image_average(const float2 *images, int64_t image_size, int n_images, float2 *out,
                          cudaStream_t s);
+
+// Device fault word of the current device (bit 0: a bounded wait on a bulk copy gave up);
+// cleared after reading when `clear` is set.  Synchronous.
+int read_device_fault(unsigned int *bits, bool clear);
+int launch_wait_timeout_selftest(cudaStream_t s);
 
 // number of SMs of the current device (cached)
 int sm_count();

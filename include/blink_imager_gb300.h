@@ -251,6 +251,15 @@ BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n
                               double delta_v, int n_pixels, double min_uv, int pol, float *images,
                               void *stream);
 
+/* Device fault word of a device: bit 0 set when a kernel's bounded wait on its own bulk
+ * asynchronous copies gave up (after about 50 ms) and the kernel skipped its work instead of
+ * hanging.  clear != 0 resets it after reading.  Synchronous.  bgi_image_host checks it and
+ * returns BGI_ERR_CUDA when it is set.  bgi_selftest_wait_timeout launches one kernel that
+ * waits on a barrier nothing arrives on, so that the limit runs out and sets the bit (a test of
+ * that path; it takes about 50 ms of one SM).  No reference counterpart. */
+BGI_API int bgi_device_fault(int device, unsigned int *fault_bits, int clear);
+BGI_API int bgi_selftest_wait_timeout(int device, void *stream);
+
 /* Deterministic mode (default off): bgi_image and bgi_image_host grid with the ordered
  * per-cell sums of bgi_gridding_sorted_gpu on the full plane, so every image is the same bits
  * on every run and whatever else shares the call.  No reference counterpart. */
