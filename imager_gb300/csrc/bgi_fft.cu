@@ -170,7 +170,15 @@ struct NoClear {
 // gclear(i), when given, runs for every input element after all of this thread's first-pass
 // loads have been issued (clearing a source behind the loads without serialising them: a store
 // between two loads through possibly aliasing pointers would make each load wait for the last).
-template <int N, int R, bool WARP, bool ALIASED, class GLoad, class GStore, class GClear = NoClear>
+// TWS: tw points to a copy of the tables in shared memory (plain loads) instead of global
+// memory (read-only cached loads).
+template <bool TWS>
+__device__ __forceinline__ float2 tw_load(const float2 *tw, int i) {
+    if constexpr (TWS) return tw[i];
+    else return __ldg(tw + i);
+}
+
+template <int N, int R, bool WARP, bool ALIASED, bool TWS = false, class GLoad, class GStore, class GClear = NoClear>
 __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *tw, GLoad gload,
                                               GStore gstore, GClear gclear = GClear()) {
     using C = FftCfg<N, R>;
@@ -190,7 +198,7 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
         const int k = t & (Ns - 1);
         if (p > 0) {
 #pragma unroll
-            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], __ldg(tw + toff + (m - 1) * Ns + k));
+            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw_load<TWS>(tw, toff + (m - 1) * Ns + k));
             toff += (R - 1) * Ns;
         }
         dft<R>(a);
@@ -224,7 +232,7 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
             float2 b[R2];
 #pragma unroll
             for (int m = 0; m < R2; ++m)
-                b[m] = m ? cmul(a[q * R2 + m], __ldg(tw + TT::OFF_REM + (m - 1) * (N / R2) + j)) : a[q * R2];
+                b[m] = m ? cmul(a[q * R2 + m], tw_load<TWS>(tw, TT::OFF_REM + (m - 1) * (N / R2) + j)) : a[q * R2];
             dft<R2>(b);
 #pragma unroll
             for (int m = 0; m < R2; ++m) gstore(j + m * (N / R2), b[m]);
@@ -277,7 +285,7 @@ constexpr TwEntry twiddle_exact(int idx, int n) {
 }
 
 template <int N, int R>
-struct TwData {
+struct alignas(16) TwData {  // 16-byte aligned: bulk copies stage it in shared memory
     TwEntry v[TwTables<N, R>::SIZE];
 };
 
@@ -401,7 +409,7 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
 
 // exp(+2*pi*i*k/N) for k < N/2 (compile-time, as the pass tables).
 template <int N>
-struct ZTwData {
+struct alignas(16) ZTwData {
     TwEntry v[N / 2];
 };
 template <int N>
@@ -462,6 +470,20 @@ template <int N>
 constexpr unsigned c2r_row_bytes() {
     return (unsigned)(((N / 2 + 1) * sizeof(float2) + 15) & ~(size_t)15);
 }
+// bytes of the pass twiddle table and of the z twiddles staged next to the rows
+template <int N>
+constexpr unsigned c2r_tw_bytes() {
+    return (unsigned)(TwTables<N / 2, C2RShape<N>::R>::SIZE * sizeof(float2));
+}
+template <int N>
+constexpr unsigned c2r_wz_bytes() {
+    return (unsigned)((N / 2) * sizeof(float2));
+}
+template <int N>
+constexpr size_t c2r_smem_bytes() {
+    return sizeof(float2) * (size_t)C2RShape<N>::ROWS * C2RShape<N>::BUF + c2r_row_bytes<N>() + c2r_tw_bytes<N>() +
+           c2r_wz_bytes<N>() + sizeof(uint64_t);
+}
 
 template <int N, bool REAL>
 __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
@@ -472,11 +494,13 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     static_assert(ROW_BYTES <= S::BUF * sizeof(float2), "staged row larger than its buffer");
     static_assert(ROW_BYTES <= W * sizeof(float2) && (W * sizeof(float2)) % 16 == 0, "rows copied whole");
     static_assert((S::BUF * sizeof(float2)) % 16 == 0, "row buffers 16-byte aligned");
+    constexpr unsigned TW_BYTES = c2r_tw_bytes<N>(), WZ_BYTES = c2r_wz_bytes<N>();
+    static_assert(TW_BYTES % 16 == 0 && WZ_BYTES % 16 == 0, "twiddle tables copied whole");
     extern __shared__ __align__(16) float2 smem[];
     float2 *zeros = smem + S::ROWS * S::BUF;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(zeros + ROW_BYTES / sizeof(float2));
-    const float2 *tw = twiddles<M, S::R>();
-    const float2 *wz = reinterpret_cast<const float2 *>(g_z_twiddles<N>.v);
+    float2 *tw = zeros + ROW_BYTES / sizeof(float2);  // pass twiddles, then z twiddles
+    float2 *wz = tw + TW_BYTES / sizeof(float2);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(wz + WZ_BYTES / sizeof(float2));
     const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
     const size_t row0 = (size_t)blockIdx.x * S::ROWS;
     const size_t row = row0 + slot;
@@ -491,7 +515,9 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(bar, S::ROWS * ROW_BYTES);
+        mbar_arrive_expect_tx(bar, S::ROWS * ROW_BYTES + TW_BYTES + WZ_BYTES);
+        bulk_load(tw, twiddles<M, S::R>(), TW_BYTES, bar);
+        bulk_load(wz, g_z_twiddles<N>.v, WZ_BYTES, bar);
         for (int r = 0; r < S::ROWS; ++r) bulk_load(smem + r * S::BUF, grids + (row0 + r) * W, ROW_BYTES, bar);
     }
     if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
@@ -504,10 +530,10 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     }
     const float scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
     float2 *dst = images + row * N;
-    fft_transform<M, S::R, S::WARP, false>(
+    fft_transform<M, S::R, S::WARP, false, true>(
         t, buf, tw,
         [&](int k) {
-            const float2 a = buf[k], b = buf[M - k], w = __ldg(wz + k);
+            const float2 a = buf[k], b = buf[M - k], w = wz[k];
             // a * (1 + i w) + conj(b) * (1 - i w)
             const float pr = 1.f - w.y, pi = w.x, qr = 1.f + w.y, qi = -w.x;
             const float br = b.x, bi = -b.y;
@@ -576,7 +602,7 @@ int cols_half_n(float2 *grids, int n_images, cudaStream_t s) {
 template <int N>
 int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, bool real, cudaStream_t s) {
     using S = C2RShape<N>;
-    const size_t smem = sizeof(float2) * ((size_t)S::ROWS * S::BUF) + c2r_row_bytes<N>() + sizeof(uint64_t);
+    const size_t smem = c2r_smem_bytes<N>();
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
     auto k = real ? c2r_rows_kernel<N, true> : c2r_rows_kernel<N, false>;
     int st = prepare(k, smem);
