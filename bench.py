@@ -315,6 +315,12 @@ def run_ours(args, rank, world, local_rank):
         return lambda: h.image_compressed(d, sc, f, flags=flags, out=out)
 
     step = step_for(im, fmt)
+    tuned = None
+    if args.autotune:  # wave size and lane count timed on this block (bgi_autotune), untimed here
+        if fmt == "c64":
+            tuned = im.autotune(vis, None, "c64", flags=flags, out=out)
+        else:
+            tuned = im.autotune(stored[fmt][0], stored[fmt][1], fmt, flags=flags, out=out)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -489,7 +495,8 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic (seeded; shapes and distributions of the workload)",
         "config": {"workload": WORKLOAD if T == 10 else WORKLOAD.replace("10 intervals", f"{T} intervals"),
                    "images_per_step": n_images, "n_pixels": N, "baselines": B,
-                   "wave_images": args.wave or "auto",
+                   "schedule": {"images_per_wave": im.schedule[0] or "auto", "lanes": im.schedule[1],
+                                "chosen_by": "bgi_autotune on this block" if tuned else "default"},
                    "l2": "flushed before every timed step (512 MB written outside the step's events)",
                    "bytes_per_step": {"stored_visibilities_read": n_images * vis_bytes, "images_written": d2h},
                    "parallelism": "one block per GPU, no collective" if world > 1 else "single GPU"},
@@ -526,6 +533,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--storage", choices=["s16", "bf16", "fp16", "c64"], default="s16",
                     help="visibility storage of the timed step (s16: 16-bit block floating point)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default schedule (auto wave, two lanes) instead of bgi_autotune's")
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip timing the deterministic and full-plane variants")
     ap.add_argument("--intervals", type=int, default=10,

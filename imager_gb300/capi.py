@@ -64,6 +64,9 @@ _SIGNATURES = {
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
     "bgi_set_deterministic": (_i, [_vp, _i]),
+    "bgi_set_schedule": (_i, [_vp, _i, _i]),
+    "bgi_get_schedule": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
+    "bgi_autotune": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp, C.POINTER(C.c_double)]),
     "bgi_device_fault": (_i, [_i, C.POINTER(C.c_uint), _i]),
     "bgi_selftest_wait_timeout": (_i, [_i, _vp]),
     "bgi_set_stage_timing": (_i, [_vp, _i]),

@@ -123,14 +123,16 @@ struct bgi_imager {
     bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
     double *d_freqs = nullptr;
-    // Two lanes (streams) image alternate waves, each with its own grid scratch, so one wave's
+    // Lanes (streams; two unless bgi_set_schedule or bgi_autotune chose otherwise) image
+    // alternate waves, each with its own grid scratch, so one wave's
     // FFT passes overlap the next wave's gridding; the scratch of a lane is reused wave after
     // wave and sized to stay in L2.
-    static constexpr int kLanes = 2;
+    static constexpr int kLanes = 4;  // at most; `lanes` are in use (bgi_set_schedule, bgi_autotune)
+    int lanes = 2;
     DevBuf<float2> grid[kLanes];  // wave scratch: images x N*N, zero between waves
-    bool grid_dirty[kLanes] = {false, false};
-    cudaStream_t lane[kLanes] = {nullptr, nullptr};
-    cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {nullptr, nullptr};
+    bool grid_dirty[kLanes] = {false, false, false, false};
+    cudaStream_t lane[kLanes] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {nullptr, nullptr, nullptr, nullptr};
     // Deterministic mode: gridding by sort and ordered per-cell sums (full plane), with a
     // workspace per lane for one wave.
     bool deterministic = false;
@@ -528,7 +530,7 @@ int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *w
     }
     wave = std::min(wave, n_images);
     const int n_waves = (n_images + wave - 1) / wave;
-    const int n_lanes = std::min(n_waves, (int)bgi_imager::kLanes);
+    const int n_lanes = std::min(n_waves, im->lanes);
     for (int l = 0; l < n_lanes; ++l) {
         bool fresh = false;
         BGI_TRY(im->grid[l].ensure((size_t)wave * npix, "grid scratch", &fresh));
@@ -660,7 +662,7 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     GridParams p = block_params(im, vis, n_intervals, flags, images, format, scales);
     BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
     p.chan_consts = im->d_cc.ptr;
-    cudaStream_t streams[bgi_imager::kLanes] = {s, s};
+    cudaStream_t streams[bgi_imager::kLanes] = {s, s, s, s};
     if (n_lanes > 1) {
         BGI_TRY(im->ensure_lanes());
         BGI_TRY(check_cuda(cudaEventRecord(im->ev_fork, s), "fork record"));
@@ -695,6 +697,72 @@ int bgi_image_compressed(bgi_imager *im, int format, const void *data, const flo
     if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
         return set_error(BGI_ERR_INVALID, "image_compressed: bad format %d", format);
     return image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+}
+
+int bgi_set_schedule(bgi_imager *im, int images_per_wave, int lanes) {
+    if (!im || images_per_wave < 0 || lanes < 1 || lanes > bgi_imager::kLanes)
+        return set_error(BGI_ERR_INVALID, "set_schedule: wave >= 0 (0 = auto) and 1 <= lanes <= %d", bgi_imager::kLanes);
+    im->cfg.max_images_per_wave = images_per_wave;
+    im->lanes = lanes;
+    return BGI_OK;
+}
+
+int bgi_get_schedule(const bgi_imager *im, int *images_per_wave, int *lanes) {
+    if (!im || !images_per_wave || !lanes) return set_error(BGI_ERR_INVALID, "get_schedule: bad arguments");
+    *images_per_wave = im->cfg.max_images_per_wave;
+    *lanes = im->lanes;
+    return BGI_OK;
+}
+
+int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals, unsigned flags,
+                 float *images, void *stream, double *best_ms) {
+    BGI_TRY(image_checks(im, n_intervals, flags));
+    if (format < BGI_VIS_C64 || format > BGI_VIS_FP16) return set_error(BGI_ERR_INVALID, "autotune: bad format %d", format);
+    BGI_TRY(im->activate());
+    cudaStream_t s = as_stream(stream);
+    const int n_images = n_intervals * im->n_channels;
+    const bool timing = im->timing;
+    im->timing = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    BGI_TRY(check_cuda(cudaEventCreate(&e0), "autotune event"));
+    int st = check_cuda(cudaEventCreate(&e1), "autotune event");
+    static const int kWaves[] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64};
+    int best_wave = im->cfg.max_images_per_wave, best_lanes = im->lanes;
+    float best = 3.4e38f;
+    for (int wi = 0; !st && wi < (int)(sizeof(kWaves) / sizeof(kWaves[0])); ++wi) {
+        if (kWaves[wi] > n_images) break;
+        for (int lanes = 1; !st && lanes <= bgi_imager::kLanes; ++lanes) {
+            im->cfg.max_images_per_wave = kWaves[wi];
+            im->lanes = lanes;
+            st = image_impl(im, format, data, scales, n_intervals, flags, images, stream);  // sizes the scratch
+            if (!st) st = check_cuda(cudaEventRecord(e0, s), "autotune record");
+            for (int rep = 0; !st && rep < 3; ++rep) st = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+            if (!st) st = check_cuda(cudaEventRecord(e1, s), "autotune record");
+            if (!st) st = check_cuda(cudaEventSynchronize(e1), "autotune sync");
+            float ms = 0.f;
+            if (!st) st = check_cuda(cudaEventElapsedTime(&ms, e0, e1), "autotune elapsed");
+            if (!st && ms / 3.f < best) {
+                best = ms / 3.f;
+                best_wave = kWaves[wi];
+                best_lanes = lanes;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    im->timing = timing;
+    im->cfg.max_images_per_wave = best_wave;
+    im->lanes = best_lanes;
+    if (st) return st;
+    // drop the candidates' scratch; the chosen schedule sizes its own on the next call
+    BGI_TRY(check_cuda(cudaStreamSynchronize(s), "autotune sync"));
+    for (int l = 0; l < bgi_imager::kLanes; ++l) {
+        im->grid[l].release();
+        im->sorted_ws[l].release();
+        im->grid_dirty[l] = false;
+    }
+    if (best_ms) *best_ms = best;
+    return BGI_OK;
 }
 
 int bgi_compressed_size(int n_ant, int n_channels, int n_intervals, size_t *data_bytes, size_t *scale_bytes) {

@@ -254,6 +254,29 @@ class Imager:
              _ptr(out), _stream(stream))
         return out
 
+    @property
+    def schedule(self):
+        """(images per wave, lanes) of the bgi_image* calls; 0 images per wave = auto."""
+        w, l = C.c_int(0), C.c_int(0)
+        call("bgi_get_schedule", self._h, C.byref(w), C.byref(l))
+        return w.value, l.value
+
+    def set_schedule(self, images_per_wave: int = 0, lanes: int = 2):
+        call("bgi_set_schedule", self._h, int(images_per_wave), int(lanes))
+
+    def autotune(self, data, scales=None, fmt="c64", flags: int = APPLY_GEOMETRIC | APPLY_CABLE, out=None,
+                 stream=None):
+        """Times wave sizes and lane counts on this block (device buffers) and keeps the fastest;
+        returns (images per wave, lanes, ms per call)."""
+        T, Cn = int(data.shape[0]), int(data.shape[1])
+        n = self.n_pixels
+        if out is None:
+            out = torch.empty((T, Cn, n, n), dtype=_out_dtype(flags), device=data.device)
+        best = C.c_double(0.0)
+        call("bgi_autotune", self._h, VIS_FORMAT[fmt], _ptr(data), _ptr(scales), T, int(flags), _ptr(out),
+             _stream(stream), C.byref(best))
+        return (*self.schedule, best.value)
+
     def set_deterministic(self, enable: bool = True):
         """Grid by sort and ordered per-cell sums (full plane): the same image bits on every run."""
         call("bgi_set_deterministic", self._h, int(bool(enable)))

@@ -260,6 +260,20 @@ BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n
 BGI_API int bgi_device_fault(int device, unsigned int *fault_bits, int clear);
 BGI_API int bgi_selftest_wait_timeout(int device, void *stream);
 
+/* Launch schedule of the bgi_image* calls: images per wave (0 = auto: about 26 MiB of grid
+ * per lane, 24 half-plane images at 512^2) and lanes (1..4 streams that image alternate waves,
+ * each with its own grid scratch; 2 by default).  bgi_autotune times every wave size in
+ * {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to the block's image count) with 1-4
+ * lanes on the caller's own block (4 calls each: one to size the scratch, three timed with CUDA
+ * events on the stream), keeps the fastest on the handle, frees the candidates' scratch and
+ * writes the best milliseconds per call to *best_ms (may be NULL).  Synchronous; `images`
+ * receives the block's images.  No reference counterpart. */
+BGI_API int bgi_set_schedule(bgi_imager *im, int images_per_wave, int lanes);
+BGI_API int bgi_get_schedule(const bgi_imager *im, int *images_per_wave, int *lanes);
+BGI_API int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scales,
+                         int n_intervals, unsigned flags, float *images, void *stream,
+                         double *best_ms);
+
 /* Deterministic mode (default off): bgi_image and bgi_image_host grid with the ordered
  * per-cell sums of bgi_gridding_sorted_gpu on the full plane, so every image is the same bits
  * on every run and whatever else shares the call.  No reference counterpart. */

@@ -438,3 +438,25 @@ def test_image_real_output(im, full_plane, pol):
     fast = h.image(dev(vis), flags=fl | im.OUTPUT_REAL).cpu().numpy()  # atomic gridder
     assert rel_l2(fast, real) < 1e-6
     h.close()
+
+
+def test_schedule_and_autotune(im):
+    """Any schedule (wave size, lanes) gives the same images; the autotuner keeps a valid one."""
+    n = 128
+    obs = synth.small(seed=61, n_ant=40, n_intervals=3, n_channels=4, n_pixels=n)
+    vis = dev(obs.vis_f32())
+    h = _imager_for(im, obs, n, "XX")
+    h.set_deterministic(True)
+    ref = h.image(vis).cpu().numpy()
+    for wave, lanes in ((1, 1), (5, 3), (12, 4), (0, 2)):
+        h.set_schedule(wave, lanes)
+        assert h.schedule == (wave, lanes)
+        out = h.image(vis).cpu().numpy()
+        assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), (wave, lanes)
+    with pytest.raises(capi.BgiError):
+        h.set_schedule(8, 5)
+    h.set_deterministic(False)
+    wave, lanes, ms = h.autotune(vis)
+    assert wave in (0, 4, 8, 12) and 1 <= lanes <= 4 and ms > 0
+    assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6
+    h.close()
