@@ -33,6 +33,19 @@ class Config(C.Structure):
                 ("full_plane", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("max_slots", C.c_int), ("hbm_budget_bytes", C.c_size_t),
+                ("reserve_bytes", C.c_size_t), ("deterministic", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("images", C.c_uint64), ("admission_waits", C.c_uint64), ("queued", C.c_uint64),
+                ("device_bytes_in_use", C.c_size_t), ("device_budget_bytes", C.c_size_t),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double),
+                ("wall_s", C.c_double), ("images_per_s", C.c_double)]
+
+
 _vp, _i, _i64, _d, _f, _u = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_float, C.c_uint
 _SIGNATURES = {
     "bgi_last_error": (C.c_char_p, []),
@@ -64,6 +77,14 @@ _SIGNATURES = {
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
     "bgi_set_deterministic": (_i, [_vp, _i]),
+    "bgi_server_create": (_i, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "bgi_server_destroy": (_i, [_vp]),
+    "bgi_server_add_array": (_i, [_vp, C.POINTER(Config), _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, C.POINTER(_i)]),
+    "bgi_server_submit": (_i, [_vp, _i, _i, _vp, _vp, _i, C.c_uint, _vp, C.POINTER(C.c_uint64)]),
+    "bgi_server_wait": (_i, [_vp, C.c_uint64, _i, C.POINTER(_i)]),
+    "bgi_server_poll": (_i, [_vp, C.c_uint64, C.POINTER(_i), C.POINTER(_i)]),
+    "bgi_server_get_stats": (_i, [_vp, C.POINTER(ServerStats)]),
+    "bgi_server_reset_stats": (_i, [_vp]),
     "bgi_set_schedule": (_i, [_vp, _i, _i]),
     "bgi_get_schedule": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
     "bgi_autotune": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp, C.POINTER(C.c_double)]),

@@ -288,6 +288,61 @@ BGI_API int bgi_set_deterministic(bgi_imager *im, int enable);
 BGI_API int bgi_set_stage_timing(bgi_imager *im, int enable);
 BGI_API int bgi_get_stage_times(bgi_imager *im, double ms[3], int64_t launches[3]);
 
+/* ------------------------------------------------------------------------------------------
+ * 3. Serving runtime (no reference counterpart)
+ *
+ * A request loop over imager handles.  Arrays are registered once: each slot makes its own
+ * handle from the registered state, so UVW, flags, cable lengths and frequencies stay resident on
+ * the device.  bgi_server_submit queues a block of visibilities in host memory (pinned memory
+ * gives asynchronous copies) and returns at once with a ticket.  A scheduler thread admits queued
+ * requests in arrival order as soon as a slot (a CUDA stream) is free and the request's device
+ * buffers (visibilities -- for the 16-bit formats only the pol planes the array's pol needs --
+ * and images) fit both the byte budget and the device's free memory less reserve_bytes; it then
+ * uploads, images and downloads on the slot's stream, so requests that arrive while others run
+ * overlap with them on the GPU.  A request that cannot fit even on an idle device fails with
+ * BGI_ERR_ALLOC.  Latency is measured from submission to the completion of the download.
+ * With deterministic = 1 every request grids with the ordered gridder, so a request's images
+ * are the same bits whatever else runs beside it; otherwise they agree to float summation
+ * order (~1e-7 relative).  All calls are thread-safe.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct bgi_server bgi_server;
+
+typedef struct bgi_server_config {
+    int device;               /* CUDA device of the server and of every array's config */
+    int max_slots;            /* requests on the GPU at once (1..64) */
+    size_t hbm_budget_bytes;  /* request buffers at once; 0 = free memory at creation less the reserve */
+    size_t reserve_bytes;     /* device memory left free at admission (handles' scratch, other users) */
+    int deterministic;        /* 1: ordered gridding (results independent of the mix) */
+} bgi_server_config;
+
+typedef struct bgi_server_stats {
+    uint64_t submitted, completed, failed, images, admission_waits, queued;
+    size_t device_bytes_in_use, device_budget_bytes;
+    double p50_ms, p99_ms, max_ms, mean_ms; /* submit-to-done latency of completed requests */
+    double wall_s, images_per_s;            /* first submission to last completion */
+} bgi_server_stats;
+
+BGI_API int bgi_server_create(const bgi_server_config *cfg, bgi_server **out);
+/* Finishes every queued request, then frees the server. */
+BGI_API int bgi_server_destroy(bgi_server *sv);
+/* Registers an array (arguments as bgi_create + bgi_set_array + bgi_set_frequencies, copied). */
+BGI_API int bgi_server_add_array(bgi_server *sv, const bgi_config *cfg, int n_ant, int n_uvw_sets,
+                                 const float *u, const float *v, const float *w,
+                                 const int *baseline_flags, const double *cable_lengths,
+                                 int n_channels, const double *freqs_hz, int *array_id);
+/* Queues a block: vis_host in `format` (scales_host for the 16-bit formats) for n_intervals
+ * intervals of the array's channels; images_host receives T*C images (flags as bgi_image,
+ * BGI_OUTPUT_REAL included).  Host buffers must stay valid until the request is collected. */
+BGI_API int bgi_server_submit(bgi_server *sv, int array_id, int format, const void *vis_host,
+                              const float *scales_host, int n_intervals, unsigned flags,
+                              float *images_host, uint64_t *ticket);
+/* Wait for (timeout_ms < 0: without limit) or poll a request; a finished request reports its
+ * status once (BGI_OK or the failure, message in bgi_last_error) and its ticket is released. */
+BGI_API int bgi_server_wait(bgi_server *sv, uint64_t ticket, int timeout_ms, int *status);
+BGI_API int bgi_server_poll(bgi_server *sv, uint64_t ticket, int *done, int *status);
+BGI_API int bgi_server_get_stats(bgi_server *sv, bgi_server_stats *out);
+BGI_API int bgi_server_reset_stats(bgi_server *sv);
+
 #ifdef __cplusplus
 }
 #endif
