@@ -279,6 +279,96 @@ def plain_dropin_step(obs, vis, du, dv, out):
     return step, fresh
 
 
+def serving_measure(args):
+    """The serving workload through bgi_server: blocks of 32 channels x 1 interval from a mix of
+    128/256/512-antenna arrays (images 256/512/1024^2), stored as s16, complex images back to
+    pinned host buffers.  Phase 1: Poisson arrivals (mean args.serve_interarrival_ms) -> latency
+    p50/p99.  Phase 2: closed loop with args.serve_outstanding requests outstanding -> sustained
+    images/s.  Errors: channel 0 of one request per array against the FP64 oracle."""
+    import collections
+    import torch
+    from imager_gb300 import imager as IM
+    from imager_gb300 import server as SV
+    from imager_gb300 import synth
+    from oracle import oracle as O
+    arrays = synth.serving_arrays(device="cuda")
+    rng = np.random.default_rng(1239)
+    K = args.serve_outstanding
+    res = {"workload": "arrays of 128 (35 m disk, 256^2), 256 (35 m disk, 512^2) and 512 antennas (16 sub-stations "
+                       "over 3 km, 1024^2); blocks of 32 channels x 1 interval, s16 stored, pol XX, corrections "
+                       "fused, complex images to pinned host memory; array of each request drawn uniformly",
+           "slots": args.serve_slots}
+    with SV.Server(max_slots=args.serve_slots) as sv:
+        ids = [sv.add_array(o.n_pixels, o.u, o.v, o.w, o.flags, o.cable, o.freqs) for o in arrays]
+        stored = []
+        for o in arrays:
+            d, sc = IM.compress_visibilities(torch.from_numpy(o.vis_f32()).cuda(), "s16")
+            stored.append((d.cpu().pin_memory(), sc.cpu().pin_memory()))
+        bufs = [collections.deque(torch.empty((1, o.n_channels, o.n_pixels, o.n_pixels), dtype=torch.complex64,
+                                              pin_memory=True) for _ in range(K)) for o in arrays]
+        busy = collections.deque()  # (ticket, array index, buffer), in submission order
+
+        def submit(k):
+            while not bufs[k]:  # reuse a buffer only after its request is collected
+                t, kk, b = busy.popleft()
+                sv.wait(t)
+                bufs[kk].append(b)
+            b = bufs[k].popleft()
+            t = sv.submit(ids[k], data=stored[k][0], scales=stored[k][1], fmt="s16", out=b)
+            busy.append((t, k, b))
+
+        def drain():
+            while busy:
+                t, kk, b = busy.popleft()
+                sv.wait(t)
+                bufs[kk].append(b)
+
+        for k in range(len(arrays)):  # warm every slot's handle for every array
+            for _ in range(args.serve_slots):
+                submit(k)
+            drain()
+        # errors of one request per array, channel 0
+        errs = []
+        for k, o in enumerate(arrays):
+            submit(k)
+            t, kk, b = busy.pop()
+            out = sv.wait(t)[0, 0].numpy().astype(np.complex128)
+            bufs[kk].append(b)
+            corr = np.ascontiguousarray(o.vis_f32()[:, :1])
+            O.apply_geometric(corr, o.w, o.freqs[:1])
+            O.apply_cable(corr, o.cable, o.freqs[:1])
+            umax, vmax = O.uv_max(o.u, o.v, o.flags)
+            du, dv = O.delta_uv(2.0, umax, o.n_pixels), O.delta_uv(2.0, vmax, o.n_pixels)
+            g, cnt, _ = O.gridding(corr, o.u, o.v, o.flags, o.freqs[:1], du, dv, o.n_pixels)
+            ref = O.image_f64(g, cnt)[0, 0]
+            errs.append(float(np.linalg.norm(out - ref) / np.linalg.norm(ref)))
+        res["errors_vs_fp64_rel_l2"] = max(errs)
+        # phase 1: Poisson arrivals
+        sv.reset_stats()
+        t0 = time.perf_counter()
+        arrival = 0.0
+        for _ in range(args.serve_requests):
+            arrival += rng.exponential(args.serve_interarrival_ms / 1000.0)
+            while time.perf_counter() - t0 < arrival:
+                time.sleep(0.0002)
+            submit(int(rng.integers(len(arrays))))
+        drain()
+        st = sv.stats()
+        res["poisson"] = {"mean_interarrival_ms": args.serve_interarrival_ms, "requests": st["completed"],
+                          "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                          "images_per_s": st["images_per_s"], "failed": st["failed"]}
+        # phase 2: closed loop, K outstanding per array
+        sv.reset_stats()
+        for _ in range(args.serve_requests * 3):
+            submit(int(rng.integers(len(arrays))))
+        drain()
+        st = sv.stats()
+        res["saturated"] = {"outstanding_per_array": K, "requests": st["completed"], "p50_ms": st["p50_ms"],
+                            "p99_ms": st["p99_ms"], "images_per_s": st["images_per_s"],
+                            "admission_waits": st["admission_waits"], "failed": st["failed"]}
+    return res
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from imager_gb300 import capi, synth
@@ -440,6 +530,7 @@ def run_ours(args, rank, world, local_rank):
     if rank != 0:
         dist.destroy_process_group()
         return 0
+    serving = serving_measure(args) if (args.serving and world == 1) else None
 
     images_per_s = world * n_images * args.steps / (ms / 1000.0)
     hbm_peak, peak_kind = measured_peaks()
@@ -522,6 +613,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks.summary(t0, t3),
         "gpu_launches": sum(v[1] for v in stages.values()) * args.steps // stage_steps,
         "variants": variants,
+        "serving": serving,
         "parity_sample_rel_l2": errs["rel_l2"],
         "errors_vs_fp64": {**errs, "images": [f"interval {t % T}, channel {c}" for t, c in SAMPLES],
                            "oracle": "FP64 oracle of the original complex64 visibilities"},
@@ -544,6 +636,11 @@ def main():
                     help="visibility storage of the timed step (s16: 16-bit block floating point)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default schedule (auto wave, two lanes) instead of bgi_autotune's")
+    ap.add_argument("--no-serving", dest="serving", action="store_false", help="skip the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--serve-interarrival-ms", type=float, default=100.0)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-outstanding", type=int, default=3)
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip timing the deterministic and full-plane variants")
     ap.add_argument("--intervals", type=int, default=10,

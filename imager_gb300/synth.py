@@ -234,3 +234,16 @@ def small(seed=7, n_ant=24, n_intervals=2, n_channels=3, n_pixels=64, radius=35.
     return make_observation(seed, n_ant, enu, n_intervals, freqs, n_pixels, n_src=n_src,
                             per_interval_uvw=per_interval_uvw, flagged_ants=flagged_ants,
                             pol=pol, device=device)
+
+
+def serving_arrays(device="cpu", n_channels=32):
+    """The serving workload's arrays, one 1-interval block of `n_channels` channels each:
+    128 antennas in a 35 m disk imaged at 256x256, 256 antennas in a 35 m disk at 512x512 and
+    512 antennas in 16 clustered sub-stations over 3 km at 1024x1024 (seed 1239)."""
+    freqs = 150e6 + np.arange(n_channels) * 0.9375e6
+    out = []
+    for k, (n_ant, n_pix) in enumerate(((128, 256), (256, 512), (512, 1024))):
+        rng = np.random.Generator(np.random.PCG64(1239 + k))
+        enu = layout_substations(rng, n_ant, 16) if n_ant == 512 else layout_uniform_disk(rng, n_ant, 35.0)
+        out.append(make_observation(1239 + k, n_ant, enu, 1, freqs, n_pix, device=device))
+    return out
