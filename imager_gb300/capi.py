@@ -46,6 +46,11 @@ class ServerStats(C.Structure):
                 ("wall_s", C.c_double), ("images_per_s", C.c_double)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("imager", C.c_void_p), ("format", C.c_int), ("data", C.c_void_p), ("scales", C.c_void_p),
+                ("n_intervals", C.c_int), ("flags", C.c_uint), ("images", C.c_void_p)]
+
+
 _vp, _i, _i64, _d, _f, _u = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_float, C.c_uint
 _SIGNATURES = {
     "bgi_last_error": (C.c_char_p, []),
@@ -77,6 +82,9 @@ _SIGNATURES = {
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
     "bgi_set_deterministic": (_i, [_vp, _i]),
+    "bgi_batch_create": (_i, [C.POINTER(BatchItem), _i, _vp, C.POINTER(_vp)]),
+    "bgi_batch_launch": (_i, [_vp, _vp]),
+    "bgi_batch_destroy": (_i, [_vp]),
     "bgi_server_create": (_i, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "bgi_server_destroy": (_i, [_vp]),
     "bgi_server_add_array": (_i, [_vp, C.POINTER(Config), _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, C.POINTER(_i)]),

@@ -13,6 +13,7 @@
 #include <limits>
 #include <new>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "bgi_internal.h"
@@ -697,6 +698,124 @@ int bgi_image_compressed(bgi_imager *im, int format, const void *data, const flo
     if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
         return set_error(BGI_ERR_INVALID, "image_compressed: bad format %d", format);
     return image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+}
+
+}  // extern "C"
+
+struct bgi_batch {
+    int device = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int n_items = 0;
+};
+
+namespace {
+
+// Issues every item on stream s: items of one handle chain on one forked stream (they share its
+// scratch); different handles run on different streams.  `streams` and `events` hold the forks.
+int issue_batch(const bgi_batch_item *items, int n_items, cudaStream_t s, std::vector<cudaStream_t> &streams,
+                std::vector<cudaEvent_t> &joins, cudaEvent_t fork) {
+    std::vector<bgi_imager *> handles;
+    for (int i = 0; i < n_items; ++i)
+        if (std::find(handles.begin(), handles.end(), items[i].imager) == handles.end())
+            handles.push_back(items[i].imager);
+    BGI_TRY(check_cuda(cudaEventRecord(fork, s), "batch fork"));
+    for (size_t k = 0; k < handles.size(); ++k) {
+        BGI_TRY(check_cuda(cudaStreamWaitEvent(streams[k], fork, 0), "batch fork wait"));
+        for (int i = 0; i < n_items; ++i) {
+            if (items[i].imager != handles[k]) continue;
+            const bgi_batch_item &it = items[i];
+            BGI_TRY(image_impl(it.imager, it.format, it.data, it.scales, it.n_intervals, it.flags, it.images,
+                               streams[k]));
+        }
+        BGI_TRY(check_cuda(cudaEventRecord(joins[k], streams[k]), "batch join"));
+        BGI_TRY(check_cuda(cudaStreamWaitEvent(s, joins[k], 0), "batch join wait"));
+    }
+    return BGI_OK;
+}
+
+int distinct_handles(const bgi_batch_item *items, int n_items) {
+    std::vector<bgi_imager *> handles;
+    for (int i = 0; i < n_items; ++i)
+        if (std::find(handles.begin(), handles.end(), items[i].imager) == handles.end())
+            handles.push_back(items[i].imager);
+    return (int)handles.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi_batch **out) {
+    if (!items || n_items < 1 || !out) return set_error(BGI_ERR_INVALID, "batch_create: bad arguments");
+    *out = nullptr;
+    const int device = items[0].imager ? items[0].imager->cfg.device : -1;
+    for (int i = 0; i < n_items; ++i) {
+        if (!items[i].imager) return set_error(BGI_ERR_INVALID, "batch_create: item %d has no imager", i);
+        if (items[i].imager->cfg.device != device)
+            return set_error(BGI_ERR_INVALID, "batch_create: items on different devices");
+        if (items[i].imager->timing) return set_error(BGI_ERR_STATE, "batch_create: stage timing is on (item %d)", i);
+    }
+    BGI_TRY(items[0].imager->activate());
+    // the items run and are captured on a stream of our own (the legacy default stream cannot
+    // be captured), ordered after the caller's stream
+    cudaStream_t user = as_stream(stream), s = nullptr;
+    BGI_TRY(check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "batch stream"));
+    const int n_h = distinct_handles(items, n_items);
+    std::vector<cudaStream_t> streams((size_t)n_h, nullptr);
+    std::vector<cudaEvent_t> joins((size_t)n_h, nullptr);
+    cudaEvent_t fork = nullptr;
+    int st = check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "batch event");
+    if (!st) st = check_cuda(cudaEventRecord(fork, user), "batch order");
+    if (!st) st = check_cuda(cudaStreamWaitEvent(s, fork, 0), "batch order");
+    for (int k = 0; !st && k < n_h; ++k) {
+        st = check_cuda(cudaStreamCreateWithFlags(&streams[(size_t)k], cudaStreamNonBlocking), "batch stream");
+        if (!st) st = check_cuda(cudaEventCreateWithFlags(&joins[(size_t)k], cudaEventDisableTiming), "batch event");
+    }
+    // one run outside the capture sizes every scratch buffer and builds the channel tables, so
+    // that the captured calls allocate nothing
+    if (!st) st = issue_batch(items, n_items, s, streams, joins, fork);
+    if (!st) st = check_cuda(cudaStreamSynchronize(s), "batch warm-up");
+    if (!st) st = check_cuda(cudaGetLastError(), "batch warm-up");
+    auto b = std::make_unique<bgi_batch>();
+    b->device = device;
+    b->n_items = n_items;
+    if (!st) st = check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "batch capture");
+    if (!st) {
+        const int issued = issue_batch(items, n_items, s, streams, joins, fork);
+        const int ended = check_cuda(cudaStreamEndCapture(s, &b->graph), "batch end capture");
+        st = issued ? issued : ended;
+    }
+    if (!st) st = check_cuda(cudaGraphInstantiate(&b->exec, b->graph, 0), "batch instantiate");
+    for (int k = 0; k < n_h; ++k) {
+        if (streams[(size_t)k]) cudaStreamDestroy(streams[(size_t)k]);
+        if (joins[(size_t)k]) cudaEventDestroy(joins[(size_t)k]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    cudaStreamDestroy(s);
+    if (st) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        return st;
+    }
+    *out = b.release();
+    return BGI_OK;
+}
+
+int bgi_batch_launch(bgi_batch *b, void *stream) {
+    if (!b || !b->exec) return set_error(BGI_ERR_INVALID, "batch_launch: no batch");
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != b->device) BGI_TRY(check_cuda(cudaSetDevice(b->device), "cudaSetDevice"));
+    return check_cuda(cudaGraphLaunch(b->exec, as_stream(stream)), "batch launch");
+}
+
+int bgi_batch_destroy(bgi_batch *b) {
+    if (!b) return BGI_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    delete b;
+    return BGI_OK;
 }
 
 int bgi_set_schedule(bgi_imager *im, int images_per_wave, int lanes) {

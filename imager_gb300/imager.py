@@ -297,3 +297,48 @@ class Imager:
         out = np.zeros(n_images, np.uint32)
         call("bgi_last_weight_sums", self._h, _ptr(out), int(n_images), _stream(stream))
         return out
+
+
+class Batch:
+    """Uneven items (imager, device data, images) replayed as one CUDA graph.
+
+    items: list of dicts with keys imager, data, and optionally scales, fmt ("c64"), flags,
+    out (allocated when missing).  Creating the batch runs the items once."""
+
+    def __init__(self, items, stream=None):
+        self._items = []
+        arr = (capi.BatchItem * len(items))()
+        for k, it in enumerate(items):
+            h = it["imager"]
+            data = it["data"]
+            fmt = it.get("fmt", "c64")
+            flags = int(it.get("flags", APPLY_GEOMETRIC | APPLY_CABLE))
+            T, Cn = int(data.shape[0]), int(data.shape[1])
+            out = it.get("out")
+            if out is None:
+                out = torch.empty((T, Cn, h.n_pixels, h.n_pixels), dtype=_out_dtype(flags), device=data.device)
+            scales = it.get("scales")
+            arr[k] = capi.BatchItem(h._h.value, VIS_FORMAT[fmt], data.data_ptr(),
+                                    scales.data_ptr() if scales is not None else None, T, flags, out.data_ptr())
+            self._items.append((h, data, scales, out))
+        b = C.c_void_p()
+        call("bgi_batch_create", arr, len(items), _stream(stream), C.byref(b))
+        self._b = b
+
+    @property
+    def outputs(self):
+        return [it[3] for it in self._items]
+
+    def launch(self, stream=None):
+        call("bgi_batch_launch", self._b, _stream(stream))
+
+    def close(self):
+        if self._b:
+            capi.lib().bgi_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -274,6 +274,30 @@ BGI_API int bgi_autotune(bgi_imager *im, int format, const void *data, const flo
                          int n_intervals, unsigned flags, float *images, void *stream,
                          double *best_ms);
 
+/* Batches of uneven items replayed as one CUDA graph (no reference counterpart).  An item is
+ * one bgi_image / bgi_image_compressed call on device buffers: its imager (array, image side,
+ * pol and schedule), storage format, data (+ scales), interval count, flags and images.
+ * bgi_batch_create runs the items once on `stream` (sizing every scratch buffer; synchronous),
+ * then captures them into a graph in which items of different imagers run concurrently (each
+ * imager's items in order, as they share its scratch) and instantiates it.  bgi_batch_launch
+ * replays the whole batch with one graph launch on `stream`: the same buffers, read and written
+ * again.  The imagers and buffers must outlive the batch and keep their state (no set_array,
+ * set_frequencies, set_uv_cell, set_schedule or set_deterministic on them while it exists;
+ * stage timing off). */
+typedef struct bgi_batch bgi_batch;
+typedef struct bgi_batch_item {
+    bgi_imager *imager;
+    int format;          /* enum bgi_vis_format */
+    const void *data;    /* device visibilities in that format */
+    const float *scales; /* device block scales (16-bit formats), else NULL */
+    int n_intervals;
+    unsigned flags;      /* BGI_APPLY_*, BGI_OUTPUT_REAL */
+    float *images;       /* device images */
+} bgi_batch_item;
+BGI_API int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi_batch **out);
+BGI_API int bgi_batch_launch(bgi_batch *batch, void *stream);
+BGI_API int bgi_batch_destroy(bgi_batch *batch);
+
 /* Deterministic mode (default off): bgi_image and bgi_image_host grid with the ordered
  * per-cell sums of bgi_gridding_sorted_gpu on the full plane, so every image is the same bits
  * on every run and whatever else shares the call.  No reference counterpart. */
