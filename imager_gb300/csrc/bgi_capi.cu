@@ -711,35 +711,15 @@ struct bgi_batch {
 
 namespace {
 
-// Issues every item on stream s: items of one handle chain on one forked stream (they share its
-// scratch); different handles run on different streams.  `streams` and `events` hold the forks.
-int issue_batch(const bgi_batch_item *items, int n_items, cudaStream_t s, std::vector<cudaStream_t> &streams,
-                std::vector<cudaEvent_t> &joins, cudaEvent_t fork) {
-    std::vector<bgi_imager *> handles;
-    for (int i = 0; i < n_items; ++i)
-        if (std::find(handles.begin(), handles.end(), items[i].imager) == handles.end())
-            handles.push_back(items[i].imager);
-    BGI_TRY(check_cuda(cudaEventRecord(fork, s), "batch fork"));
-    for (size_t k = 0; k < handles.size(); ++k) {
-        BGI_TRY(check_cuda(cudaStreamWaitEvent(streams[k], fork, 0), "batch fork wait"));
-        for (int i = 0; i < n_items; ++i) {
-            if (items[i].imager != handles[k]) continue;
-            const bgi_batch_item &it = items[i];
-            BGI_TRY(image_impl(it.imager, it.format, it.data, it.scales, it.n_intervals, it.flags, it.images,
-                               streams[k]));
-        }
-        BGI_TRY(check_cuda(cudaEventRecord(joins[k], streams[k]), "batch join"));
-        BGI_TRY(check_cuda(cudaStreamWaitEvent(s, joins[k], 0), "batch join wait"));
+// Issues every item on stream s, in order.  Each item overlaps its own waves on its imager's
+// lanes; running different items at once as well would hold several imagers' L2-sized grid
+// scratch at the same time and push it out of L2 (measured slower).
+int issue_batch(const bgi_batch_item *items, int n_items, cudaStream_t s) {
+    for (int i = 0; i < n_items; ++i) {
+        const bgi_batch_item &it = items[i];
+        BGI_TRY(image_impl(it.imager, it.format, it.data, it.scales, it.n_intervals, it.flags, it.images, s));
     }
     return BGI_OK;
-}
-
-int distinct_handles(const bgi_batch_item *items, int n_items) {
-    std::vector<bgi_imager *> handles;
-    for (int i = 0; i < n_items; ++i)
-        if (std::find(handles.begin(), handles.end(), items[i].imager) == handles.end())
-            handles.push_back(items[i].imager);
-    return (int)handles.size();
 }
 
 }  // namespace
@@ -761,20 +741,13 @@ int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi
     // be captured), ordered after the caller's stream
     cudaStream_t user = as_stream(stream), s = nullptr;
     BGI_TRY(check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "batch stream"));
-    const int n_h = distinct_handles(items, n_items);
-    std::vector<cudaStream_t> streams((size_t)n_h, nullptr);
-    std::vector<cudaEvent_t> joins((size_t)n_h, nullptr);
     cudaEvent_t fork = nullptr;
     int st = check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "batch event");
     if (!st) st = check_cuda(cudaEventRecord(fork, user), "batch order");
     if (!st) st = check_cuda(cudaStreamWaitEvent(s, fork, 0), "batch order");
-    for (int k = 0; !st && k < n_h; ++k) {
-        st = check_cuda(cudaStreamCreateWithFlags(&streams[(size_t)k], cudaStreamNonBlocking), "batch stream");
-        if (!st) st = check_cuda(cudaEventCreateWithFlags(&joins[(size_t)k], cudaEventDisableTiming), "batch event");
-    }
     // one run outside the capture sizes every scratch buffer and builds the channel tables, so
     // that the captured calls allocate nothing
-    if (!st) st = issue_batch(items, n_items, s, streams, joins, fork);
+    if (!st) st = issue_batch(items, n_items, s);
     if (!st) st = check_cuda(cudaStreamSynchronize(s), "batch warm-up");
     if (!st) st = check_cuda(cudaGetLastError(), "batch warm-up");
     auto b = std::make_unique<bgi_batch>();
@@ -782,15 +755,11 @@ int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi
     b->n_items = n_items;
     if (!st) st = check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "batch capture");
     if (!st) {
-        const int issued = issue_batch(items, n_items, s, streams, joins, fork);
+        const int issued = issue_batch(items, n_items, s);
         const int ended = check_cuda(cudaStreamEndCapture(s, &b->graph), "batch end capture");
         st = issued ? issued : ended;
     }
     if (!st) st = check_cuda(cudaGraphInstantiate(&b->exec, b->graph, 0), "batch instantiate");
-    for (int k = 0; k < n_h; ++k) {
-        if (streams[(size_t)k]) cudaStreamDestroy(streams[(size_t)k]);
-        if (joins[(size_t)k]) cudaEventDestroy(joins[(size_t)k]);
-    }
     if (fork) cudaEventDestroy(fork);
     cudaStreamDestroy(s);
     if (st) {

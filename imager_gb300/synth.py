@@ -137,8 +137,10 @@ def point_sources(rng, n_src, s_min=0.1, s_max=100.0, alpha=-2.0):
     return s, sin_t * np.cos(phi), sin_t * np.sin(phi), n
 
 
-def _model_vis(uvw, freqs, flux, l, m, n, device):
-    """Sum over sources of S*exp(-2*pi*i*(u*l + v*m + w*(n-1))/lambda): complex128 [T][C][B]."""
+def _model_vis(uvw, freqs, flux, l, m, n, device, fast=False):
+    """Sum over sources of S*exp(-2*pi*i*(u*l + v*m + w*(n-1))/lambda): complex128 [T][C][B].
+    fast: the phase is reduced to a fractional turn in FP64 and the exponential and the sum run
+    in FP32 (for large blocks; the result is input data, not a reference)."""
     import torch
     dev = torch.device(device)
     uvw_t = torch.as_tensor(uvw, dtype=torch.float64, device=dev)          # [T][B][3]
@@ -148,6 +150,14 @@ def _model_vis(uvw, freqs, flux, l, m, n, device):
     lmn = torch.as_tensor(np.stack([l, m, n - 1.0], 1), dtype=torch.float64, device=dev)
     s = torch.as_tensor(flux, dtype=torch.float64, device=dev)
     delay = uvw_t @ lmn.T                                                   # [T][B][S] metres
+    if fast:
+        s32 = s.to(torch.float32)
+        for c in range(len(freqs)):
+            turns = inv_lam[c] * delay
+            frac = (turns - torch.round(turns)).to(torch.float32)           # [T][B][S]
+            ph = (-2 * math.pi) * frac
+            out[:, c, :] = torch.complex(torch.cos(ph) @ s32, torch.sin(ph) @ s32).to(torch.complex128)
+        return out
     for c in range(len(freqs)):
         ph = (-2 * math.pi) * inv_lam[c] * delay                            # [T][B][S]
         out[:, c, :] = torch.sum(s * torch.exp(1j * ph), dim=-1)
@@ -156,7 +166,9 @@ def _model_vis(uvw, freqs, flux, l, m, n, device):
 
 def make_observation(seed, n_ant, enu, n_intervals, freqs, n_pixels, n_src=50, noise_sigma=1.0,
                      per_interval_uvw=True, flagged_ants=(), cadence_s=1.0, device="cpu",
-                     cable_max_m=200.0, pol="XX") -> Observation:
+                     cable_max_m=200.0, pol="XX", fast=False, diffuse=None) -> Observation:
+    """diffuse = (amp_jy, beta): a diffuse background whose visibilities are complex Gaussian with
+    rms amp * (1 + |uv|/10 wavelengths)^(-beta/2) (a power-law sky), the same in XX and YY."""
     import torch
     rng = np.random.Generator(np.random.PCG64(seed))
     freqs = np.asarray(freqs, np.float64)
@@ -170,16 +182,27 @@ def make_observation(seed, n_ant, enu, n_intervals, freqs, n_pixels, n_src=50, n
     uvw_full = uvw32.astype(np.float64)
     if n_sets == 1 and T > 1:
         uvw_full = np.ascontiguousarray(np.broadcast_to(uvw_full, (T,) + uvw_full.shape[1:]))
-    model = _model_vis(uvw_full, freqs, flux, l, m, n, device)             # [T][C][B]
+    model = _model_vis(uvw_full, freqs, flux, l, m, n, device, fast=fast)  # [T][C][B]
     dev = model.device
     g = torch.Generator(device="cpu").manual_seed(seed)
     sig = noise_sigma / math.sqrt(2.0)
 
+    gd = torch.Generator(device=dev).manual_seed(seed) if fast else None  # large blocks: draw on the device
+
     def noise():
-        re = torch.randn((T, Cn, B), generator=g, dtype=torch.float32).to(dev)
-        im = torch.randn((T, Cn, B), generator=g, dtype=torch.float32).to(dev)
+        if gd is not None:
+            re = torch.randn((T, Cn, B), generator=gd, dtype=torch.float32, device=dev)
+            im = torch.randn((T, Cn, B), generator=gd, dtype=torch.float32, device=dev)
+        else:
+            re = torch.randn((T, Cn, B), generator=g, dtype=torch.float32).to(dev)
+            im = torch.randn((T, Cn, B), generator=g, dtype=torch.float32).to(dev)
         return torch.complex(re, im).to(torch.complex128) * sig
 
+    if diffuse is not None:
+        amp, beta = diffuse
+        uv = torch.as_tensor(np.hypot(uvw_full[..., 0], uvw_full[..., 1]), dtype=torch.float64, device=dev)  # [T][B]
+        uv_lam = uv[:, None, :] * torch.as_tensor(freqs / VEL_LIGHT, dtype=torch.float64, device=dev)[None, :, None]
+        model = model + noise() * (amp / sig if sig else amp) * (1.0 + uv_lam / 10.0) ** (-beta / 2.0)
     vis = torch.empty((T, Cn, B, 4), dtype=torch.complex128, device=dev)
     vis[..., 0] = model + noise()
     vis[..., 1] = noise()
@@ -247,3 +270,16 @@ def serving_arrays(device="cpu", n_channels=32):
         enu = layout_substations(rng, n_ant, 16) if n_ant == 512 else layout_uniform_disk(rng, n_ant, 35.0)
         out.append(make_observation(1239 + k, n_ant, enu, 1, freqs, n_pix, device=device))
     return out
+
+
+
+def batched_bands(device="cpu", n_intervals=5):
+    """The uneven batch workload: 512 antennas in 16 clustered sub-stations over 3 km, 256 channels
+    over 100-200 MHz in four bands of 64 imaged at 256, 512, 1024 and 2048 pixels, 5 intervals,
+    400 point sources and a diffuse power-law background (seed 1238).  One Observation per band
+    (the same array)."""
+    rng = np.random.Generator(np.random.PCG64(1238))
+    enu = layout_substations(rng, 512, 16)
+    freqs = 100e6 + np.arange(256) * (100e6 / 256)
+    return [make_observation(1238 + k, 512, enu, n_intervals, freqs[64 * k:64 * (k + 1)], 256 << k, n_src=400,
+                             device=device, fast=True, diffuse=(10.0, 2.0)) for k in range(4)]

@@ -278,8 +278,9 @@ BGI_API int bgi_autotune(bgi_imager *im, int format, const void *data, const flo
  * one bgi_image / bgi_image_compressed call on device buffers: its imager (array, image side,
  * pol and schedule), storage format, data (+ scales), interval count, flags and images.
  * bgi_batch_create runs the items once on `stream` (sizing every scratch buffer; synchronous),
- * then captures them into a graph in which items of different imagers run concurrently (each
- * imager's items in order, as they share its scratch) and instantiates it.  bgi_batch_launch
+ * then captures them, in order, into a graph and instantiates it (each item overlaps its own
+ * waves on its imager's lanes; items are not run at once, which would hold several imagers'
+ * L2-sized grid scratch together and push it out of L2).  bgi_batch_launch
  * replays the whole batch with one graph launch on `stream`: the same buffers, read and written
  * again.  The imagers and buffers must outlive the batch and keep their state (no set_array,
  * set_frequencies, set_uv_cell, set_schedule or set_deterministic on them while it exists;
