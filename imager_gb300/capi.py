@@ -65,6 +65,7 @@ _SIGNATURES = {
     "bgi_fft_inverse_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
     "bgi_compressed_size": (_i, [_i, _i, _i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "bgi_compress_visibilities": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "bgi_ingest_correlation_matrices": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "bgi_image_compressed": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp]),
     "bgi_image_compressed_host": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp]),
     "bgi_fft_shift_and_norm_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp]),

@@ -863,6 +863,22 @@ int bgi_compressed_size(int n_ant, int n_channels, int n_intervals, size_t *data
     return BGI_OK;
 }
 
+int bgi_ingest_correlation_matrices(const float *re_xx, const float *im_xx, const float *re_yy, const float *im_yy,
+                                    int n_ant, int n_channels, int n_intervals, int format, void *data,
+                                    float *scales, void *stream) {
+    if (!re_xx || !im_xx || !data || n_ant < 1 || n_ant > 46340 || n_channels < 1 || n_intervals < 0)
+        return set_error(BGI_ERR_INVALID, "ingest: bad arguments");
+    if ((re_yy == nullptr) != (im_yy == nullptr)) return set_error(BGI_ERR_INVALID, "ingest: YY needs both parts");
+    if (format < BGI_VIS_C64 || format > BGI_VIS_FP16) return set_error(BGI_ERR_INVALID, "ingest: bad format %d", format);
+    if (format != BGI_VIS_C64 && !scales) return set_error(BGI_ERR_INVALID, "ingest: the 16-bit formats need scales");
+    const uintptr_t need = format == BGI_VIS_C64 ? 15u : 3u;
+    if ((reinterpret_cast<uintptr_t>(data) & need) || (reinterpret_cast<uintptr_t>(scales) & 3u) ||
+        (reinterpret_cast<uintptr_t>(re_xx) & 3u) || (reinterpret_cast<uintptr_t>(im_xx) & 3u))
+        return set_error(BGI_ERR_INVALID, "ingest: misaligned buffer");
+    return launch_ingest(re_xx, im_xx, re_yy, im_yy, n_ant, (long long)n_channels * n_intervals, format, data, scales,
+                         as_stream(stream));
+}
+
 int bgi_compress_visibilities(const float *vis, int n_ant, int n_channels, int n_intervals, int format, void *data,
                               float *scales, void *stream) {
     if (!vis || !data || !scales || n_ant < 1 || n_channels < 1 || n_intervals < 0)

@@ -54,6 +54,9 @@ int launch_channel_consts(const double *freqs, int n_channels, double du, double
 long long vis_blocks(long long n_baselines);
 int launch_compress(const float *vis, long long n_baselines, long long n_images, int format, void *data,
                     float *scales, cudaStream_t s);
+// correlation matrices [img][n_ant][n_ant] (XX, YY or null) -> records (BGI_VIS_C64) or planes
+int launch_ingest(const float *re_xx, const float *im_xx, const float *re_yy, const float *im_yy, int n_ant,
+                  long long n_images, int format, void *data, float *scales, cudaStream_t s);
 
 // ---- deterministic gridding (bgi_sorted.cu) ------------------------------------------------
 // Point indices 2*b(+1) are 32-bit: at most 46,340 antennas (about 1.07e9 baselines).

@@ -128,6 +128,23 @@ def compress_visibilities(vis, fmt="s16", stream=None):
     return data, scales
 
 
+def ingest_correlation_matrices(re_xx, im_xx, re_yy=None, im_yy=None, fmt="c64", stream=None):
+    """Correlation matrices (device float32 [T][C][n][n]) to visibilities: complex64 records
+    [T][C][B][4] for fmt "c64", else 16-bit stored (data, scales) as compress_visibilities."""
+    T, Cn, n = int(re_xx.shape[0]), int(re_xx.shape[1]), int(re_xx.shape[2])
+    B = n * (n + 1) // 2
+    if fmt == "c64":
+        vis = torch.empty((T, Cn, B, 4), dtype=torch.complex64, device=re_xx.device)
+        call("bgi_ingest_correlation_matrices", _ptr(re_xx), _ptr(im_xx), _ptr(re_yy), _ptr(im_yy), n, Cn, T,
+             VIS_FORMAT[fmt], _ptr(vis), None, _stream(stream))
+        return vis
+    data = torch.empty((T, Cn, 4, B, 2), dtype=torch.int16, device=re_xx.device)
+    scales = torch.empty((T, Cn, 4, (B + 127) // 128), dtype=torch.float32, device=re_xx.device)
+    call("bgi_ingest_correlation_matrices", _ptr(re_xx), _ptr(im_xx), _ptr(re_yy), _ptr(im_yy), n, Cn, T,
+         VIS_FORMAT[fmt], _ptr(data), _ptr(scales), _stream(stream))
+    return data, scales
+
+
 def fft_inverse(grids, images, stream=None):
     """gpufftExecC2C(..., BACKWARD) replacement: unnormalised inverse 2D FFT, out of place."""
     n = int(grids.shape[-1])

@@ -223,6 +223,17 @@ BGI_API int bgi_compressed_size(int n_ant, int n_channels, int n_intervals, size
                                 size_t *scale_bytes);
 BGI_API int bgi_compress_visibilities(const float *vis, int n_ant, int n_channels, int n_intervals,
                                       int format, void *data, float *scales, void *stream);
+/* ConvertFits2XCorr (apps/pacer_imager_main.cpp:720-804), on the GPU for whole blocks:
+ * correlation matrices float[T][C][n_ant][n_ant] (row = first antenna; XX, and YY or both NULL)
+ * to visibilities.  Element (i, j), j <= i, is baseline i(i+1)/2 + j; XX goes to pol 0, YY to
+ * pol 3 (zero without YY matrices, as the reference), XY and YX are zero (the reference leaves
+ * them unset).  format BGI_VIS_C64 writes records float[T][C][B][4][2] to data; the 16-bit
+ * formats write the pol planes and scales directly, encoded as bgi_compress_visibilities would
+ * encode the records (one pass from correlator output to stored visibilities). */
+BGI_API int bgi_ingest_correlation_matrices(const float *re_xx, const float *im_xx,
+                                            const float *re_yy, const float *im_yy, int n_ant,
+                                            int n_channels, int n_intervals, int format, void *data,
+                                            float *scales, void *stream);
 BGI_API int bgi_image_compressed(bgi_imager *im, int format, const void *data, const float *scales,
                                  int n_intervals, unsigned flags, float *images, void *stream);
 BGI_API int bgi_image_compressed_host(bgi_imager *im, int format, const void *data_host,

@@ -463,3 +463,24 @@ void bgo_image_average(const float *images, int64_t image_size, int n_images, fl
         out[2 * k + 1] = m / (float)n_images;
     }
 }
+
+/* apps/pacer_imager_main.cpp:720-804 (ConvertFits2XCorr): the lower triangle of the XX (and YY)
+ * correlation matrices into visibility records.  Element (row i, column j) of a matrix, j <= i,
+ * is baseline i*(i+1)/2 + j (the reference reads getXY(j, i) of its row-major FITS image); XX
+ * goes to record slot 0 and YY to slot 3 (zero when no YY matrices are given, :777); the
+ * reference leaves XY and YX unset, here they are zero.  Matrices float[n_matrices][n][n]. */
+void bgo_ingest_matrices(const float *re_xx, const float *im_xx, const float *re_yy,
+                         const float *im_yy, int n_ant, int64_t n_matrices, float *vis) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2, nn = (int64_t)n_ant * n_ant;
+    for (int64_t m = 0; m < n_matrices; ++m)
+        for (int i = 0; i < n_ant; ++i)
+            for (int j = 0; j <= i; ++j) {
+                const int64_t b = (int64_t)i * (i + 1) / 2 + j, e = m * nn + (int64_t)i * n_ant + j;
+                float *rec = vis + (m * nb + b) * 8;
+                rec[0] = (float)(double)re_xx[e];
+                rec[1] = (float)(double)im_xx[e];
+                rec[2] = rec[3] = rec[4] = rec[5] = 0.0f;
+                rec[6] = re_yy && im_yy ? (float)(double)re_yy[e] : 0.0f;
+                rec[7] = re_yy && im_yy ? (float)(double)im_yy[e] : 0.0f;
+            }
+}

@@ -117,6 +117,11 @@ void bgo_image_average(const float *images, int64_t image_size, int n_images, fl
 
 int bgo_max_threads(void);
 
+/* Correlation matrices float[n_matrices][n_ant][n_ant] (XX, and YY or NULL) to visibility
+ * records float[n_matrices][B][4][2] (apps/pacer_imager_main.cpp:720-804). */
+void bgo_ingest_matrices(const float *re_xx, const float *im_xx, const float *re_yy,
+                         const float *im_yy, int n_ant, int64_t n_matrices, float *vis);
+
 /* Block-scaled 16-bit visibility storage of the GB300 imager (no reference counterpart; the
  * format is stated in blink_compress.c).  format: BGO_VIS_S16, BGO_VIS_BF16 or BGO_VIS_FP16. */
 enum { BGO_VIS_C64 = 0, BGO_VIS_S16 = 1, BGO_VIS_BF16 = 2, BGO_VIS_FP16 = 3 };

@@ -69,6 +69,7 @@ def library():
             "bgo_image_average": (None, [_f32p, i64, i32, _f32p]),
             "bgo_max_threads": (i32, []),
             "bgo_compressed_blocks": (i64, [i64]),
+            "bgo_ingest_matrices": (None, [_f32p, _f32p, C.c_void_p, C.c_void_p, i32, i64, _f32p]),
             "bgo_compress": (None, [_f32p, i64, i64, i32, _u16p, _f32p]),
             "bgo_decompress": (None, [_u16p, _f32p, i64, i64, i32, _f32p]),
         }
@@ -260,4 +261,19 @@ def decompress(data, scales, fmt="s16"):
     T, Cn, _, nb = data.shape[:4]
     vis = np.empty((T, Cn, nb, 4, 2), np.float32)
     library().bgo_decompress(data.reshape(-1), scales.reshape(-1), T * Cn, nb, VIS_FORMAT[fmt], vis.reshape(-1))
+    return vis
+
+
+def ingest_matrices(re_xx, im_xx, re_yy=None, im_yy=None):
+    """Correlation matrices float32 [M][n][n] -> visibility records float32 [M][B][4][2]
+    (apps/pacer_imager_main.cpp:720-804)."""
+    re_xx = np.ascontiguousarray(re_xx, np.float32)
+    im_xx = np.ascontiguousarray(im_xx, np.float32)
+    M, n = re_xx.shape[0], re_xx.shape[1]
+    yy = re_yy is not None and im_yy is not None
+    ry = np.ascontiguousarray(re_yy, np.float32) if yy else None
+    iy = np.ascontiguousarray(im_yy, np.float32) if yy else None
+    vis = np.empty((M, n * (n + 1) // 2, 4, 2), np.float32)
+    library().bgo_ingest_matrices(re_xx.reshape(-1), im_xx.reshape(-1), ry.ctypes.data if yy else None,
+                                  iy.ctypes.data if yy else None, n, M, vis.reshape(-1))
     return vis

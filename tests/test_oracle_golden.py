@@ -171,3 +171,21 @@ def test_compress_s16_known_answers(oracle_lib):
     back = O.decompress(data, scales, "s16")
     assert np.isnan(back[0, 0, 1, 0, 0]) and np.isnan(back[0, 0, 2, 0, 0])
     assert back[0, 0, 0, 0, 0] == np.float32(32767) * scales[0, 0, 0, 0]
+
+
+def test_ingest_matrices_known_answer(oracle_lib):
+    """ConvertFits2XCorr's mapping (apps/pacer_imager_main.cpp:720-804): element (i, j), j <= i,
+    of the XX matrix is baseline i(i+1)/2 + j, pol 0; YY goes to pol 3, zero without YY."""
+    O = oracle_lib
+    n = 3
+    re = np.arange(9, dtype=np.float32).reshape(1, n, n)
+    im = -re - 0.5
+    vis = O.ingest_matrices(re, im)
+    assert vis.shape == (1, 6, 4, 2)
+    # baselines (0,0) (1,0) (1,1) (2,0) (2,1) (2,2) -> matrix elements 0, 3, 4, 6, 7, 8
+    assert np.array_equal(vis[0, :, 0, 0], np.float32([0, 3, 4, 6, 7, 8]))
+    assert np.array_equal(vis[0, :, 0, 1], np.float32([0, 3, 4, 6, 7, 8]) * -1 - 0.5)
+    assert not vis[0, :, 1:, :].any()
+    vis_yy = O.ingest_matrices(re, im, re * 2, im * 2)
+    assert np.array_equal(vis_yy[0, :, 3, 0], 2 * vis[0, :, 0, 0])
+    assert not vis_yy[0, :, 1:3, :].any()
