@@ -484,3 +484,132 @@ void bgo_ingest_matrices(const float *re_xx, const float *im_xx, const float *re
                 rec[7] = re_yy && im_yy ? (float)(double)im_yy[e] : 0.0f;
             }
 }
+
+/* ------------------------------------------------------------------------------------------
+ * Kaiser-Bessel convolutional gridding, CPU only in the reference (m_nConvolvingKernelSize > 0,
+ * src/pacer_imager.cpp:378-403 and 565-750).
+ * ------------------------------------------------------------------------------------------ */
+
+/* src/pacer_imager.cpp:565-577: unnormalised modified Bessel function I0 by its series */
+static double kb_bessel0(double x, double precision) {
+    double d = 0.0, ds = 1.0, sum = 1.0;
+    do {
+        d += 2.0;
+        ds *= x * x / (d * d);
+        sum += ds;
+    } while (ds > sum * precision);
+    return sum;
+}
+
+/* src/pacer_imager.cpp:579-596.  For an even length the reference also writes kernel[n], one
+ * element past its vector; nothing reads it, and it is not written here. */
+static void kb_kernel_1d(double *kernel, size_t n, double alpha, size_t osf, int with_sinc) {
+    const size_t mid = n / 2;
+    double *sinc = (double *)malloc(sizeof(double) * (mid + 1));
+    const double filter_ratio = 1.0 / (double)osf;
+    sinc[0] = filter_ratio;
+    for (size_t i = 1; i != mid + 1; i++) {
+        const double x = (double)i;
+        sinc[i] = with_sinc ? (sin(M_PI * filter_ratio * x) / (M_PI * x)) : filter_ratio;
+    }
+    const double norm = (double)osf / kb_bessel0(alpha, 1e-8);
+    for (size_t i = 0; i != mid + 1; i++) {
+        const double term = (double)i / (double)mid;
+        if (mid + i < n) kernel[mid + i] = sinc[i] * kb_bessel0(alpha * sqrt(1.0 - (term * term)), 1e-8) * norm;
+    }
+    for (size_t i = 0; i != mid; i++) kernel[i] = kernel[n - 1 - i];
+    free(sinc);
+}
+
+/* src/pacer_imager.cpp:599-651 (makeKernels, alpha 8.6, oversampling 1023): tables[o][x] for
+ * o < 1023, x < kernel_size, with the reference's reversed order of the oversampled rows. */
+void bgo_kb_tables(int kernel_size, int with_sinc, double *tables) {
+    const size_t osf = BGO_KB_OVERSAMPLING, n = (size_t)kernel_size * osf;
+    double *k1 = (double *)malloc(sizeof(double) * n);
+    kb_kernel_1d(k1, n, 8.6, osf, with_sinc);
+    for (size_t i = 0; i != osf; ++i)
+        for (size_t x = 0; x != (size_t)kernel_size; ++x) tables[(osf - i - 1) * kernel_size + x] = k1[x * osf + i];
+    free(k1);
+}
+
+/* src/pacer_imager.cpp:753-778 (calc_xy_grid2 with is_odd = 0) */
+static void kb_xy_grid(double u_pix, double v_pix, int n, int *x_grid, int *y_grid, int im_sign) {
+    const int cx = n / 2, cy = n / 2;
+    const int ui = (int)(im_sign * u_pix + n / 2), vi = (int)(im_sign * v_pix + n / 2);
+    *x_grid = ui < cx ? cx + ui : ui - cx;
+    *y_grid = vi < cy ? cy + vi : vi - cy;
+}
+
+/* src/pacer_imager.cpp:655-750 (convolve_with_kernel): u, v in wavelengths; im_sign +1 for the
+ * visibility, -1 for its conjugate (the same u, v: the taps are mirrored by calc_xy_grid2). */
+static void kb_convolve(float *grid, double re, double im, double u, double v, double du, double dv, int n,
+                        double im_sign, int ksize, const double *tables) {
+    const int osf = BGO_KB_OVERSAMPLING;
+    const double u_exact = u / du, v_exact = v / dv;
+    const double u_pix = round(u / du), v_pix = round(v / dv);
+    int xk = (int)round((u_exact - u_pix) * osf);
+    int yk = (int)round((v_exact - v_pix) * osf);
+    xk = (xk + (osf * 3) / 2) % osf;
+    yk = (yk + (osf * 3) / 2) % osf;
+    const double *xkern = tables + (size_t)xk * ksize, *ykern = tables + (size_t)yk * ksize;
+    const int mid = ksize / 2;
+    int vv = (int)(v_pix - mid);
+    for (int j = 0; j != ksize; ++j) {
+        const double ykv = ykern[j];
+        int uu = (int)(u_pix - mid);
+        for (int i = 0; i != ksize; ++i) {
+            const double kv = ykv * xkern[i];
+            const double re_conv = re * kv;
+            const double im_conv = im_sign * im * kv;
+            int xg, yg;
+            kb_xy_grid(uu, vv, n, &xg, &yg, (int)im_sign);
+            if (xg >= 0 && yg >= 0 && xg < n && yg < n) {
+                float *c = grid + 2 * ((int64_t)yg * n + xg);
+                c[0] = (float)((double)c[0] + re_conv);
+                c[1] = (float)((double)c[1] + im_conv);
+            }
+            uu++;
+        }
+        vv++;
+    }
+}
+
+/* The gridding loop of src/pacer_imager.cpp:297-408 with the convolution kernel: the checks and
+ * counters as the nearest-neighbour loop (counter +1 at the visibility's own cell). */
+int64_t bgo_gridding_kb(const float *vis, int n_intervals, int n_channels, int n_ant, const float *u,
+                        const float *v, int n_uvw_sets, const int *baseline_flags, const double *freqs_hz,
+                        double delta_u, double delta_v, int n_pixels, double min_uv, int pol, int kernel_size,
+                        int with_sinc, float *grids, float *counters) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2, npix = (int64_t)n_pixels * n_pixels;
+    double *tables = (double *)malloc(sizeof(double) * BGO_KB_OVERSAMPLING * kernel_size);
+    bgo_kb_tables(kernel_size, with_sinc, tables);
+    int64_t total = 0;
+    for (int t = 0; t < n_intervals; ++t)
+        for (int ch = 0; ch < n_channels; ++ch) {
+            const int64_t img = (int64_t)t * n_channels + ch, set = n_uvw_sets > 1 ? t : 0;
+            const double wavelength = BGO_VEL_LIGHT / freqs_hz[ch];
+            float *grid = grids + img * npix * 2, *counter = counters + img * npix;
+            memset(grid, 0, sizeof(float) * 2 * npix);
+            memset(counter, 0, sizeof(float) * npix);
+            const float *rec0 = vis + img * nb * 8;
+            for (int64_t b = 0; b < nb; ++b) {
+                if (baseline_flags[b]) continue;
+                float re, im;
+                select_pol(rec0 + b * 8, pol, &re, &im);
+                if (isnan(re) || isnan(im)) continue;
+                if (!(fabsf(re) < BGO_MAX_VIS && fabsf(im) < BGO_MAX_VIS)) continue;
+                const double uu = (double)u[set * nb + b] / wavelength, vv = (double)v[set * nb + b] / wavelength;
+                const int64_t pos = bgo_cell_index(u[set * nb + b], v[set * nb + b], delta_u, delta_v, wavelength,
+                                                   min_uv, n_pixels, +1);
+                const int64_t pos2 = bgo_cell_index(u[set * nb + b], v[set * nb + b], delta_u, delta_v, wavelength,
+                                                    min_uv, n_pixels, -1);
+                if (pos < 0 && pos2 < 0) continue; /* cut by min_uv */
+                kb_convolve(grid, re, im, uu, vv, delta_u, delta_v, n_pixels, 1.0, kernel_size, tables);
+                if (pos >= 0 && pos < npix) { counter[pos] += 1.0f; ++total; }
+                kb_convolve(grid, re, im, uu, vv, delta_u, delta_v, n_pixels, -1.0, kernel_size, tables);
+                if (pos2 >= 0 && pos2 < npix) { counter[pos2] += 1.0f; ++total; }
+            }
+        }
+    free(tables);
+    return total;
+}

@@ -117,6 +117,17 @@ void bgo_image_average(const float *images, int64_t image_size, int n_images, fl
 
 int bgo_max_threads(void);
 
+/* Kaiser-Bessel convolutional gridding (src/pacer_imager.cpp:378-403, 565-750): oversampling
+ * 1023, alpha 8.6, with or without the sinc factor.  bgo_kb_tables writes the reference's
+ * _griddingKernels as double[1023][kernel_size]; bgo_gridding_kb is bgo_gridding with each point
+ * and its conjugate spread over kernel_size^2 cells (sums in double, rounded to float per add). */
+#define BGO_KB_OVERSAMPLING 1023
+void bgo_kb_tables(int kernel_size, int with_sinc, double *tables);
+int64_t bgo_gridding_kb(const float *vis, int n_intervals, int n_channels, int n_ant, const float *u,
+                        const float *v, int n_uvw_sets, const int *baseline_flags, const double *freqs_hz,
+                        double delta_u, double delta_v, int n_pixels, double min_uv, int pol,
+                        int kernel_size, int with_sinc, float *grids, float *counters);
+
 /* Correlation matrices float[n_matrices][n_ant][n_ant] (XX, and YY or NULL) to visibility
  * records float[n_matrices][B][4][2] (apps/pacer_imager_main.cpp:720-804). */
 void bgo_ingest_matrices(const float *re_xx, const float *im_xx, const float *re_yy,

@@ -70,6 +70,9 @@ def library():
             "bgo_max_threads": (i32, []),
             "bgo_compressed_blocks": (i64, [i64]),
             "bgo_ingest_matrices": (None, [_f32p, _f32p, C.c_void_p, C.c_void_p, i32, i64, _f32p]),
+            "bgo_kb_tables": (None, [i32, i32, _f64p]),
+            "bgo_gridding_kb": (i64, [_f32p, i32, i32, i32, _f32p, _f32p, i32, _i32p, _f64p, dbl, dbl, i32, dbl,
+                                      i32, i32, i32, _f32p, _f32p]),
             "bgo_compress": (None, [_f32p, i64, i64, i32, _u16p, _f32p]),
             "bgo_decompress": (None, [_u16p, _f32p, i64, i64, i32, _f32p]),
         }
@@ -91,6 +94,8 @@ def ref_library():
         lib.ref_apply_cable_cpu.argtypes = [_f32p, i32, i32, i32, _f64p, _f64p]
         lib.ref_fft_shift.argtypes = [_f32p, i32, i32]
         lib.ref_fft_shift.restype = None
+        lib.ref_set_kernel_size.argtypes = [i32]
+        lib.ref_set_kernel_size.restype = None
         lib.ref_run.argtypes = [_f32p, i32, i32, i32, _f32p, _f32p, _f32p, _f64p, _i32p, i32,
                                 dbl, i32, dbl, i32, dbl, i32, flt, dbl, i32, C.c_char_p, i32,
                                 i32, _f32p, _f32p, _f32p, _f32p, _f64p]
@@ -277,3 +282,25 @@ def ingest_matrices(re_xx, im_xx, re_yy=None, im_yy=None):
     library().bgo_ingest_matrices(re_xx.reshape(-1), im_xx.reshape(-1), ry.ctypes.data if yy else None,
                                   iy.ctypes.data if yy else None, n, M, vis.reshape(-1))
     return vis
+
+
+def kb_tables(kernel_size, with_sinc=True):
+    """The reference's Kaiser-Bessel gridding kernels, float64 [1023][kernel_size]."""
+    t = np.empty((1023, kernel_size), np.float64)
+    library().bgo_kb_tables(int(kernel_size), int(bool(with_sinc)), t.reshape(-1))
+    return t
+
+
+def gridding_kb(vis, u, v, flags, freqs, du, dv, n_pixels, kernel_size, min_uv=-1000.0, pol="XX", n_uvw_sets=1,
+                with_sinc=True):
+    """Kaiser-Bessel convolutional gridding (src/pacer_imager.cpp:378-403, 565-750)."""
+    T, Cn, nb = vis.shape[:3]
+    n_ant = int(round((-1 + np.sqrt(1 + 8 * nb)) / 2))
+    grids = np.zeros((T, Cn, n_pixels, n_pixels, 2), np.float32)
+    counters = np.zeros((T, Cn, n_pixels, n_pixels), np.float32)
+    n = library().bgo_gridding_kb(np.ascontiguousarray(vis, np.float32).reshape(-1), T, Cn, n_ant,
+                                  np.ascontiguousarray(u, np.float32), np.ascontiguousarray(v, np.float32),
+                                  n_uvw_sets, np.ascontiguousarray(flags, np.int32),
+                                  np.ascontiguousarray(freqs, np.float64), du, dv, n_pixels, min_uv, POL[pol],
+                                  int(kernel_size), int(bool(with_sinc)), grids.reshape(-1), counters.reshape(-1))
+    return grids, counters, n

@@ -10,11 +10,15 @@
 extern std::vector<float> g_shim_u, g_shim_v, g_shim_w_tri;
 
 namespace {
+int g_kernel_size = 0;  // convolution kernel of the next harness (0: nearest neighbour)
+
 struct Harness : public CPacerImager {
     Harness(int n_pixels, const std::vector<int> &flagged, Polarization pol, float osf,
             double min_uv, const char *weighting)
         : CPacerImager("", n_pixels, flagged, false, pol, osf, min_uv,
-                       std::numeric_limits<double>::infinity(), weighting) {}
+                       std::numeric_limits<double>::infinity(), weighting) {
+        m_nConvolvingKernelSize = g_kernel_size;
+    }
     MemoryBuffer<std::complex<float>> &grid_buffer() { return grids; }
     MemoryBuffer<float> &counter_buffer() { return grids_counters; }
 };
@@ -29,6 +33,9 @@ Visibilities make_vis(const float *vis, int T, int C, int n_ant) {
 }  // namespace
 
 extern "C" {
+
+// m_nConvolvingKernelSize of the imagers that ref_run builds from now on (src/pacer_imager.h:169)
+void ref_set_kernel_size(int k) { g_kernel_size = k; }
 
 int ref_apply_geometric_cpu(float *vis, int T, int C, int n_ant, const float *w_tri,
                             const double *freqs) {
@@ -90,6 +97,10 @@ int ref_run(const float *vis_in, int T, int C, int n_ant, const float *u, const 
     x.nAveragedChannels = n_avg;
     memcpy(x.data(), vis_in, sizeof(float) * 2 * x.buf.size());
 
+    // The reference builds its convolution kernels lazily inside convolve_with_kernel, which
+    // runs in its OpenMP loop over images: concurrent first calls race on the kernel vectors
+    // (src/pacer_imager.cpp:599-606).  Build them once here; later calls return at once.
+    if (g_kernel_size > 0) im.makeKernels(g_kernel_size);
     im.grid(x);
     const size_t npix = size_t(n_pixels) * n_pixels * T * C;
     memcpy(vis_out, x.data(), sizeof(float) * 2 * x.buf.size());

@@ -28,8 +28,9 @@ COARSE_BW_MHZ, COARSE_CHANNEL, FREQ_RES_MHZ, N_AVG = 1.28, 118, 0.04, 4
 
 
 def ref_run(obs, vis, n_pixels, pol, min_uv=-1000.0, weighting=b"N", geom=1, cable=1,
-            flagged=(3,), freq_override_mhz=-1.0, osf=2.0):
+            flagged=(3,), freq_override_mhz=-1.0, osf=2.0, kernel=0):
     ref = O.ref_library()
+    ref.ref_set_kernel_size(int(kernel))  # m_nConvolvingKernelSize (0: nearest neighbour)
     T, Cn, nb = vis.shape[:3]
     n_ant = obs.n_ant
     npix = n_pixels * n_pixels * T * Cn
@@ -89,6 +90,11 @@ def main():
     cases["run_I_32_fixedfreq"] = (obs, vis, 32, 2, dict(freq_override_mhz=159.375, flagged=()))
     # 6) uniform weighting: empty cells become 0/0 (src/pacer_imager.cpp:421-428)
     cases["run_XX_32_uniform"] = (obs, vis, 32, 0, dict(weighting=b"U"))
+    # 7) Kaiser-Bessel convolution kernels (src/pacer_imager.cpp:378-403, 565-750); odd sizes,
+    #    as an even size makes the reference write one element past its kernel vector
+    cases["run_XX_32_kb7"] = (obs, vis, 32, 0, dict(kernel=7))
+    cases["run_I_48_kb11"] = (obs, vis, 48, 2, dict(kernel=11))
+    cases["run_V_32_kb5_minuv"] = (obs, vis, 32, 3, dict(kernel=5, min_uv=20.0))
 
     arrays = dict(u=obs.u[0], v=obs.v[0], w=obs.w[0], cable=obs.cable, vis=vis, vis_bad=bad,
                   freqs_cotter=freqs)

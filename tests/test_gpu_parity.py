@@ -161,7 +161,7 @@ def test_gridding_against_reference_golden(im):
     meta = ast.literal_eval(str(g["meta"]))
     pols = ["XX", "YY", "I", "V"]
     for name, m in meta.items():
-        if m.get("weighting") == "U":
+        if m.get("weighting") == "U" or m.get("kernel"):
             continue
         vis_c = g[f"{name}__vis_out"]
         Cn = vis_c.shape[1]
@@ -284,7 +284,7 @@ def test_image_against_reference_golden(im):
     checked = 0
     for name, m in meta.items():
         n = m["n_pixels"]
-        if m.get("weighting") == "U" or n & (n - 1):
+        if m.get("weighting") == "U" or m.get("kernel") or n & (n - 1):
             continue
         vis = g["vis_bad"] if name.endswith("_bad") else g["vis"]
         Cn = vis.shape[1]

@@ -56,6 +56,10 @@ def test_imager_run_golden(oracle_lib, run_gold):
         sc = g[f"{name}__scalars"]
         assert du == sc[0] and dv == sc[1], name
         assert np.array_equal(_bits(vis_c), _bits(g[f"{name}__vis_out"])), name
+        if m.get("kernel"):  # Kaiser-Bessel convolutional gridding (src/pacer_imager.cpp:378-403, 565-750)
+            grids, counters, _ = O.gridding_kb(vis_c, g["u"][None], g["v"][None], flags, freqs, du, dv, n,
+                                               m["kernel"], m.get("min_uv", -1000.0), pol)
+            images = O.image_f64(grids, counters)
         if m.get("weighting") == "U":
             grids, counters, _ = O.gridding(vis_c, g["u"][None], g["v"][None], flags, freqs, du, dv, n,
                                             m.get("min_uv", -1000.0), pol, uniform=True)
