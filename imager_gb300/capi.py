@@ -83,6 +83,9 @@ _SIGNATURES = {
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
     "bgi_set_deterministic": (_i, [_vp, _i]),
+    "bgi_set_gridding_kernel": (_i, [_vp, _i, _i]),
+    "bgi_gridding_kb_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _i, _vp, _vp, _i, _i,
+                                 _vp]),
     "bgi_batch_create": (_i, [C.POINTER(BatchItem), _i, _vp, C.POINTER(_vp)]),
     "bgi_batch_launch": (_i, [_vp, _vp]),
     "bgi_batch_destroy": (_i, [_vp]),

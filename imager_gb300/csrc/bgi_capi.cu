@@ -121,6 +121,8 @@ struct bgi_imager {
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
     DevBuf<ChannelConst> d_cc; // per-channel gridding constants for the current delta_u/v
+    int kb_size = 0;           // Kaiser-Bessel kernel size (0: nearest neighbour)
+    DevBuf<float> kb_table;    // its rows [1023][kb_size]
     bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
     double *d_freqs = nullptr;
@@ -392,6 +394,7 @@ int bgi_destroy(bgi_imager *im) {
         im->sorted_ws[l].release();
     }
     im->d_cc.release();
+    im->kb_table.release();
     if (im->ev_fork) cudaEventDestroy(im->ev_fork);
     for (cudaEvent_t e : im->ev_in) cudaEventDestroy(e);
     for (cudaEvent_t e : im->ev_done) cudaEventDestroy(e);
@@ -580,7 +583,9 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.n_pixels = im->cfg.n_pixels;
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
-    p.half_width = im->half_plane() && !im->deterministic ? half_plane_width(im->cfg.n_pixels) : 0;
+    p.half_width = im->half_plane() && !im->deterministic && im->kb_size == 0 ? half_plane_width(im->cfg.n_pixels) : 0;
+    p.kb_size = im->kb_size;
+    p.kb_table = im->kb_table.ptr;
     // the complex-to-real pass stores pixel pairs: 16 bytes of complex or 8 bytes of real pixels
     if ((reinterpret_cast<uintptr_t>(images) & ((flags & BGI_OUTPUT_REAL) ? 7u : 15u)) != 0) p.half_width = 0;
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
@@ -651,6 +656,8 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     BGI_TRY(image_checks(im, n_intervals, flags));
     const float *vis = static_cast<const float *>(data);
     if (!vis || !images || (format != BGI_VIS_C64 && !scales)) return set_error(BGI_ERR_INVALID, "image: null buffer");
+    if (im->deterministic && im->kb_size > 0)
+        return set_error(BGI_ERR_UNSUPPORTED, "image: the ordered gridder has no convolution kernel");
     const uintptr_t need = format == BGI_VIS_C64 ? 15u : 3u;
     if ((reinterpret_cast<uintptr_t>(vis) & need) != 0 || (reinterpret_cast<uintptr_t>(scales) & 3u) != 0 ||
         (reinterpret_cast<uintptr_t>(images) & 7u) != 0)
@@ -1037,6 +1044,43 @@ int bgi_selftest_wait_timeout(int device, void *stream) {
     const int st = launch_wait_timeout_selftest(as_stream(stream));
     cudaSetDevice(prev);
     return st;
+}
+
+int bgi_set_gridding_kernel(bgi_imager *im, int kernel_size, int with_sinc) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_gridding_kernel: null handle");
+    if (kernel_size < 0 || kernel_size > kMaxKernel)
+        return set_error(BGI_ERR_INVALID, "set_gridding_kernel: kernel size 0..%d", kMaxKernel);
+    if (kernel_size == 0) {
+        im->kb_size = 0;
+        return BGI_OK;
+    }
+    BGI_TRY(im->activate());
+    std::vector<float> table;
+    kb_tables(kernel_size, with_sinc != 0, table);
+    BGI_TRY(im->kb_table.ensure(table.size(), "kb table"));
+    BGI_TRY(check_cuda(cudaMemcpy(im->kb_table.ptr, table.data(), sizeof(float) * table.size(), cudaMemcpyHostToDevice),
+                       "kb table upload"));
+    im->kb_size = kernel_size;
+    return BGI_OK;
+}
+
+int bgi_gridding_kb_gpu(const float *vis, int n_ant, int n_channels, int n_intervals, const float *u, const float *v,
+                        int n_uvw_sets, const int *baseline_flags, const double *freqs_hz, double delta_u,
+                        double delta_v, int n_pixels, double min_uv, int pol, int counter_mode, float *counters,
+                        float *grids, int kernel_size, int with_sinc, void *stream) {
+    if (kernel_size < 1 || kernel_size > kMaxKernel)
+        return set_error(BGI_ERR_INVALID, "gridding_kb: kernel size 1..%d", kMaxKernel);
+    GridParams p;
+    BGI_TRY(gridding_params("gridding_kb", vis, n_ant, n_channels, n_intervals, u, v, n_uvw_sets, baseline_flags,
+                            freqs_hz, delta_u, delta_v, n_pixels, min_uv, pol, counter_mode, counters, grids, &p));
+    std::vector<float> table;
+    kb_tables(kernel_size, with_sinc != 0, table);
+    int st = BGI_OK;
+    cudaStream_t s = as_stream(stream);
+    p.kb_table = kb_free_table(s, table, &st);
+    if (st) return st;
+    p.kb_size = kernel_size;
+    return launch_gridding(p, s);
 }
 
 int bgi_set_deterministic(bgi_imager *im, int enable) {

@@ -182,6 +182,10 @@ int launch_channel_consts(const double *freqs, int n_channels, double du, double
 
 int launch_gridding(const GridParams &p, cudaStream_t s) {
     if (p.img_count <= 0 || p.n_baselines <= 0) return BGI_OK;
+    if (p.kb_size > 0) {
+        if (p.half_width > 0) return set_error(BGI_ERR_INVALID, "kb gridding: full-plane grids only");
+        return launch_gridding_kb(p, p.kb_table, p.kb_size, s);
+    }
     if (p.vis_format != BGI_VIS_C64 && p.counter_mode >= 0)
         return set_error(BGI_ERR_UNSUPPORTED, "gridding: counter grids need complex64 visibilities");
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "bgi_common.cuh"
 
 namespace bgi {
@@ -44,11 +46,21 @@ struct GridParams {
     int apply_geom, apply_cable;
     int grids_zero;            // 1: grids hold zeros on entry (the ordered gridder then writes
                                // cells instead of reading them first)
+    const float *kb_table;     // Kaiser-Bessel kernel rows [1023][kb_size] (kb_size > 0), else null
+    int kb_size;               // 0: nearest neighbour; K: K x K convolution kernel (full plane)
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
 // table[c] = make_channel_const(freqs[c], du, dv) for c < n_channels
 int launch_channel_consts(const double *freqs, int n_channels, double du, double dv, ChannelConst *table,
                           cudaStream_t s);
+
+// ---- Kaiser-Bessel convolutional gridding (bgi_kb.cu) ----------------------------------------
+constexpr int kMaxKernel = 16;
+// the reference's kernel rows [1023][ksize] as float
+void kb_tables(int ksize, bool with_sinc, std::vector<float> &out);
+int launch_gridding_kb(const GridParams &p, const float *table, int ksize, cudaStream_t s);
+// the free function's device table, filled with `table` (synchronous)
+float *kb_free_table(cudaStream_t s, const std::vector<float> &table, int *status);
 
 // ---- block-scaled 16-bit visibilities (bgi_compress.cu) -------------------------------------
 long long vis_blocks(long long n_baselines);

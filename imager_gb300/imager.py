@@ -92,6 +92,16 @@ def gridding(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv, pol, g
          _ptr(grids), _stream(stream))
 
 
+def gridding_kb(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv, pol, grids, counters=None,
+                kernel_size=7, with_sinc=True, counter_mode=capi.COUNTERS_PER_IMAGE, n_uvw_sets=1, stream=None):
+    """Kaiser-Bessel convolutional gridding (src/pacer_imager.cpp:378-403, 565-750) into grids."""
+    T, Cn, B = _vis_dims(vis)
+    call("bgi_gridding_kb_gpu", _ptr(vis), _n_ant(B), Cn, T, _ptr(u), _ptr(v), n_uvw_sets, _ptr(flags),
+         _ptr(freqs), float(delta_u), float(delta_v), int(n_pixels), float(min_uv),
+         POL[pol] if isinstance(pol, str) else int(pol), int(counter_mode), _ptr(counters), _ptr(grids),
+         int(kernel_size), int(bool(with_sinc)), _stream(stream))
+
+
 def gridding_sorted_workspace_bytes(n_ant, n_pixels, n_images):
     """Device bytes bgi_gridding_sorted_gpu needs to grid n_images images in one chunk."""
     out = C.c_size_t(0)
@@ -293,6 +303,10 @@ class Imager:
         call("bgi_autotune", self._h, VIS_FORMAT[fmt], _ptr(data), _ptr(scales), T, int(flags), _ptr(out),
              _stream(stream), C.byref(best))
         return (*self.schedule, best.value)
+
+    def set_gridding_kernel(self, kernel_size: int = 0, with_sinc: bool = True):
+        """0: nearest neighbour; 1..16: the reference's Kaiser-Bessel convolution kernel."""
+        call("bgi_set_gridding_kernel", self._h, int(kernel_size), int(bool(with_sinc)))
 
     def set_deterministic(self, enable: bool = True):
         """Grid by sort and ordered per-cell sums (full plane): the same image bits on every run."""

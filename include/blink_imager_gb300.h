@@ -134,6 +134,19 @@ BGI_API int bgi_gridding_sorted_gpu(const float *vis, int n_ant, int n_channels,
                             int counter_mode, float *counters, float *grids, void *workspace,
                             size_t workspace_bytes, void *stream);
 
+/* Kaiser-Bessel convolutional gridding (the reference's CPU gridding with
+ * m_nConvolvingKernelSize > 0, src/pacer_imager.cpp:378-403 and 565-750; CPU only there): as
+ * bgi_gridding_gpu, but each visibility and its conjugate are spread over kernel_size^2 cells
+ * (1..16) with the reference's kernel (1023 oversampled rows, Kaiser-Bessel alpha 8.6, times a
+ * sinc unless with_sinc == 0); counters count the nearest cells, as the reference's.  The kernel
+ * table lives in a device array of the library, uploaded on `stream` by each call (synchronous). */
+BGI_API int bgi_gridding_kb_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
+                                const float *u, const float *v, int n_uvw_sets,
+                                const int *baseline_flags, const double *freqs_hz, double delta_u,
+                                double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
+                                float *counters, float *grids, int kernel_size, int with_sinc,
+                                void *stream);
+
 /* gpufftPlanMany + gpufftExecC2C(..., BACKWARD) (src/gpu/pacer_imager_hip.cpp:83-99): batched
  * unnormalised inverse 2D FFT, out of place, our own kernels.  n_pixels: power of two,
  * 16..4096. */
@@ -309,6 +322,10 @@ typedef struct bgi_batch_item {
 BGI_API int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi_batch **out);
 BGI_API int bgi_batch_launch(bgi_batch *batch, void *stream);
 BGI_API int bgi_batch_destroy(bgi_batch *batch);
+
+/* Gridding kernel of the handle: 0 (default) nearest neighbour; 1..16 the Kaiser-Bessel kernel
+ * of bgi_gridding_kb_gpu (the full-plane path; not with deterministic mode). */
+BGI_API int bgi_set_gridding_kernel(bgi_imager *im, int kernel_size, int with_sinc);
 
 /* Deterministic mode (default off): bgi_image and bgi_image_host grid with the ordered
  * per-cell sums of bgi_gridding_sorted_gpu on the full plane, so every image is the same bits
