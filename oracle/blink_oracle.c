@@ -613,3 +613,43 @@ int64_t bgo_gridding_kb(const float *vis, int n_intervals, int n_channels, int n
     free(tables);
     return total;
 }
+
+/* Pointed-observation UVW (CAntennaPositions::CalculateUVW with metadata,
+ * src/antenna_positions.cpp:23-92, and PacerGeometry::CalcUVW_NEW / precXYZ / CalcUVW,
+ * src/pacer_geometry.h:101-134, 208-215, 312-334): per timestep, each antenna's XYZ rotated to the
+ * frame at lmst, precessed by rmatpr, rotated back at lmst2000, projected with the hour angle and
+ * declination (TMS eq. 4.1); baseline (i >= j) = -(uvw_i - uvw_j) as float.  step[17]:
+ * rmatpr[9] row-major, sin/cos of lmst, lmst2000, ha2000 and dec_aber (computed by the caller, as
+ * the reference computes them once per timestep with PAL). */
+static void bgo_antenna_uvw(const double *st, double x, double y, double z, double *u, double *v, double *w) {
+    const double *r = st;
+    const double sep = st[9], cep = st[10], s2000 = st[11], c2000 = st[12];
+    const double sh = st[13], ch = st[14], sd = st[15], cd = st[16];
+    const double xpr = cep * x - sep * y;
+    const double ypr = sep * x + cep * y;
+    const double zpr = z;
+    const double xpr2 = (r[0]) * xpr + (r[1]) * ypr + (r[2]) * zpr;
+    const double ypr2 = (r[3]) * xpr + (r[4]) * ypr + (r[5]) * zpr;
+    const double zpr2 = (r[6]) * xpr + (r[7]) * ypr + (r[8]) * zpr;
+    const double xp = c2000 * xpr2 + s2000 * ypr2;
+    const double yp = -s2000 * xpr2 + c2000 * ypr2;
+    const double zp = zpr2;
+    *u = sh * xp + ch * yp;
+    *v = -sd * ch * xp + sd * sh * yp + cd * zp;
+    *w = cd * ch * xp - cd * sh * yp + sd * zp;
+}
+
+void bgo_pointed_uvw(const double *xyz, int n_ant, const double *steps, int n_steps, float *u, float *v, float *w) {
+    const int64_t nb = (int64_t)n_ant * (n_ant + 1) / 2;
+    for (int t = 0; t < n_steps; ++t)
+        for (int i = 0; i < n_ant; ++i)
+            for (int j = 0; j <= i; ++j) {
+                double u1, v1, w1, u2, v2, w2;
+                bgo_antenna_uvw(steps + 17 * t, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], &u1, &v1, &w1);
+                bgo_antenna_uvw(steps + 17 * t, xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], &u2, &v2, &w2);
+                const int64_t b = t * nb + (int64_t)i * (i + 1) / 2 + j;
+                u[b] = (float)(-(u1 - u2));
+                v[b] = (float)(-(v1 - v2));
+                w[b] = (float)(-(w1 - w2));
+            }
+}

@@ -128,6 +128,12 @@ int64_t bgo_gridding_kb(const float *vis, int n_intervals, int n_channels, int n
                         double delta_u, double delta_v, int n_pixels, double min_uv, int pol,
                         int kernel_size, int with_sinc, float *grids, float *counters);
 
+/* Pointed-observation UVW of every baseline for n_steps timesteps (src/antenna_positions.cpp:23-92,
+ * src/pacer_geometry.h:101-134, 208-215, 312-334): xyz double[n_ant][3]; steps double[n_steps][17]
+ * = rmatpr row-major, then sin, cos of lmst, lmst2000, ha2000 and dec_aber; u, v, w float[n_steps][B]. */
+void bgo_pointed_uvw(const double *xyz, int n_ant, const double *steps, int n_steps, float *u, float *v,
+                     float *w);
+
 /* Correlation matrices float[n_matrices][n_ant][n_ant] (XX, and YY or NULL) to visibility
  * records float[n_matrices][B][4][2] (apps/pacer_imager_main.cpp:720-804). */
 void bgo_ingest_matrices(const float *re_xx, const float *im_xx, const float *re_yy,

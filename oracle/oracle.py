@@ -71,6 +71,7 @@ def library():
             "bgo_compressed_blocks": (i64, [i64]),
             "bgo_ingest_matrices": (None, [_f32p, _f32p, C.c_void_p, C.c_void_p, i32, i64, _f32p]),
             "bgo_kb_tables": (None, [i32, i32, _f64p]),
+            "bgo_pointed_uvw": (None, [_f64p, i32, _f64p, i32, _f32p, _f32p, _f32p]),
             "bgo_gridding_kb": (i64, [_f32p, i32, i32, i32, _f32p, _f32p, i32, _i32p, _f64p, dbl, dbl, i32, dbl,
                                       i32, i32, i32, _f32p, _f32p]),
             "bgo_compress": (None, [_f32p, i64, i64, i32, _u16p, _f32p]),
@@ -94,6 +95,8 @@ def ref_library():
         lib.ref_apply_cable_cpu.argtypes = [_f32p, i32, i32, i32, _f64p, _f64p]
         lib.ref_fft_shift.argtypes = [_f32p, i32, i32]
         lib.ref_fft_shift.restype = None
+        lib.ref_pointed_uvw.argtypes = [_f64p, i32, _f64p, _f64p, _f64p, _f64p, _f64p, i32, _f32p, _f32p, _f32p, _f64p]
+        lib.ref_pointed_uvw.restype = None
         lib.ref_set_kernel_size.argtypes = [i32]
         lib.ref_set_kernel_size.restype = None
         lib.ref_run.argtypes = [_f32p, i32, i32, i32, _f32p, _f32p, _f32p, _f64p, _i32p, i32,
@@ -304,3 +307,21 @@ def gridding_kb(vis, u, v, flags, freqs, du, dv, n_pixels, kernel_size, min_uv=-
                                   np.ascontiguousarray(freqs, np.float64), du, dv, n_pixels, min_uv, POL[pol],
                                   int(kernel_size), int(bool(with_sinc)), grids.reshape(-1), counters.reshape(-1))
     return grids, counters, n
+
+
+def uvw_step(rmatpr, ha2000, dec_aber, lmst, lmst2000):
+    """One timestep's geometry as the 17 numbers the pointed-UVW routines take."""
+    r = np.asarray(rmatpr, np.float64).reshape(9)
+    return np.concatenate([r, [np.sin(lmst), np.cos(lmst), np.sin(lmst2000), np.cos(lmst2000), np.sin(ha2000),
+                               np.cos(ha2000), np.sin(dec_aber), np.cos(dec_aber)]])
+
+
+def pointed_uvw(xyz, steps):
+    """Pointed UVW float32 [T][B] x3 from antenna XYZ [n][3] and steps [T][17]."""
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    steps = np.ascontiguousarray(np.atleast_2d(steps), np.float64)
+    n, T = xyz.shape[0], steps.shape[0]
+    nb = n * (n + 1) // 2
+    u, v, w = (np.empty((T, nb), np.float32) for _ in range(3))
+    library().bgo_pointed_uvw(xyz.reshape(-1), n, steps.reshape(-1), T, u.reshape(-1), v.reshape(-1), w.reshape(-1))
+    return u, v, w

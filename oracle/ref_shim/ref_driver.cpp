@@ -1,6 +1,7 @@
 // C-ABI driver around the reference imager's own CPU code (compiled from its sources with the
 // stand-ins in this folder).  Used here only to generate golden vectors that pin the oracle.
 #include "pacer_imager.h"
+#include "pacer_geometry.h"
 #include "corrections.h"
 #include <astroio.hpp>
 #include <cstring>
@@ -113,5 +114,42 @@ int ref_run(const float *vis_in, int T, int C, int n_ant, const float *u, const 
     scalars_out[2] = im.u_max;
     scalars_out[3] = im.v_max;
     return 0;
+}
+
+// Pointed-observation UVW with the reference's own geometry (src/pacer_geometry.h): per
+// timestep t, UVWTimestepInfo from the given angles and matrix, each antenna through
+// PacerGeometry::CalcUVW_NEW, and the baseline loop of CAntennaPositions::CalculateUVW
+// (src/antenna_positions.cpp:57-89).  Also writes each timestep's 17 numbers (matrix, then
+// sin/cos of lmst, lmst2000, ha2000, dec_aber from this libm) for the oracle.
+void ref_pointed_uvw(const double *xyz, int n_ant, const double *rmat, const double *ha2000,
+                     const double *dec_aber, const double *lmst, const double *lmst2000, int n_steps,
+                     float *u_out, float *v_out, float *w_out, double *steps_out) {
+    const unsigned nb = (unsigned)(n_ant * (n_ant + 1)) / 2;
+    for (int t = 0; t < n_steps; ++t) {
+        PacerGeometry::UVWTimestepInfo info;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) info.rmatpr[i][j] = rmat[9 * t + 3 * i + j];
+        info.ha2000 = ha2000[t];
+        info.dec_aber = dec_aber[t];
+        info.lmst = lmst[t];
+        info.lmst2000 = lmst2000[t];
+        double *st = steps_out + 17 * t;
+        for (int k = 0; k < 9; ++k) st[k] = rmat[9 * t + k];
+        st[9] = sin(lmst[t]), st[10] = cos(lmst[t]), st[11] = sin(lmst2000[t]), st[12] = cos(lmst2000[t]);
+        st[13] = sin(ha2000[t]), st[14] = cos(ha2000[t]), st[15] = sin(dec_aber[t]), st[16] = cos(dec_aber[t]);
+        for (unsigned baseline = 0; baseline < nb; baseline++) {
+            unsigned int i{static_cast<unsigned int>(-0.5 + std::sqrt(0.25 + 2 * baseline))};
+            unsigned int j{baseline - ((i + 1) * i) / 2};
+            double u = 0, v = 0, w = 0, u2 = 0, v2 = 0, w2 = 0;
+            PacerGeometry::CalcUVW_NEW(info, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], u, v, w);
+            PacerGeometry::CalcUVW_NEW(info, xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], u2, v2, w2);
+            u = u - u2;
+            v = v - v2;
+            w = w - w2;
+            u_out[t * nb + baseline] = -u;
+            v_out[t * nb + baseline] = -v;
+            w_out[t * nb + baseline] = -w;
+        }
+    }
 }
 }

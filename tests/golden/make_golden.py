@@ -108,6 +108,25 @@ def main():
     arrays["meta"] = np.array(repr(meta))
     np.savez_compressed(os.path.join(OUT, "imager_run.npz"), **arrays)
 
+    # 8) pointed-observation UVW with the reference's geometry routines (src/pacer_geometry.h)
+    rng = np.random.default_rng(17)
+    n_ant, T = 30, 3
+    xyz = rng.uniform(-1500.0, 1500.0, (n_ant, 3))
+    ang = [rng.uniform(0, 2 * np.pi, T) for _ in range(4)]  # ha2000, dec (below), lmst, lmst2000
+    dec = rng.uniform(-1.2, 0.3, T)
+    rmat = np.empty((T, 3, 3))
+    for t in range(T):  # a small rotation, as the precession-nutation matrix is
+        a, b, c = rng.uniform(-3e-3, 3e-3, 3)
+        k = np.array([[0, -c, b], [c, 0, -a], [-b, a, 0]])
+        rmat[t] = np.eye(3) + k + 0.5 * k @ k
+    nb = n_ant * (n_ant + 1) // 2
+    u, v, w = (np.empty((T, nb), np.float32) for _ in range(3))
+    steps = np.empty((T, 17))
+    O.ref_library().ref_pointed_uvw(np.ascontiguousarray(xyz).reshape(-1), n_ant, rmat.reshape(-1), ang[0], dec,
+                                    ang[2], ang[3], T, u.reshape(-1), v.reshape(-1), w.reshape(-1), steps.reshape(-1))
+    np.savez_compressed(os.path.join(OUT, "pointed_uvw.npz"), xyz=xyz, rmat=rmat, ha2000=ang[0], dec_aber=dec,
+                        lmst=ang[2], lmst2000=ang[3], steps=steps, u=u, v=v, w=w)
+
     # 7) fft_shift known answers, computed by the reference's fft_shift (src/pacer_imager.cpp:110)
     shifts = {}
     for (ny, nx) in ((2, 2), (2, 3), (3, 3), (4, 6), (5, 4)):
