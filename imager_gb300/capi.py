@@ -51,6 +51,12 @@ class BatchItem(C.Structure):
                 ("n_intervals", C.c_int), ("flags", C.c_uint), ("images", C.c_void_p)]
 
 
+class UvwStep(C.Structure):
+    _fields_ = [("rmatpr", C.c_double * 9), ("sin_lmst", C.c_double), ("cos_lmst", C.c_double),
+                ("sin_lmst2000", C.c_double), ("cos_lmst2000", C.c_double), ("sin_ha2000", C.c_double),
+                ("cos_ha2000", C.c_double), ("sin_dec", C.c_double), ("cos_dec", C.c_double)]
+
+
 _vp, _i, _i64, _d, _f, _u = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_float, C.c_uint
 _SIGNATURES = {
     "bgi_last_error": (C.c_char_p, []),
@@ -83,6 +89,9 @@ _SIGNATURES = {
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),
     "bgi_image_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _vp, _vp]),
     "bgi_set_deterministic": (_i, [_vp, _i]),
+    "bgi_uvw_step_from_angles": (_i, [_vp, _d, _d, _d, _d, C.POINTER(UvwStep)]),
+    "bgi_pointed_uvw_gpu": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
+    "bgi_set_array_pointed": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
     "bgi_set_gridding_kernel": (_i, [_vp, _i, _i]),
     "bgi_gridding_kb_gpu": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _d, _d, _i, _d, _i, _i, _vp, _vp, _i, _i,
                                  _vp]),

@@ -456,6 +456,80 @@ int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, con
     return BGI_OK;
 }
 
+int bgi_uvw_step_from_angles(const double *rmatpr, double ha2000, double dec_aber, double lmst, double lmst2000,
+                             bgi_uvw_step *out) {
+    if (!rmatpr || !out) return set_error(BGI_ERR_INVALID, "uvw_step_from_angles: null argument");
+    for (int k = 0; k < 9; ++k) out->rmatpr[k] = rmatpr[k];
+    out->sin_lmst = std::sin(lmst);
+    out->cos_lmst = std::cos(lmst);
+    out->sin_lmst2000 = std::sin(lmst2000);
+    out->cos_lmst2000 = std::cos(lmst2000);
+    out->sin_ha2000 = std::sin(ha2000);
+    out->cos_ha2000 = std::cos(ha2000);
+    out->sin_dec = std::sin(dec_aber);
+    out->cos_dec = std::cos(dec_aber);
+    return BGI_OK;
+}
+
+int bgi_pointed_uvw_gpu(const double *xyz, int n_ant, const bgi_uvw_step *steps, int n_steps, float *u, float *v,
+                        float *w, void *stream) {
+    if (!xyz || !steps || !u || !v || !w || n_ant < 1 || n_ant > 46340 || n_steps < 0)
+        return set_error(BGI_ERR_INVALID, "pointed_uvw: bad arguments");
+    static_assert(sizeof(bgi_uvw_step) == 17 * sizeof(double), "bgi_uvw_step is 17 doubles");
+    return launch_pointed_uvw(xyz, n_ant, reinterpret_cast<const double *>(steps), n_steps, u, v, w,
+                              as_stream(stream));
+}
+
+int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_host, int n_steps,
+                          const bgi_uvw_step *steps_host, const int *baseline_flags, const double *cable_lengths) {
+    if (!im || !xyz_host || !steps_host || !baseline_flags || n_ant < 1 || n_ant > 46340 || n_steps < 1)
+        return set_error(BGI_ERR_INVALID, "set_array_pointed: bad arguments");
+    BGI_TRY(im->activate());
+    const long long nb = baselines_of(n_ant);
+    const size_t nuv = (size_t)nb * n_steps;
+    // flags and cable delays as bgi_set_array installs them (with zero placeholder UVW), then the
+    // UVW computed on the device in place of the placeholder
+    double *d_xyz = nullptr, *d_steps = nullptr;
+    unsigned *d_max = nullptr;
+    int st = BGI_OK;
+    {
+        std::vector<float> zero((size_t)nb, 0.f);
+        BGI_TRY(bgi_set_array(im, n_ant, 1, zero.data(), zero.data(), nullptr, baseline_flags, cable_lengths));
+    }
+    // grow the resident UVW to one set per step and compute it
+    dev_free(im->d_u);
+    dev_free(im->d_v);
+    dev_free(im->d_w);
+    im->d_u = im->d_v = im->d_w = nullptr;
+    BGI_TRY(dev_alloc(&im->d_u, nuv, "set_array_pointed u"));
+    BGI_TRY(dev_alloc(&im->d_v, nuv, "set_array_pointed v"));
+    BGI_TRY(dev_alloc(&im->d_w, nuv, "set_array_pointed w"));
+    if (!st) st = dev_alloc(&d_xyz, (size_t)n_ant * 3, "set_array_pointed xyz");
+    if (!st) st = dev_alloc(&d_steps, (size_t)n_steps * 17, "set_array_pointed steps");
+    if (!st) st = dev_alloc(&d_max, (size_t)2, "set_array_pointed max");
+    if (!st) st = check_cuda(cudaMemcpy(d_xyz, xyz_host, sizeof(double) * 3 * n_ant, cudaMemcpyHostToDevice), "copy");
+    if (!st)
+        st = check_cuda(cudaMemcpy(d_steps, steps_host, sizeof(double) * 17 * n_steps, cudaMemcpyHostToDevice), "copy");
+    if (!st) st = launch_pointed_uvw(d_xyz, n_ant, d_steps, n_steps, im->d_u, im->d_v, im->d_w, nullptr);
+    if (!st) st = launch_uv_absmax(im->d_u, im->d_v, im->d_flags, nb, n_steps, d_max, nullptr);
+    unsigned mx[2] = {0, 0};
+    if (!st) st = check_cuda(cudaMemcpy(mx, d_max, sizeof(mx), cudaMemcpyDeviceToHost), "uv max");
+    dev_free(d_xyz);
+    dev_free(d_steps);
+    dev_free(d_max);
+    if (st) return st;
+    float fu, fv;
+    std::memcpy(&fu, &mx[0], 4);
+    std::memcpy(&fv, &mx[1], 4);
+    im->n_uvw_sets = n_steps;
+    im->u_max = fu;
+    im->v_max = fv;
+    im->cc_valid = false;
+    im->delta_u = (double)im->cfg.oversampling_factor * im->u_max / im->cfg.n_pixels;
+    im->delta_v = (double)im->cfg.oversampling_factor * im->v_max / im->cfg.n_pixels;
+    return BGI_OK;
+}
+
 int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz) {
     if (!im || !freqs_hz || n_channels < 1) return set_error(BGI_ERR_INVALID, "set_frequencies: bad arguments");
     for (int c = 0; c < n_channels; ++c)

@@ -54,6 +54,14 @@ int launch_gridding(const GridParams &p, cudaStream_t s);
 int launch_channel_consts(const double *freqs, int n_channels, double du, double dv, ChannelConst *table,
                           cudaStream_t s);
 
+// ---- pointed-observation UVW (bgi_geometry.cu) -------------------------------------------------
+// steps: double[n_steps][17] (bgi_uvw_step); u, v, w: float[n_steps][B]
+int launch_pointed_uvw(const double *xyz, int n_ant, const double *steps, int n_steps, float *u, float *v, float *w,
+                       cudaStream_t s);
+// out2[0], out2[1] = bit patterns of max |u|, max |v| over unflagged baselines of every set
+int launch_uv_absmax(const float *u, const float *v, const int *flags, long long nb, int n_sets, unsigned *out2,
+                     cudaStream_t s);
+
 // ---- Kaiser-Bessel convolutional gridding (bgi_kb.cu) ----------------------------------------
 constexpr int kMaxKernel = 16;
 // the reference's kernel rows [1023][ksize] as float

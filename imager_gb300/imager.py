@@ -102,6 +102,32 @@ def gridding_kb(vis, u, v, flags, freqs, delta_u, delta_v, n_pixels, min_uv, pol
          int(kernel_size), int(bool(with_sinc)), _stream(stream))
 
 
+def pointed_uvw(xyz, steps, stream=None):
+    """Pointed-observation UVW on the device: xyz (device float64 [n_ant][3]) and steps (device
+    float64 [T][17], see uvw_steps) -> u, v, w float32 [T][B] on the device."""
+    n_ant, T = int(xyz.shape[0]), int(steps.shape[0])
+    B = n_ant * (n_ant + 1) // 2
+    u, v, w = (torch.empty((T, B), dtype=torch.float32, device=xyz.device) for _ in range(3))
+    call("bgi_pointed_uvw_gpu", _ptr(xyz), n_ant, _ptr(steps), T, _ptr(u), _ptr(v), _ptr(w), _stream(stream))
+    return u, v, w
+
+
+def uvw_steps(rmatpr, ha2000, dec_aber, lmst, lmst2000):
+    """Timestep geometry float64 [T][17] from per-timestep matrices and angles (host libm)."""
+    rm = np.asarray(rmatpr, np.float64).reshape(-1, 9)
+    ha, dec, lm, lm2 = (np.atleast_1d(np.asarray(a, np.float64)) for a in (ha2000, dec_aber, lmst, lmst2000))
+    out = np.empty((len(ha), 17), np.float64)
+    for t in range(len(ha)):
+        st = capi.UvwStep()
+        r = (C.c_double * 9)(*rm[t])
+        call("bgi_uvw_step_from_angles", C.cast(r, C.c_void_p), float(ha[t]), float(dec[t]), float(lm[t]),
+             float(lm2[t]), C.byref(st))
+        out[t, :9] = list(st.rmatpr)
+        out[t, 9:] = [st.sin_lmst, st.cos_lmst, st.sin_lmst2000, st.cos_lmst2000, st.sin_ha2000, st.cos_ha2000,
+                      st.sin_dec, st.cos_dec]
+    return out
+
+
 def gridding_sorted_workspace_bytes(n_ant, n_pixels, n_images):
     """Device bytes bgi_gridding_sorted_gpu needs to grid n_images images in one chunk."""
     out = C.c_size_t(0)
@@ -215,6 +241,16 @@ class Imager:
         cable = None if cable is None else np.ascontiguousarray(cable, np.float64)
         n_ant = _n_ant(u.shape[1])
         call("bgi_set_array", self._h, n_ant, u.shape[0], _ptr(u), _ptr(v), _ptr(w), _ptr(flags),
+             _ptr(cable))
+
+    def set_array_pointed(self, xyz, steps, flags, cable):
+        """Resident state with pointed UVW computed on the device: xyz float64 [n_ant][3] (local
+        XYZ, metres), steps float64 [T][17] (uvw_steps), one UVW set per interval."""
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        steps = np.ascontiguousarray(np.atleast_2d(steps), np.float64)
+        flags = np.ascontiguousarray(flags, np.int32)
+        cable = None if cable is None else np.ascontiguousarray(cable, np.float64)
+        call("bgi_set_array_pointed", self._h, xyz.shape[0], _ptr(xyz), steps.shape[0], _ptr(steps), _ptr(flags),
              _ptr(cable))
 
     def set_frequencies(self, freqs):

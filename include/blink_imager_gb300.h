@@ -213,6 +213,29 @@ BGI_API int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v);
 BGI_API int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
                     double *v_max);
 
+/* Pointed-observation UVW on the device (CAntennaPositions::CalculateUVW with metadata,
+ * src/antenna_positions.cpp:23-92; PacerGeometry::CalcUVW_NEW, precXYZ and CalcUVW,
+ * src/pacer_geometry.h).  A timestep is what the reference derives once per timestep with PAL
+ * (PrepareTimestepUVW): the precession-nutation matrix rmatpr and the sines and cosines of the
+ * local mean sidereal time, its J2000 value, the J2000 hour angle and the aberrated
+ * declination; bgi_uvw_step_from_angles fills one from the angles (host libm).  Antenna
+ * positions xyz are local XYZ in metres, double[n_ant][3].  bgi_pointed_uvw_gpu writes
+ * u, v, w float[n_steps][B] on the device (xyz and steps in device memory); the result is the
+ * reference's, bit for bit, for the same timestep numbers.  bgi_set_array_pointed does the same
+ * into a handle's resident state (one UVW set per interval) and derives u_max, v_max and
+ * delta_u/v there, as bgi_set_array. */
+typedef struct bgi_uvw_step {
+    double rmatpr[9]; /* row-major */
+    double sin_lmst, cos_lmst, sin_lmst2000, cos_lmst2000, sin_ha2000, cos_ha2000, sin_dec, cos_dec;
+} bgi_uvw_step;
+BGI_API int bgi_uvw_step_from_angles(const double *rmatpr, double ha2000, double dec_aber, double lmst,
+                                     double lmst2000, bgi_uvw_step *out);
+BGI_API int bgi_pointed_uvw_gpu(const double *xyz, int n_ant, const bgi_uvw_step *steps, int n_steps,
+                                float *u, float *v, float *w, void *stream);
+BGI_API int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_host, int n_steps,
+                                  const bgi_uvw_step *steps_host, const int *baseline_flags,
+                                  const double *cable_lengths);
+
 /* Whole path on device buffers: vis float[T][C][B][4][2] (read only: corrections are applied
  * in registers and not written back), images float[T][C][N][N][2] out.  Each image is
  * normalised by its own weight sum (the CPU path, src/pacer_imager.cpp:171-178) and

@@ -76,3 +76,13 @@ def test_sorted_workspace_size(lib):
     assert lib.bgi_gridding_sorted_gpu(C.c_void_p(16), 4, 1, 1, C.c_void_p(16), C.c_void_p(16), 1,
                                        C.c_void_p(16), C.c_void_p(16), 1.0, 1.0, 64, -1.0, 0, 1, None,
                                        C.c_void_p(16), C.c_void_p(24), 1 << 20, None) == capi.ERR_INVALID
+
+
+def test_uvw_step_from_angles(lib):
+    """The timestep helper fills the 17 numbers the pointed-UVW routines take (no GPU needed)."""
+    import os
+    import numpy as np
+    from imager_gb300 import imager
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pointed_uvw.npz"))
+    steps = imager.uvw_steps(g["rmat"], g["ha2000"], g["dec_aber"], g["lmst"], g["lmst2000"])
+    np.testing.assert_allclose(steps, g["steps"], rtol=0, atol=1e-15)
