@@ -44,17 +44,35 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def extra_flags():
+    """Extra nvcc flags from BGI_EXTRA_NVCC_FLAGS (space-separated), e.g. -DC2R_THREADS=256;
+    objects built with other flags are rebuilt."""
+    return os.environ.get("BGI_EXTRA_NVCC_FLAGS", "").split()
+
+
+def _flags_changed() -> bool:
+    stamp = os.path.join(BUILD_DIR, "flags.txt")
+    want = " ".join(NVCC_FLAGS + extra_flags())
+    have = open(stamp).read() if os.path.exists(stamp) else None
+    if have != want:
+        with open(stamp, "w") as f:
+            f.write(want)
+        return True
+    return False
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(BUILD_DIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "blink_imager_gb300.h"))
     objs, jobs = [], []
+    rebuild = _flags_changed()
     for src in sources():
         obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
-        if _stale(obj, [src] + headers) or ptxas_info:
-            cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        if rebuild or _stale(obj, [src] + headers) or ptxas_info:
+            cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra_flags(), "-c", src, "-o", obj]
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
@@ -69,7 +87,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
                 sys.stderr.write(r.stdout + r.stderr)
             if r.returncode:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
-    if _stale(LIB_PATH, objs):
+    if jobs or _stale(LIB_PATH, objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", LIB_PATH, *objs, "-cudart", "static"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:

@@ -8,7 +8,7 @@
 // exchange data through shared memory.  The first pass reads x[t + m*P] and the last pass
 // writes x[t + m*P'] -- consecutive threads touch consecutive elements -- so both HBM-facing
 // passes are coalesced and no separate transpose kernel exists.  Twiddles exp(+2*pi*i*k/N)
-// come from sincospif into shared memory once per block.
+// are compile-time tables in device memory (below).
 //
 //   row pass:    grids -> images rows; in the fused path it also re-zeroes the grid scratch
 //                it has read, so the next wave's gridding finds a clean grid.
@@ -446,13 +446,18 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ha
 }
 
 // Complex-to-real row pass shape: transforms of length M = N/2.
+#ifndef C2R_THREADS
+#define C2R_THREADS 128
+#endif
 template <int N>
 struct C2RShape {
     static constexpr int M = N / 2;
     static constexpr int R = Shape<M>::R;
     static constexpr int P = M / R;
     static constexpr bool WARP = P <= 32;
-    static constexpr int ROWS = WARP ? ((256 / P) < N ? (256 / P) : N) : 256 / P;
+    // threads per block: 128 gives more independent blocks (and bulk copies) in flight per SM
+    static constexpr int THREADS = P <= 32 ? C2R_THREADS : 256;
+    static constexpr int ROWS = WARP ? ((THREADS / P) < N ? (THREADS / P) : N) : (THREADS / P > 0 ? THREADS / P : 1);
     static constexpr int LEN = FftCfg<M, R>::LEN;
     static constexpr int BUF = ((LEN > M + 1 ? LEN : M + 1) + 1) & ~1;
 };
