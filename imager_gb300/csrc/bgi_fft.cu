@@ -325,11 +325,14 @@ struct Shape {
 };
 
 // Column-pass shape: COLS columns per block (a tile pair), P threads per column, block barriers.
+#ifndef COL_THREADS
+#define COL_THREADS 256
+#endif
 template <int N>
 struct ColShape {
     static constexpr int R = Shape<N>::R;
     static constexpr int P = N / R;
-    static constexpr int COLS = (256 / P) < 4 ? 4 : ((256 / P) > N ? N : (256 / P));
+    static constexpr int COLS = (COL_THREADS / P) < 4 ? 4 : ((COL_THREADS / P) > N ? N : (COL_THREADS / P));
     static constexpr int MOD = COLS >= 16 ? 1 : 16 / COLS;  // column stride modulo 16 (banks)
     static constexpr int LEN = FftCfg<N, R>::LEN;
     static constexpr int STRIDE = LEN + ((MOD - LEN % 16) + 16) % 16;

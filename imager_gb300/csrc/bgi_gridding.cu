@@ -18,11 +18,18 @@
 namespace bgi {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kCPT = 4;  // images per thread
+#ifndef GRID_THREADS
+#define GRID_THREADS 128
+#endif
+#ifndef GRID_CPT
+#define GRID_CPT 4
+#endif
+constexpr int kThreads = GRID_THREADS;
+constexpr int kCPT = GRID_CPT;  // images per thread
+constexpr int kMinBlocks = 768 / GRID_THREADS;  // resident blocks per SM the registers must allow
 
 template <int POL, bool COUNTERS, bool HALF, int FMT>
-__global__ void __launch_bounds__(kThreads, 3) grid_kernel(const GridParams p) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridParams p) {
     __shared__ ChannelConst s_cc[kCPT];
     __shared__ unsigned int s_count[kCPT][kThreads / 32];  // per-warp weight counts
     const int img_first = p.img_begin + blockIdx.y * kCPT;
