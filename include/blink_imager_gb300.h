@@ -6,7 +6,7 @@
  * (src/gpu/pacer_imager_hip.cpp:36-146).  Two layers:
  *
  *  1. Free functions with the reference's argument meaning, on device pointers, one per
- *     reference GPU entry point (src/gpu/*.h).  A caller that already holds device buffers
+ *     reference GPU entry point (the headers in src/gpu).  A caller that already holds device buffers
  *     (the CPacerImagerHip shape) swaps the call and nothing else.
  *  2. An imager handle that keeps the array state (UVW, flags, cable lengths, frequencies)
  *     resident on the device and images whole blocks in one call, with the corrections fused
