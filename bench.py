@@ -306,22 +306,43 @@ def serving_measure(args):
             stored.append((d.cpu().pin_memory(), sc.cpu().pin_memory()))
         bufs = [collections.deque(torch.empty((1, o.n_channels, o.n_pixels, o.n_pixels), dtype=torch.complex64,
                                               pin_memory=True) for _ in range(K)) for o in arrays]
-        busy = collections.deque()  # (ticket, array index, buffer), in submission order
+        busy = collections.deque()  # (ticket, array index, buffer, submit time), in submission order
+        lat = [[] for _ in arrays]   # client-side submit-to-collected ms per array
+
+        def collect():
+            t, kk, b, ts = busy.popleft()
+            sv.wait(t)
+            lat[kk].append((time.perf_counter() - ts) * 1000.0)
+            bufs[kk].append(b)
+
+        def collect_finished():  # without blocking: the oldest requests that are done
+            while busy:
+                t, kk, b, ts = busy[0]
+                if sv.poll(t) is None:
+                    return
+                busy.popleft()
+                lat[kk].append((time.perf_counter() - ts) * 1000.0)
+                bufs[kk].append(b)
 
         def submit(k):
             while not bufs[k]:  # reuse a buffer only after its request is collected
-                t, kk, b = busy.popleft()
-                sv.wait(t)
-                bufs[kk].append(b)
+                collect()
             b = bufs[k].popleft()
+            ts = time.perf_counter()
             t = sv.submit(ids[k], data=stored[k][0], scales=stored[k][1], fmt="s16", out=b)
-            busy.append((t, k, b))
+            busy.append((t, k, b, ts))
 
         def drain():
             while busy:
-                t, kk, b = busy.popleft()
-                sv.wait(t)
-                bufs[kk].append(b)
+                collect()
+
+        def per_array():
+            out = {f"{o.n_pixels}px_{o.n_ant}ant": {"requests": len(x), "p50_ms": float(np.percentile(x, 50)),
+                                                    "max_ms": float(np.max(x))}
+                   for o, x in zip(arrays, lat) if x}
+            for x in lat:
+                x.clear()
+            return out
 
         for k in range(len(arrays)):  # warm every slot's handle for every array
             for _ in range(args.serve_slots):
@@ -331,7 +352,7 @@ def serving_measure(args):
         errs = []
         for k, o in enumerate(arrays):
             submit(k)
-            t, kk, b = busy.pop()
+            t, kk, b, _ = busy.pop()
             out = sv.wait(t)[0, 0].numpy().astype(np.complex128)
             bufs[kk].append(b)
             corr = np.ascontiguousarray(o.vis_f32()[:, :1])
@@ -344,19 +365,22 @@ def serving_measure(args):
             errs.append(float(np.linalg.norm(out - ref) / np.linalg.norm(ref)))
         res["errors_vs_fp64_rel_l2"] = max(errs)
         # phase 1: Poisson arrivals
+        per_array()
         sv.reset_stats()
         t0 = time.perf_counter()
         arrival = 0.0
         for _ in range(args.serve_requests):
             arrival += rng.exponential(args.serve_interarrival_ms / 1000.0)
             while time.perf_counter() - t0 < arrival:
+                collect_finished()
                 time.sleep(0.0002)
             submit(int(rng.integers(len(arrays))))
         drain()
         st = sv.stats()
         res["poisson"] = {"mean_interarrival_ms": args.serve_interarrival_ms, "requests": st["completed"],
                           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
-                          "images_per_s": st["images_per_s"], "failed": st["failed"]}
+                          "images_per_s": st["images_per_s"], "failed": st["failed"],
+                          "client_latency_by_array": per_array()}
         # phase 2: closed loop, K outstanding per array
         sv.reset_stats()
         for _ in range(args.serve_requests * 3):
@@ -365,7 +389,8 @@ def serving_measure(args):
         st = sv.stats()
         res["saturated"] = {"outstanding_per_array": K, "requests": st["completed"], "p50_ms": st["p50_ms"],
                             "p99_ms": st["p99_ms"], "images_per_s": st["images_per_s"],
-                            "admission_waits": st["admission_waits"], "failed": st["failed"]}
+                            "admission_waits": st["admission_waits"], "failed": st["failed"],
+                            "client_latency_by_array": per_array()}
     return res
 
 

@@ -460,3 +460,31 @@ def test_schedule_and_autotune(im):
     assert wave in (0, 4, 8, 12) and 1 <= lanes <= 4 and ms > 0
     assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6
     h.close()
+
+
+@pytest.mark.parametrize("full_plane", [False, True])
+def test_image_largest_side(im, full_plane):
+    """The largest image side (4096), half and full plane, against the FP64 oracle."""
+    n = 4096
+    obs = synth.small(seed=121, n_ant=40, n_intervals=1, n_channels=2, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, _, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n, n_uvw_sets=1)
+    h = _imager_for(im, obs, n, "XX", full_plane=full_plane)
+    assert h.half_plane == (not full_plane)
+    out = h.image(dev(vis)).cpu().numpy()
+    for j in range(2):
+        assert rel_l2(out[0, j], ref[0, j]) < IMAGE_TOL, j
+    h.close()
+
+
+def test_single_image_block(im):
+    """One interval of one channel: a one-image wave on one lane."""
+    obs = synth.small(seed=122, n_ant=24, n_intervals=1, n_channels=1, n_pixels=64)
+    vis = obs.vis_f32()
+    _, _, _, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, 64, n_uvw_sets=1)
+    h = _imager_for(im, obs, 64, "XX")
+    out = h.image(dev(vis)).cpu().numpy()
+    assert out.shape == (1, 1, 64, 64) and rel_l2(out[0, 0], ref[0, 0]) < IMAGE_TOL
+    host = h.image_host(np.ascontiguousarray(vis))
+    assert rel_l2(host, out) < 1e-6
+    h.close()
