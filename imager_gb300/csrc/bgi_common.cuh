@@ -23,12 +23,14 @@ int check_cuda(cudaError_t e, const char *what);
 int check_launch(const char *what);
 
 // Per-channel constants for gridding.
-struct ChannelConst {
-    double wavelength;  // VEL_LIGHT / nu, as src/gpu/gridding_gpu.cpp:102
+struct alignas(16) ChannelConst {
+    // the fields every visibility reads first (one 16-byte load)
     float su, sv;       // nu / (VEL_LIGHT * delta_u), ... rounded to float (fast cell filter)
-    float inv_wl;       // 1 / wavelength rounded to float (fast min_uv filter)
     float f_hi, f_lo;   // nu / VEL_LIGHT as an unevaluated float sum (turns of phase per metre)
+    // the fields of the rare paths
+    float inv_wl;       // 1 / wavelength rounded to float (fast min_uv filter)
     float pad;
+    double wavelength;  // VEL_LIGHT / nu, as src/gpu/gridding_gpu.cpp:102
 };
 
 __device__ __forceinline__ ChannelConst make_channel_const(double nu, double du, double dv) {
@@ -88,13 +90,13 @@ __device__ __forceinline__ bool round_is_certain(float x) {
 
 // Returns false when the visibility is cut by min_uv (calculate_pos would return -1);
 // otherwise the rounded pixel coordinates (exact integers) in *ui, *vi.
-__device__ __forceinline__ bool uv_pixels(float u, float v, const ChannelConst &cc, double du,
-                                          double dv, double min_uv, bool min_uv_active, int *ui,
+__device__ __forceinline__ bool uv_pixels(float u, float v, float su, float sv, const ChannelConst *ccp,
+                                          double du, double dv, double min_uv, bool min_uv_active, int *ui,
                                           int *vi) {
     bool need_exact = false;
     if (min_uv_active) {
         // d32 and (float)min_uv each lie within 2^-22 (relative) of their exact values
-        float d32 = sqrtf(u * u + v * v) * cc.inv_wl;
+        float d32 = sqrtf(u * u + v * v) * ccp->inv_wl;
         float md = (float)min_uv;
         float tol = (fabsf(d32) + fabsf(md)) * 9.5367431640625e-7f + 1e-30f;  // 2^-20
         if (!(fabsf(d32 - md) > tol)) {
@@ -103,14 +105,14 @@ __device__ __forceinline__ bool uv_pixels(float u, float v, const ChannelConst &
             return false;
         }
     }
-    float xu = u * cc.su, xv = v * cc.sv;
+    float xu = u * su, xv = v * sv;
     if (!need_exact && round_is_certain(xu) && round_is_certain(xv)) {
         *ui = (int)roundf(xu);
         *vi = (int)roundf(xv);
         return true;
     }
     double up, vp;
-    if (!uv_pixels_exact(u, v, cc.wavelength, du, dv, min_uv, &up, &vp)) return false;
+    if (!uv_pixels_exact(u, v, ccp->wavelength, du, dv, min_uv, &up, &vp)) return false;
     if (!(fabs(up) < 1073741824.0) || !(fabs(vp) < 1073741824.0)) return false;
     *ui = (int)up;
     *vi = (int)vp;

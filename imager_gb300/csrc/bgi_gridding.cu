@@ -96,16 +96,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
         if (in_range && flag <= 0) {
             int chj = ch_first + j;
             if (chj >= p.n_channels) chj %= p.n_channels;
-            const ChannelConst cc = p.chan_consts ? p.chan_consts[chj] : s_cc[j];
+            const ChannelConst *ccp = p.chan_consts ? p.chan_consts + chj : &s_cc[j];
+            const float4 hot = p.chan_consts ? __ldg(reinterpret_cast<const float4 *>(ccp))
+                                             : make_float4(s_cc[j].su, s_cc[j].sv, s_cc[j].f_hi, s_cc[j].f_lo);
             float2 z = combine_pols<POL>(pa[j], pb[j]);
             if (corr) {
                 float d_hi, d_lo;
                 delay_df(ww[j], dl.x, dl.y, d_hi, d_lo);
-                z = rotate(z, phasor_df(d_hi, d_lo, cc.f_hi, cc.f_lo));
+                z = rotate(z, phasor_df(d_hi, d_lo, hot.z, hot.w));
             }
             int ui, vi;
             const bool gridded = !isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
-                                 uv_pixels(uu[j], vv[j], cc, p.du, p.dv, p.min_uv, min_uv_active, &ui, &vi);
+                                 uv_pixels(uu[j], vv[j], hot.x, hot.y, ccp, p.du, p.dv, p.min_uv, min_uv_active, &ui, &vi);
             if (HALF && gridded) {
                 // half-plane grid: keep each of the two points whose u index is <= N/2 (the
                 // caller guarantees |u|,|v| pixels < N, so both cells exist and are each

@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
         }
         int ui, vi;
         if (!isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
-            uv_pixels(p.u[set + b], p.v[set + b], s_cc, p.du, p.dv, p.min_uv, p.min_uv >= 0.0, &ui, &vi)) {
+            uv_pixels(p.u[set + b], p.v[set + b], s_cc.su, s_cc.sv, &s_cc, p.du, p.dv, p.min_uv, p.min_uv >= 0.0, &ui,
+                      &vi)) {
             const long long pos = cell_pos(ui, vi, +1, n), pos2 = cell_pos(ui, vi, -1, n);
             unsigned *cnt = w.cnt + (size_t)local * n * n;
             if (pos >= 0) {
