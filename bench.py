@@ -633,8 +633,10 @@ def run_ours(args, rank, world, local_rank):
     if half:
         hw = N * (N // 2 + 1) * 8  # half-plane grid of one image
         alg = {"gridding": vis_bytes + hw, "fft_pass1": 2 * hw, "fft_pass2": hw + 8 * N * N}
+        kernel_names = {"gridding": "grid_kernel", "fft_pass1": "fft_cols_half_kernel", "fft_pass2": "c2r_rows_kernel"}
     else:
         alg = {"gridding": vis_bytes + 8 * N * N, "fft_pass1": 16 * N * N, "fft_pass2": 16 * N * N}
+        kernel_names = {"gridding": "grid_kernel", "fft_pass1": "fft_rows_kernel", "fft_pass2": "fft_cols_kernel"}
     stage_info = {}
     for k, (tot_ms, launches) in stages.items():
         if launches:
@@ -663,7 +665,8 @@ def run_ours(args, rank, world, local_rank):
                  "compulsory_frac": compulsory / step_s / 1e9 / hbm_peak,
                  "all_passes_bytes_per_step": passes, "all_passes_gbs": passes / step_s / 1e9,
                  "note": "lanes run concurrently, so per-launch stage times overlap; these use the step time"}
-    roof = {"kernel": dom, "bound": "hbm", "achieved": stage_info[dom]["achieved_gbs"], "peak": hbm_peak,
+    roof = {"kernel": kernel_names[dom], "stage": dom, "bound": "hbm", "achieved": stage_info[dom]["achieved_gbs"],
+            "peak": hbm_peak,
             "unit": "GB/s", "frac": stage_info[dom]["achieved_gbs"] / hbm_peak,
             "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
             "traffic": traffic,

@@ -108,12 +108,15 @@ struct bgi_imager {
     long long n_baselines = 0;
     double u_max = 0, v_max = 0, delta_u = 0, delta_v = 0;
     double freq_max = 0;  // highest channel frequency (Hz)
+    // a baseline flag below zero: gridded (flags <= 0 are) but outside u_max / v_max (flag 0
+    // only), so the largest pixel coordinate is unknown and the half plane is not used
+    bool negative_flags = false;
 
     // The half-plane path needs every gridded point's mirror cell: |u|,|v| pixels < N.  The
     // largest pixel coordinate is u_max * nu_max / (c * delta_u); one pixel of margin covers
     // the rounding of the FP64 recipe.
     bool half_plane() const {
-        if (cfg.full_plane || half_plane_width(cfg.n_pixels) == 0 || freq_max <= 0) return false;
+        if (cfg.full_plane || half_plane_width(cfg.n_pixels) == 0 || freq_max <= 0 || negative_flags) return false;
         const double up = u_max * freq_max / (kVelLight * delta_u);
         const double vp = v_max * freq_max / (kVelLight * delta_v);
         return up < cfg.n_pixels - 1 && vp < cfg.n_pixels - 1;
@@ -423,6 +426,8 @@ int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, con
                 um = std::max(um, (double)std::fabs(u[s * nb + b]));
                 vm = std::max(vm, (double)std::fabs(v[s * nb + b]));
             }
+    bool negative = false;
+    for (long long b = 0; b < nb; ++b) negative = negative || baseline_flags[b] < 0;
     std::vector<float2> dl(nb, make_float2(0.f, 0.f));
     if (cable_lengths) {
         for (int a1 = 0; a1 < n_ant; ++a1)
@@ -447,6 +452,7 @@ int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, con
     im->n_ant = n_ant;
     im->n_baselines = nb;
     im->n_uvw_sets = n_uvw_sets;
+    im->negative_flags = negative;
     im->u_max = um;
     im->v_max = vm;
     // src/pacer_imager.cpp:497-499: float oversampling factor promoted to double

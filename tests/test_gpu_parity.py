@@ -410,6 +410,27 @@ def test_half_plane_falls_back_when_pixels_reach_the_side(im):
     h.close()
 
 
+def test_negative_flag_keeps_blocks_off_the_half_plane(im):
+    """A baseline flag below zero is gridded (the GPU gridder's flags <= 0, as
+    src/gpu/gridding_gpu.cpp:101) but u_max / v_max cover flag 0 only
+    (src/pacer_imager.cpp:213-221), so its pixel may reach the side: the handle images such an
+    array on the full plane, whose cell indices are checked, and counts the baseline."""
+    obs = synth.small(seed=49, n_ant=24, n_intervals=1, n_channels=2, n_pixels=64)
+    h = _imager_for(im, obs, 64)
+    assert h.half_plane
+    h.image(dev(obs.vis_f32()))
+    base = h.weight_sums(2)
+    flags = obs.flags.copy()
+    b = 5 * 6 // 2 + 3  # baseline (5, 3): antenna 3 is flagged
+    assert flags[b] == 1
+    flags[b] = -1
+    h.set_array(obs.u, obs.v, obs.w, flags, obs.cable)
+    assert not h.half_plane
+    h.image(dev(obs.vis_f32()))
+    assert np.array_equal(h.weight_sums(2), base + 2)
+    h.close()
+
+
 @pytest.mark.parametrize("full_plane", [False, True])
 @pytest.mark.parametrize("pol", ["XX", "I"])
 def test_image_real_output(im, full_plane, pol):
