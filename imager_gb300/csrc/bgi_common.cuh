@@ -80,12 +80,18 @@ __device__ __forceinline__ bool uv_pixels_exact(float u, float v, double wavelen
 }
 
 // True when x (FP32 estimate of a value whose exact counterpart lies within x*2^-21) rounds
-// to the same integer as the exact value.
-__device__ __forceinline__ bool round_is_certain(float x) {
-    float ax = fabsf(x);
-    float d = fabsf(ax - floorf(ax) - 0.5f);
-    float tol = ax * 4.76837158e-7f + 1e-30f;  // 2^-21
-    return d > tol && ax < 536870912.0f;       // and |x| < 2^29
+// to the same integer as the exact value; that integer is then *r.
+//
+// d = 0.5 - |x - rint(x)| is x's distance to the nearest half-integer: x - rint(x) is exact,
+// and so is 0.5 - |.| wherever d is small enough to matter (Sterbenz), so the decision is the
+// one of the exact distance.  When the test passes, x is not a half-integer, so rint(x) (ties
+// to even) equals the reference's round (ties away from zero).
+__device__ __forceinline__ bool round_certain(float x, float *r) {
+    const float ri = rintf(x);
+    const float d = 0.5f - fabsf(x - ri);
+    const float tol = fabsf(x) * 4.76837158e-7f + 1e-30f;  // 2^-21
+    *r = ri;
+    return d > tol && fabsf(x) < 536870912.0f;  // and |x| < 2^29
 }
 
 // Returns false when the visibility is cut by min_uv (calculate_pos would return -1);
@@ -105,10 +111,12 @@ __device__ __forceinline__ bool uv_pixels(float u, float v, float su, float sv, 
             return false;
         }
     }
-    float xu = u * su, xv = v * sv;
-    if (!need_exact && round_is_certain(xu) && round_is_certain(xv)) {
-        *ui = (int)roundf(xu);
-        *vi = (int)roundf(xv);
+    const float xu = u * su, xv = v * sv;
+    float ru, rv;
+    const bool cu = round_certain(xu, &ru), cv = round_certain(xv, &rv);
+    if (!need_exact && cu && cv) {
+        *ui = (int)ru;
+        *vi = (int)rv;
         return true;
     }
     double up, vp;

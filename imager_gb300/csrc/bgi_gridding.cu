@@ -28,8 +28,12 @@ constexpr int kThreads = GRID_THREADS;
 constexpr int kCPT = GRID_CPT;  // images per thread
 constexpr int kMinBlocks = 768 / GRID_THREADS;  // resident blocks per SM the registers must allow
 
-template <int POL, bool COUNTERS, bool HALF, int FMT>
+// ONE_SET: the kCPT images of every block share one UVW set (one set, or blocks that start at
+// multiples of kCPT with kCPT dividing the channel count), so a thread loads u, v, w and forms
+// the delay once for all of them.
+template <int POL, bool COUNTERS, bool HALF, int FMT, bool ONE_SET>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridParams p) {
+    constexpr int NUV = ONE_SET ? 1 : kCPT;  // u, v, w registers
     __shared__ ChannelConst s_cc[kCPT];
     __shared__ unsigned int s_count[kCPT][kThreads / 32];  // per-warp weight counts
     const int img_first = p.img_begin + blockIdx.y * kCPT;
@@ -44,7 +48,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
     // ---- issue every load of this thread ----------------------------------------------------
     int flag = 1;
     float2 pa[kCPT], pb[kCPT];
-    float uu[kCPT], vv[kCPT], ww[kCPT];
+    float uu[NUV], vv[NUV], ww[NUV];
     float2 dl = make_float2(0.f, 0.f);
     if (in_range) {
         flag = p.flags[b];
@@ -53,7 +57,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
 #pragma unroll
         for (int j = 0; j < kCPT; ++j) {
             pa[j] = pb[j] = make_float2(0.f, 0.f);
-            uu[j] = vv[j] = ww[j] = 0.f;
+            if (j < NUV) uu[j] = vv[j] = ww[j] = 0.f;
             if (j < n_here) {
                 const size_t img = (size_t)img_first + j;
                 const size_t off = (p.n_uvw_sets > 1 ? (size_t)t * nb : 0) + b;
@@ -62,9 +66,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
                 else
                     load_pols_planar<POL, FMT>(reinterpret_cast<const uint32_t *>(p.vis), p.vis_scales, img, nb,
                                                p.vis_blocks, b, pa[j], pb[j]);
-                uu[j] = p.u[off];
-                vv[j] = p.v[off];
-                if (p.apply_geom) ww[j] = p.w[off];
+                if (j < NUV) {
+                    uu[j] = p.u[off];
+                    vv[j] = p.v[off];
+                    if (p.apply_geom) ww[j] = p.w[off];
+                }
             }
             if (++ch == p.n_channels) {
                 ch = 0;
@@ -87,6 +93,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
     const long long npix = (long long)n * n;
     const bool corr = p.apply_geom || p.apply_cable;
     const bool min_uv_active = p.min_uv >= 0.0;
+    float d1_hi = 0.f, d1_lo = 0.f;  // the delay, once per thread when the images share a set
+    if (ONE_SET && corr) delay_df(ww[0], dl.x, dl.y, d1_hi, d1_lo);
 #pragma unroll
     for (int j = 0; j < kCPT; ++j) {
         if (j >= n_here) break;  // uniform across the block
@@ -100,22 +108,24 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
             const float4 hot = p.chan_consts ? __ldg(reinterpret_cast<const float4 *>(ccp))
                                              : make_float4(s_cc[j].su, s_cc[j].sv, s_cc[j].f_hi, s_cc[j].f_lo);
             float2 z = combine_pols<POL>(pa[j], pb[j]);
+            constexpr int J = ONE_SET ? 0 : 1;  // u, v, w index: 0 or j
             if (corr) {
-                float d_hi, d_lo;
-                delay_df(ww[j], dl.x, dl.y, d_hi, d_lo);
+                float d_hi = d1_hi, d_lo = d1_lo;
+                if (!ONE_SET) delay_df(ww[J * j], dl.x, dl.y, d_hi, d_lo);
                 z = rotate(z, phasor_df(d_hi, d_lo, hot.z, hot.w));
             }
             int ui, vi;
             const bool gridded = !isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
-                                 uv_pixels(uu[j], vv[j], hot.x, hot.y, ccp, p.du, p.dv, p.min_uv, min_uv_active, &ui, &vi);
+                                 uv_pixels(uu[J * j], vv[J * j], hot.x, hot.y, ccp, p.du, p.dv, p.min_uv,
+                                           min_uv_active, &ui, &vi);
             if (HALF && gridded) {
                 // half-plane grid: keep each of the two points whose u index is <= N/2 (the
-                // caller guarantees |u|,|v| pixels < N, so both cells exist and are each
-                // other's mirror)
+                // caller guarantees |u|,|v| pixels < N, so both cells exist, are each other's
+                // mirror, and wrap_index is i + N for negative i)
                 const int w = p.half_width;
                 float2 *grid = p.grids + (size_t)local * n * w;
-                const int u1 = wrap_index(ui, n), v1 = wrap_index(vi, n);
-                const int u2 = wrap_index(-ui, n), v2 = wrap_index(-vi, n);
+                const int u1 = ui + (n & (ui >> 31)), v1 = vi + (n & (vi >> 31));
+                const int u2 = -ui + (n & (-ui >> 31)), v2 = -vi + (n & (-vi >> 31));
                 if (u1 <= n / 2) atomicAdd(grid + (size_t)v1 * w + u1, z);
                 if (u2 <= n / 2) atomicAdd(grid + (size_t)v2 * w + u2, make_float2(z.x, -z.y));
                 counted += 2;
@@ -157,10 +167,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
     }
 }
 
+// whether every block's kCPT images share one UVW set (grid_kernel's ONE_SET)
+bool one_set(const GridParams &q) {
+    return q.n_uvw_sets == 1 || (q.n_channels % kCPT == 0 && q.img_begin % kCPT == 0);
+}
+
 template <int POL, int FMT>
 void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
-    if (q.half_width > 0) grid_kernel<POL, false, true, FMT><<<grid, kThreads, 0, s>>>(q);
-    else grid_kernel<POL, false, false, FMT><<<grid, kThreads, 0, s>>>(q);
+    const bool one = one_set(q);
+    if (q.half_width > 0) {
+        if (one) grid_kernel<POL, false, true, FMT, true><<<grid, kThreads, 0, s>>>(q);
+        else grid_kernel<POL, false, true, FMT, false><<<grid, kThreads, 0, s>>>(q);
+    } else {
+        if (one) grid_kernel<POL, false, false, FMT, true><<<grid, kThreads, 0, s>>>(q);
+        else grid_kernel<POL, false, false, FMT, false><<<grid, kThreads, 0, s>>>(q);
+    }
 }
 
 template <int POL>
@@ -170,7 +191,7 @@ void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
         case BGI_VIS_BF16: launch_fmt<POL, BGI_VIS_BF16>(grid, q, s); break;
         case BGI_VIS_FP16: launch_fmt<POL, BGI_VIS_FP16>(grid, q, s); break;
         default:
-            if (q.counter_mode >= 0) grid_kernel<POL, true, false, BGI_VIS_C64><<<grid, kThreads, 0, s>>>(q);
+            if (q.counter_mode >= 0) grid_kernel<POL, true, false, BGI_VIS_C64, false><<<grid, kThreads, 0, s>>>(q);
             else launch_fmt<POL, BGI_VIS_C64>(grid, q, s);
     }
 }
