@@ -267,7 +267,11 @@ constexpr double taylor_cos(double a) {
     }
     return sum;
 }
-constexpr TwEntry twiddle_exact(int idx, int n) {
+struct CplxD {
+    double x, y;
+};
+// exp(+2*pi*i*idx/n) in double
+constexpr CplxD exp_i_exact(int idx, int n) {
     const int q = n / 4, quad = (idx / q) & 3, k = idx % q;
     const bool swap = k > n / 8;
     const double a = 2.0 * kPi * (double)(swap ? q - k : k) / (double)n;
@@ -281,7 +285,11 @@ constexpr TwEntry twiddle_exact(int idx, int n) {
     if (quad == 1) { x = -s; y = c; }
     else if (quad == 2) { x = -c; y = -s; }
     else if (quad == 3) { x = s; y = -c; }
-    return TwEntry{(float)x, (float)y};
+    return CplxD{x, y};
+}
+constexpr TwEntry twiddle_exact(int idx, int n) {
+    const CplxD e = exp_i_exact(idx, n);
+    return TwEntry{(float)e.x, (float)e.y};
 }
 
 template <int N, int R>
@@ -380,8 +388,10 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
     const int col = c < CT ? x0 + c : N / 2 + x0 + (c - CT);
     float2 *in = src + img * (size_t)N * N;
     float2 *out = dst + img * (size_t)N * N;
-    float scale = 1.0f;
-    if (SHIFT_NORM) scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
+    // one FP64 reciprocal per block (its columns are one image's), read after the transform's
+    // block barriers
+    __shared__ float s_scale;
+    if (SHIFT_NORM && threadIdx.x == 0) s_scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
     const int dcol = SHIFT_NORM ? ((col + N / 2) & (N - 1)) : col;
     fft_transform<N, S::R, false, false>(
         t, smem + c * S::STRIDE, tw,
@@ -390,7 +400,7 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
             int r = i;
             if (SHIFT_NORM) {
                 r = (i + N / 2) & (N - 1);
-                v = make_float2(v.x * scale, v.y * scale);
+                v = make_float2(v.x * s_scale, v.y * s_scale);
             }
             if (REAL)
                 __stcs(reinterpret_cast<float *>(dst) + img * (size_t)N * N + (size_t)r * N + dcol, v.x);
@@ -410,15 +420,21 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ke
 // with M = N/2 and w = exp(+2*pi*i*k/N), Z[k] = X[k](1 + i w) + conj(X[M-k])(1 - i w) for
 // k < M, z = IDFT_M(Z), and the image row is x[2m] = Re z[m], x[2m+1] = Im z[m].
 
-// exp(+2*pi*i*k/N) for k < N/2 (compile-time, as the pass tables).
+// P[k] = 1 + i exp(+2*pi*i*k/N) = (1 - sin, cos) for k < N/2, in double then rounded
+// (compile-time, as the pass tables).  With it Z[k] = X[k](1 + i w) + conj(X[M-k])(1 - i w)
+// = 2 conj(b) + P[k] (a - conj(b)) for a = X[k], b = X[M-k], since 1 - i w = 2 - P.
 template <int N>
 struct alignas(16) ZTwData {
     TwEntry v[N / 2];
 };
+constexpr TwEntry one_plus_i_twiddle(int k, int n) {
+    const CplxD e = exp_i_exact(k, n);
+    return TwEntry{(float)(1.0 - e.y), (float)e.x};
+}
 template <int N>
 constexpr ZTwData<N> make_z_twiddles() {
     ZTwData<N> d{};
-    for (int k = 0; k < N / 2; ++k) d.v[k] = twiddle_exact(k, N);
+    for (int k = 0; k < N / 2; ++k) d.v[k] = one_plus_i_twiddle(k, N);
     return d;
 }
 template <int N>
@@ -490,7 +506,7 @@ constexpr unsigned c2r_wz_bytes() {
 template <int N>
 constexpr size_t c2r_smem_bytes() {
     return sizeof(float2) * (size_t)C2RShape<N>::ROWS * C2RShape<N>::BUF + c2r_row_bytes<N>() + c2r_tw_bytes<N>() +
-           c2r_wz_bytes<N>() + sizeof(uint64_t);
+           c2r_wz_bytes<N>() + sizeof(uint64_t) + sizeof(float);
 }
 
 template <int N, bool REAL>
@@ -509,10 +525,10 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     float2 *tw = zeros + ROW_BYTES / sizeof(float2);  // pass twiddles, then z twiddles
     float2 *wz = tw + TW_BYTES / sizeof(float2);
     uint64_t *bar = reinterpret_cast<uint64_t *>(wz + WZ_BYTES / sizeof(float2));
+    float *s_scale = reinterpret_cast<float *>(bar + 1);  // (float)(1/sum(w)) of the block's image
     const int slot = threadIdx.x / S::P, t = threadIdx.x % S::P;
     const size_t row0 = (size_t)blockIdx.x * S::ROWS;
     const size_t row = row0 + slot;
-    const size_t img = row / N;
     float2 *buf = smem + slot * S::BUF;
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -527,6 +543,8 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
         bulk_load(tw, twiddles<M, S::R>(), TW_BYTES, bar);
         bulk_load(wz, g_z_twiddles<N>.v, WZ_BYTES, bar);
         for (int r = 0; r < S::ROWS; ++r) bulk_load(smem + r * S::BUF, grids + (row0 + r) * W, ROW_BYTES, bar);
+        // one FP64 reciprocal per block (all its rows are one image's), while the copies fly
+        *s_scale = (float)(1.0 / (double)wsum[(row0 / N) * kWsumStride]);
     }
     if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
         mbar_wait_bounded(bar, 0);  // let copies still in flight land before the block exits
@@ -536,16 +554,15 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
         for (int r = 0; r < S::ROWS; ++r) bulk_store(grids + (row0 + r) * W, zeros, ROW_BYTES);
         bulk_commit();
     }
-    const float scale = (float)(1.0 / (double)wsum[img * kWsumStride]);
+    const float scale = *s_scale;
     float2 *dst = images + row * N;
     fft_transform<M, S::R, S::WARP, false, true>(
         t, buf, tw,
         [&](int k) {
-            const float2 a = buf[k], b = buf[M - k], w = wz[k];
-            // a * (1 + i w) + conj(b) * (1 - i w)
-            const float pr = 1.f - w.y, pi = w.x, qr = 1.f + w.y, qi = -w.x;
-            const float br = b.x, bi = -b.y;
-            return make_float2(a.x * pr - a.y * pi + br * qr - bi * qi, a.x * pi + a.y * pr + br * qi + bi * qr);
+            const float2 a = buf[k], b = buf[M - k], P = wz[k];
+            // 2 conj(b) + P (a - conj(b))
+            const float dx = a.x - b.x, dy = a.y + b.y;
+            return make_float2(fmaf(P.x, dx, fmaf(-P.y, dy, 2.f * b.x)), fmaf(P.x, dy, fmaf(P.y, dx, -2.f * b.y)));
         },
         [&](int m, float2 z) {
             // pixels x and x+1 as one 16-byte store (images are 16-byte aligned on this path)
