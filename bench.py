@@ -11,7 +11,11 @@ The timed step images the block from its stored form (--storage): by default 16-
 floating point (int16 pol planes with one FP32 scale per 128 baselines, encoded once before
 timing, as stored data), checked against the FP64 oracle of the original complex64
 visibilities; complex64 storage, bf16/fp16 storage, the deterministic gridder, the full-plane
-path and the reference's plain FP32 call sequence are timed beside it as variants.
+path and the reference's plain FP32 call sequence are timed beside it as variants.  The other
+workloads run as sections of the same line: `serving` (Poisson and closed-loop requests from
+three arrays), `batched_uneven` (four image sizes as direct calls and as one CUDA graph) and
+`precision_form` (768 channels x 20 intervals at 1024^2 in every storage format, errors
+against the FP64 oracle).
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--storage s16|c64|bf16|fp16]
 
@@ -458,6 +462,83 @@ def batched_measure(args, stream, flush):
             "errors_vs_fp64_rel_l2": {f"{o.n_pixels}": e for o, e in zip(bands, errs)}}
 
 
+def precision_measure(args, stream, flush):
+    """The precision form: 128 antennas in a 3 km disk with log-radial density, 768 channels of
+    10 kHz from 150 MHz x 20 intervals, 1024x1024 images (15,360 per step, complex64 on the
+    device: 129 GB), from complex64 records and from 16-bit storage with one FP32 scale per 128
+    baselines (256 components): s16, bf16 and fp16.  Per format: images/s over the whole block
+    and, for three sampled images, the error against the FP64 oracle (relative L2 and the
+    largest absolute error relative to the image peak)."""
+    import torch
+    from imager_gb300 import imager as IM
+    from imager_gb300 import synth
+    from oracle import oracle as O
+    obs = synth.precision_form(device="cuda")
+    T, Cn, n = obs.n_intervals, obs.n_channels, obs.n_pixels
+    vis = obs.vis_f32()  # float32 [T][C][B][4][2] on the device
+    flags = IM.APPLY_GEOMETRIC | IM.APPLY_CABLE
+    h = IM.Imager(n, 2.0, "XX", -1000.0)
+    h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+    h.set_frequencies(obs.freqs)
+    du, dv, _, _ = h.uv_cell
+    # schedule tuned on the first interval (a one-set imager with the block's uv cell)
+    t1 = IM.Imager(n, 2.0, "XX", -1000.0)
+    t1.set_array(obs.u[:1], obs.v[:1], obs.w[:1], obs.flags, obs.cable)
+    t1.set_frequencies(obs.freqs)
+    t1.set_uv_cell(du, dv)
+    d1, s1 = IM.compress_visibilities(vis[:1], "s16")
+    wave, lanes, _ = t1.autotune(d1, s1, "s16", flags=flags)
+    t1.close()
+    del d1, s1
+    h.set_schedule(wave, lanes)
+    out = torch.empty((T, Cn, n, n), dtype=torch.complex64, device="cuda")
+    samples = ((0, 0), (T // 2, Cn // 2), (T - 1, Cn - 1))
+    refs = {}
+    for t, c in samples:
+        corr = np.ascontiguousarray(vis[t:t + 1, c:c + 1].cpu().numpy())
+        O.apply_geometric(corr, np.ascontiguousarray(obs.w[t:t + 1]), obs.freqs[c:c + 1])
+        O.apply_cable(corr, obs.cable, obs.freqs[c:c + 1])
+        g, cnt, _ = O.gridding(corr, obs.u[t:t + 1], obs.v[t:t + 1], obs.flags, obs.freqs[c:c + 1], du, dv, n)
+        refs[(t, c)] = O.image_f64(g, cnt)[0, 0]
+    k = max(3, min(args.steps, 5))
+    n_images = T * Cn
+    gridded = int((obs.flags == 0).sum())
+    formats = {}
+    for fmt in ("s16", "bf16", "fp16", "c64"):
+        if fmt == "c64":
+            step = lambda: h.image(vis, flags=flags, out=out)  # noqa: E731
+        else:
+            data, scales = IM.compress_visibilities(vis, fmt)
+            step = lambda: h.image_compressed(data, scales, fmt, flags=flags, out=out)  # noqa: E731
+        ms = time_steps(step, k, stream, flush)
+        torch.cuda.synchronize()
+        errs = []
+        for t, c in samples:
+            got = out[t, c].cpu().numpy().astype(np.complex128)
+            ref = refs[(t, c)]
+            errs.append((float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                         float(np.abs(got - ref).max() / np.abs(ref).max())))
+        formats[fmt] = {"ms_per_step": ms, "images_per_s": n_images / (ms / 1000.0),
+                        "vis_per_s": n_images * gridded / (ms / 1000.0),
+                        "rel_l2_max": max(e[0] for e in errs), "max_abs_err_rel_peak": max(e[1] for e in errs),
+                        "rel_l2_per_image": [e[0] for e in errs]}
+        if fmt != "c64":
+            del data, scales
+    h.close()
+    del out, vis, obs
+    torch.cuda.empty_cache()
+    return {"workload": "128 antennas in a 3 km disk with log-radial density (8,256 baselines), 768 channels of "
+                        "10 kHz from 150 MHz x 20 intervals (1 s, Earth-rotated zenith UVW) -> 15,360 dirty images "
+                        "1024x1024 per step (complex64, 129 GB on the device), pol XX, corrections fused (delay "
+                        "phase reduced in double-float), 16-bit formats with one FP32 scale per 128 baselines",
+            "images_per_step": n_images, "steps": k,
+            "schedule": {"images_per_wave": wave or "auto", "lanes": lanes, "chosen_by": "bgi_autotune on interval 0"},
+            "sampled_images": [f"interval {t}, channel {c}" for t, c in samples],
+            "oracle": "FP64 oracle of the original complex64 visibilities",
+            "fft": "FP32 Stockham passes of our own (no tensor-core DFT stages)",
+            "formats": formats}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from imager_gb300 import capi, synth
@@ -621,6 +702,7 @@ def run_ours(args, rank, world, local_rank):
         return 0
     serving = serving_measure(args) if (args.serving and world == 1) else None
     batched = batched_measure(args, stream, flush) if (args.batched and world == 1) else None
+    precision = precision_measure(args, stream, flush) if (args.precision and world == 1) else None
 
     images_per_s = world * n_images * args.steps / (ms / 1000.0)
     hbm_peak, peak_kind = measured_peaks()
@@ -708,6 +790,7 @@ def run_ours(args, rank, world, local_rank):
         "variants": variants,
         "serving": serving,
         "batched_uneven": batched,
+        "precision_form": precision,
         "parity_sample_rel_l2": errs["rel_l2"],
         "errors_vs_fp64": {**errs, "images": [f"interval {t % T}, channel {c}" for t, c in SAMPLES],
                            "oracle": "FP64 oracle of the original complex64 visibilities"},
@@ -732,6 +815,8 @@ def main():
                     help="keep the default schedule (auto wave, two lanes) instead of bgi_autotune's")
     ap.add_argument("--no-serving", dest="serving", action="store_false", help="skip the serving measurement")
     ap.add_argument("--no-batched", dest="batched", action="store_false", help="skip the uneven-batch measurement")
+    ap.add_argument("--no-precision", dest="precision", action="store_false",
+                    help="skip the precision-form measurement (768 channels x 20 intervals at 1024^2)")
     ap.add_argument("--serve-requests", type=int, default=60)
     ap.add_argument("--serve-interarrival-ms", type=float, default=100.0)
     ap.add_argument("--serve-slots", type=int, default=4)

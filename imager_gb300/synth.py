@@ -67,8 +67,12 @@ class Observation:
     def n_uvw_sets(self) -> int:
         return self.u.shape[0]
 
-    def vis_f32(self) -> np.ndarray:
-        """float32 view [T][C][B][4][2]."""
+    def vis_f32(self):
+        """float32 view [T][C][B][4][2] (a numpy array, or a torch tensor when the block was
+        kept on the device)."""
+        if not isinstance(self.vis, np.ndarray):
+            import torch
+            return torch.view_as_real(self.vis)
         return self.vis.view(np.float32).reshape(self.vis.shape + (2,))
 
 
@@ -166,9 +170,10 @@ def _model_vis(uvw, freqs, flux, l, m, n, device, fast=False):
 
 def make_observation(seed, n_ant, enu, n_intervals, freqs, n_pixels, n_src=50, noise_sigma=1.0,
                      per_interval_uvw=True, flagged_ants=(), cadence_s=1.0, device="cpu",
-                     cable_max_m=200.0, pol="XX", fast=False, diffuse=None) -> Observation:
+                     cable_max_m=200.0, pol="XX", fast=False, diffuse=None, keep_device=False) -> Observation:
     """diffuse = (amp_jy, beta): a diffuse background whose visibilities are complex Gaussian with
-    rms amp * (1 + |uv|/10 wavelengths)^(-beta/2) (a power-law sky), the same in XX and YY."""
+    rms amp * (1 + |uv|/10 wavelengths)^(-beta/2) (a power-law sky), the same in XX and YY.
+    keep_device: the visibilities stay a complex64 torch tensor on `device`."""
     import torch
     rng = np.random.Generator(np.random.PCG64(seed))
     freqs = np.asarray(freqs, np.float64)
@@ -215,7 +220,10 @@ def make_observation(seed, n_ant, enu, n_intervals, freqs, n_pixels, n_src=50, n
     f = torch.as_tensor(freqs / VEL_LIGHT, dtype=torch.float64, device=dev)           # [C]
     phase = 2 * math.pi * (w[:, None, :] - dl[None, None, :]) * f[None, :, None]      # [T][C][B]
     vis = vis * torch.exp(-1j * phase)[..., None]
-    vis = vis.to(torch.complex64).cpu().numpy()
+    del phase, model
+    vis = vis.to(torch.complex64)
+    if not keep_device:
+        vis = vis.cpu().numpy()
     flags = np.zeros(B, np.int32)
     for b, (i, j) in enumerate(zip(a1, a2)):
         if i == j or i in flagged_ants or j in flagged_ants:
@@ -245,6 +253,17 @@ def config2(device="cpu", n_intervals=10, n_channels=64) -> Observation:
     enu = layout_uniform_disk(rng, 256, 35.0)
     freqs = config2_freqs()[:n_channels]
     return make_observation(1236, 256, enu, n_intervals, freqs, 512, device=device)
+
+
+def precision_form(device="cuda", n_intervals=20, n_channels=768, keep_device=True) -> Observation:
+    """128 antennas in a 3 km disk with log-radial density, 768 channels of 10 kHz from 150 MHz x
+    20 intervals of 1 s, 1024x1024 images (15,360 per block; seed 1237).  The visibilities
+    (4 GB) stay on the device unless keep_device is False."""
+    rng = np.random.Generator(np.random.PCG64(1237))
+    enu = layout_log_radial(rng, 128, 1500.0)
+    freqs = 150e6 + 10e3 * np.arange(n_channels)
+    return make_observation(1237, 128, enu, n_intervals, freqs, 1024, device=device, fast=True,
+                            keep_device=keep_device)
 
 
 def small(seed=7, n_ant=24, n_intervals=2, n_channels=3, n_pixels=64, radius=35.0,
