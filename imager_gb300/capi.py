@@ -57,6 +57,11 @@ class UvwStep(C.Structure):
                 ("cos_ha2000", C.c_double), ("sin_dec", C.c_double), ("cos_dec", C.c_double)]
 
 
+class ImageWcs(C.Structure):
+    _fields_ = [("ra_deg", C.c_double), ("dec_deg", C.c_double), ("pixscale_ra_deg", C.c_double),
+                ("pixscale_dec_deg", C.c_double)]
+
+
 _vp, _i, _i64, _d, _f, _u = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_float, C.c_uint
 _SIGNATURES = {
     "bgi_last_error": (C.c_char_p, []),
@@ -111,6 +116,9 @@ _SIGNATURES = {
     "bgi_autotune": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp, C.POINTER(C.c_double)]),
     "bgi_device_fault": (_i, [_i, C.POINTER(C.c_uint), _i]),
     "bgi_selftest_wait_timeout": (_i, [_i, _vp]),
+    "bgi_get_image_wcs": (_i, [_vp, _d, _d, C.POINTER(ImageWcs)]),
+    "bgi_write_fits": (_i, [C.c_char_p, _vp, _i, _i, _i, C.POINTER(ImageWcs), _d]),
+    "bgi_write_fits_block": (_i, [C.c_char_p, C.c_char_p, _vp, _i, _i, _i, _i, _i, C.POINTER(ImageWcs), _vp]),
     "bgi_set_stage_timing": (_i, [_vp, _i]),
     "bgi_get_stage_times": (_i, [_vp, C.POINTER(_d), C.POINTER(_i64)]),
 }

@@ -570,6 +570,20 @@ int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v) {
     return BGI_OK;
 }
 
+int bgi_get_image_wcs(const bgi_imager *im, double ra_deg, double dec_deg, bgi_image_wcs *out) {
+    if (!im || !out) return set_error(BGI_ERR_INVALID, "get_image_wcs: bad arguments");
+    if (im->n_ant == 0 || !(im->u_max > 0) || !(im->v_max > 0))
+        return set_error(BGI_ERR_STATE, "get_image_wcs: no array state with u_max, v_max > 0");
+    // src/gpu/pacer_imager_hip.cpp:113-115: (1/(osf*u_max))*(180/pi), u_max in metres
+    const double osf = (double)im->cfg.oversampling_factor;
+    const double rad2deg = 180.00 / 3.14159265358979323846;
+    out->ra_deg = ra_deg;
+    out->dec_deg = dec_deg;
+    out->pixscale_ra_deg = (1.00 / (osf * im->u_max)) * rad2deg;
+    out->pixscale_dec_deg = (1.00 / (osf * im->v_max)) * rad2deg;
+    return BGI_OK;
+}
+
 int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
                     double *v_max) {
     if (!im) return set_error(BGI_ERR_INVALID, "get_uv_cell: null handle");

@@ -348,6 +348,14 @@ class Imager:
         """Grid by sort and ordered per-cell sums (full plane): the same image bits on every run."""
         call("bgi_set_deterministic", self._h, int(bool(enable)))
 
+    def image_wcs(self, ra_deg: float = 0.0, dec_deg: float = -26.703319) -> dict:
+        """Phase centre and pixel scales (degrees) of this handle's images, as the reference
+        attaches them to its Images (bgi_get_image_wcs)."""
+        w = capi.ImageWcs()
+        call("bgi_get_image_wcs", self._h, float(ra_deg), float(dec_deg), C.byref(w))
+        return {"ra_deg": w.ra_deg, "dec_deg": w.dec_deg, "pixscale_ra_deg": w.pixscale_ra_deg,
+                "pixscale_dec_deg": w.pixscale_dec_deg}
+
     def set_stage_timing(self, enable: bool = True):
         call("bgi_set_stage_timing", self._h, int(bool(enable)))
 
@@ -409,3 +417,43 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------------------------------
+# FITS output (bgi_write_fits, bgi_write_fits_block)
+# ------------------------------------------------------------------------------------------
+def _wcs_struct(wcs):
+    if wcs is None:
+        return None
+    return C.byref(capi.ImageWcs(wcs["ra_deg"], wcs["dec_deg"], wcs["pixscale_ra_deg"], wcs["pixscale_dec_deg"]))
+
+
+def _host_image_block(images):
+    """(float32 host array, pixel stride): real images as they are, complex ones by real part."""
+    if isinstance(images, torch.Tensor):
+        images = images.detach().cpu().numpy()
+    a = np.ascontiguousarray(images)
+    if a.dtype == np.complex64:
+        return a.view(np.float32), 2
+    if a.dtype != np.float32:
+        raise TypeError("images must be float32 (real) or complex64")
+    return a, 1
+
+
+def write_fits(path, image, wcs=None, freq_hz: float = 0.0):
+    """One image [ny][nx] (float32, or complex64: its real part) to a FITS file; wcs from
+    Imager.image_wcs."""
+    if len(image.shape) != 2:
+        raise ValueError("one image [ny][nx]")
+    ny, nx = int(image.shape[0]), int(image.shape[1])
+    a, stride = _host_image_block(image)
+    call("bgi_write_fits", str(path).encode(), _ptr(a), int(nx), int(ny), stride, _wcs_struct(wcs), float(freq_hz))
+
+
+def write_fits_block(directory, prefix, images, wcs=None, freqs_hz=None):
+    """Every image of a block [T][C][ny][nx] to <directory>/<prefix>_t<TTTT>_c<CCCC>.fits."""
+    a, stride = _host_image_block(images)
+    T, Cn, ny, nx = (int(x) for x in images.shape)
+    f = None if freqs_hz is None else np.ascontiguousarray(freqs_hz, np.float64)
+    call("bgi_write_fits_block", str(directory).encode(), str(prefix).encode(), _ptr(a), T, Cn, nx, ny, stride,
+         _wcs_struct(wcs), _ptr(f) if f is not None else None)

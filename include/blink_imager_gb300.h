@@ -282,6 +282,34 @@ BGI_API int bgi_image_compressed_host(bgi_imager *im, int format, const void *da
  * handle, as uint32[n_images]; copies to host and synchronises the stream. */
 BGI_API int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream);
 
+/* Image coordinates as the reference attaches them to its Images
+ * (src/gpu/pacer_imager_hip.cpp:110-119, src/pacer_imager.cpp:192-201): the phase centre in
+ * degrees (the caller's; the reference takes it from its metadata) and the pixel scales
+ * (1 / (osf * u_max)) * 180/pi and (1 / (osf * v_max)) * 180/pi in degrees, u_max and v_max
+ * in metres as the handle holds them.  Needs the array state. */
+typedef struct bgi_image_wcs {
+    double ra_deg, dec_deg;
+    double pixscale_ra_deg, pixscale_dec_deg;
+} bgi_image_wcs;
+BGI_API int bgi_get_image_wcs(const bgi_imager *im, double ra_deg, double dec_deg, bgi_image_wcs *out);
+
+/* FITS files of host images (the reference writes its Images through astroio's
+ * Images::to_fits_files, apps/pacer_imager_main.cpp:578; astroio is not part of the
+ * reference, so the layout here is the FITS standard's).  One image per file: a primary HDU with
+ * BITPIX -32 (big-endian float32), NAXIS1 = nx columns varying fastest, NAXIS2 = ny rows in
+ * memory order, BUNIT, and with wcs the SIN-projection keywords CTYPE/CRVAL/CRPIX/CDELT/CUNIT
+ * (centre pixel nx/2+1, ny/2+1, the fftshifted phase centre; CDELT1 = -pixscale_ra,
+ * CDELT2 = pixscale_dec) and EQUINOX; FREQ (Hz) when freq_hz > 0.  pixel_stride: floats from
+ * one pixel to the next, 1 for real images, 2 to write the real parts of complex images.
+ * bgi_write_fits_block writes every image of a block [T][C][ny][nx] to
+ * <dir>/<prefix>_t<TTTT>_c<CCCC>.fits with INTERVAL and CHANNEL cards (and FREQ from
+ * freqs_hz[c] when given).  Host code only; no reference counterpart in the imaging path. */
+BGI_API int bgi_write_fits(const char *path, const float *image_host, int nx, int ny, int pixel_stride,
+                           const bgi_image_wcs *wcs, double freq_hz);
+BGI_API int bgi_write_fits_block(const char *dir, const char *prefix, const float *images_host,
+                                 int n_intervals, int n_channels, int nx, int ny, int pixel_stride,
+                                 const bgi_image_wcs *wcs, const double *freqs_hz);
+
 /* Dirty images with no device allocation.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory while they run -- a real-time pipeline that
  * budgets all GPU memory when an observation starts, a host framework that owns the device

@@ -509,3 +509,22 @@ def test_single_image_block(im):
     host = h.image_host(np.ascontiguousarray(vis))
     assert rel_l2(host, out) < 1e-6
     h.close()
+
+
+def test_image_wcs_and_fits_output(im, tmp_path):
+    """bgi_get_image_wcs gives the reference's pixel scales (src/gpu/pacer_imager_hip.cpp:113-115)
+    and a block of images goes to FITS files whose pixels are the images' real parts."""
+    obs = synth.small(seed=55, n_ant=32, n_intervals=2, n_channels=2, n_pixels=64)
+    h = _imager_for(im, obs, 64)
+    out = h.image(dev(obs.vis_f32())).cpu().numpy()
+    wcs = h.image_wcs(10.0, -26.7)
+    _, _, umax, vmax = h.uv_cell
+    assert wcs["pixscale_ra_deg"] == (1.0 / (2.0 * umax)) * (180.0 / math.pi)
+    assert wcs["pixscale_dec_deg"] == (1.0 / (2.0 * vmax)) * (180.0 / math.pi)
+    im.write_fits_block(tmp_path, "img", out, wcs, obs.freqs)
+    raw = open(tmp_path / "img_t0001_c0001.fits", "rb").read()
+    header = raw[:2880].decode("ascii")
+    assert header.startswith("SIMPLE  =                    T") and "RA---SIN" in header
+    data = np.frombuffer(raw[2880:2880 + 4 * 64 * 64], ">f4").reshape(64, 64)
+    assert np.array_equal(data, out[1, 1].real)
+    h.close()
