@@ -124,3 +124,28 @@ def test_compressed_argument_checks(im):
     with pytest.raises(capi.BgiError):
         h.image_compressed(data, None, "s16")
     h.close()
+
+
+def test_precision_form_array_at_1024(im):
+    """The precision form's array and image side on a reduced block: 128 antennas in a 3 km disk
+    with log-radial density, 10 kHz channels, 1024^2 images.  16-bit integer storage stays
+    within the 1e-4 image tolerance of the FP64 oracle; bfloat16 (8 significant bits per
+    component) does not, by the margin its rounding predicts."""
+    obs = synth.precision_form(device="cpu", n_intervals=2, n_channels=3, keep_device=False)
+    vis = obs.vis_f32()
+    n = obs.n_pixels
+    assert n == 1024 and obs.n_ant == 128
+    _, _, counters, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n,
+                                             n_uvw_sets=2)
+    h = im.Imager(n, 2.0, "XX", -1000.0)
+    h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
+    h.set_frequencies(obs.freqs)
+    errs = {}
+    for fmt in ("s16", "bf16"):
+        data, scales = im.compress_visibilities(dev(vis), fmt)
+        out = h.image_compressed(data, scales, fmt).cpu().numpy()
+        errs[fmt] = max(rel_l2(out[i, j], ref[i, j]) for i in range(2) for j in range(3))
+        assert np.array_equal(h.weight_sums(6), counters.reshape(6, -1).sum(1).astype(np.uint32))
+    assert errs["s16"] < IMAGE_TOL
+    assert IMAGE_TOL < errs["bf16"] < 1e-2
+    h.close()
