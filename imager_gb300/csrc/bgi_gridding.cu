@@ -2,17 +2,19 @@
 // src/gpu/gridding_gpu.cpp:58-124, with the CPU path's value checks,
 // src/pacer_imager.cpp:297-418).
 //
-// Grid: x = blocks of 256 baselines, y = groups of CPT consecutive images.  A thread owns one
-// baseline for CPT images (consecutive channels of an interval in the common case), so the
-// flags, u/v/w and cable delay it loads serve several visibilities, and all CPT record loads
-// are issued before any is used.  The CPT channels' constants (wavelength and fast cell
-// scales, FP64) are computed by CPT threads in parallel while those loads are in flight.
+// Grid: x = blocks of GRID_THREADS baselines, y = groups of CPT consecutive images.  A thread
+// owns one baseline for CPT images (consecutive channels of an interval in the common case), so
+// the flags and cable delay it loads -- and u/v/w and the delay when the images share a UVW set
+// -- serve several visibilities, and all of its loads are issued before any is used.  The
+// channel constants (wavelength, fast cell scales, nu/c as a float pair) come from a table the
+// handle computes once per frequency or uv-cell change (else CPT threads compute them).
 //
 // Per visibility: optional fused corrections (one delay phasor in double-float arithmetic and
 // one rotation of the selected pol -- selection is linear, so rotating after selecting equals
-// rotating the four pols first), value checks, exact cell indices, and two 8-byte vector
-// atomics (float2 atomicAdd) for the point and its conjugate.  Weight counts are reduced per
-// warp before one atomic per warp and image.
+// rotating the four pols first), value checks, exact cell indices, and 8-byte vector atomics
+// (float2 atomicAdd): one for the half-plane point (two on columns 0 and N/2), or the point and
+// its conjugate on the full plane.  Weight counts are reduced per warp, then per block, before
+// one atomic per block and image.
 #include "bgi_internal.h"
 
 namespace bgi {
@@ -22,7 +24,7 @@ namespace {
 #define GRID_THREADS 128
 #endif
 #ifndef GRID_CPT
-#define GRID_CPT 4
+#define GRID_CPT 2  // measured best with u, v, w loaded once per thread (2: 0.657 ms, 4: 0.662, 8: 0.705)
 #endif
 constexpr int kThreads = GRID_THREADS;
 constexpr int kCPT = GRID_CPT;  // images per thread
