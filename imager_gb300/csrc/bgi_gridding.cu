@@ -23,18 +23,22 @@ namespace {
 #ifndef GRID_THREADS
 #define GRID_THREADS 128
 #endif
-#ifndef GRID_CPT
-#define GRID_CPT 2  // measured best with u, v, w loaded once per thread (2: 0.657 ms, 4: 0.662, 8: 0.705)
-#endif
 constexpr int kThreads = GRID_THREADS;
-constexpr int kCPT = GRID_CPT;  // images per thread
 constexpr int kMinBlocks = 768 / GRID_THREADS;  // resident blocks per SM the registers must allow
 
-// ONE_SET: the kCPT images of every block share one UVW set (one set, or blocks that start at
-// multiples of kCPT with kCPT dividing the channel count), so a thread loads u, v, w and forms
-// the delay once for all of them.
-template <int POL, bool COUNTERS, bool HALF, int FMT, bool ONE_SET>
+// Images per thread, by array size (measured, u/v/w loaded once per thread): 2 for arrays below
+// 65,536 baselines (256 antennas, 640 images of 512^2: 0.657 ms per step against 0.662 with 4),
+// 4 above (512 antennas, the uneven batch: 9.26 ms against 9.77 with 2) -- small arrays need the
+// extra blocks, large ones the loads shared by more visibilities.
+constexpr long long kCpt4Baselines = 65536;
+int images_per_thread(long long n_baselines) { return n_baselines >= kCpt4Baselines ? 4 : 2; }
+
+// CPT: images per thread.  ONE_SET: the CPT images of every block share one UVW set (one set, or
+// blocks that start at multiples of CPT with CPT dividing the channel count), so a thread loads
+// u, v, w and forms the delay once for all of them.
+template <int POL, bool COUNTERS, bool HALF, int FMT, bool ONE_SET, int CPT>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridParams p) {
+    constexpr int kCPT = CPT;
     constexpr int NUV = ONE_SET ? 1 : kCPT;  // u, v, w registers
     __shared__ ChannelConst s_cc[kCPT];
     __shared__ unsigned int s_count[kCPT][kThreads / 32];  // per-warp weight counts
@@ -169,32 +173,42 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
     }
 }
 
-// whether every block's kCPT images share one UVW set (grid_kernel's ONE_SET)
-bool one_set(const GridParams &q) {
-    return q.n_uvw_sets == 1 || (q.n_channels % kCPT == 0 && q.img_begin % kCPT == 0);
+// whether every block's cpt images share one UVW set (grid_kernel's ONE_SET)
+bool one_set(const GridParams &q, int cpt) {
+    return q.n_uvw_sets == 1 || (q.n_channels % cpt == 0 && q.img_begin % cpt == 0);
 }
 
-template <int POL, int FMT>
+template <int POL, int FMT, int CPT>
 void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
-    const bool one = one_set(q);
+    const bool one = one_set(q, CPT);
     if (q.half_width > 0) {
-        if (one) grid_kernel<POL, false, true, FMT, true><<<grid, kThreads, 0, s>>>(q);
-        else grid_kernel<POL, false, true, FMT, false><<<grid, kThreads, 0, s>>>(q);
+        if (one) grid_kernel<POL, false, true, FMT, true, CPT><<<grid, kThreads, 0, s>>>(q);
+        else grid_kernel<POL, false, true, FMT, false, CPT><<<grid, kThreads, 0, s>>>(q);
     } else {
-        if (one) grid_kernel<POL, false, false, FMT, true><<<grid, kThreads, 0, s>>>(q);
-        else grid_kernel<POL, false, false, FMT, false><<<grid, kThreads, 0, s>>>(q);
+        if (one) grid_kernel<POL, false, false, FMT, true, CPT><<<grid, kThreads, 0, s>>>(q);
+        else grid_kernel<POL, false, false, FMT, false, CPT><<<grid, kThreads, 0, s>>>(q);
     }
 }
 
-template <int POL>
+template <int POL, int CPT>
 void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
     switch (q.vis_format) {
-        case BGI_VIS_S16: launch_fmt<POL, BGI_VIS_S16>(grid, q, s); break;
-        case BGI_VIS_BF16: launch_fmt<POL, BGI_VIS_BF16>(grid, q, s); break;
-        case BGI_VIS_FP16: launch_fmt<POL, BGI_VIS_FP16>(grid, q, s); break;
+        case BGI_VIS_S16: launch_fmt<POL, BGI_VIS_S16, CPT>(grid, q, s); break;
+        case BGI_VIS_BF16: launch_fmt<POL, BGI_VIS_BF16, CPT>(grid, q, s); break;
+        case BGI_VIS_FP16: launch_fmt<POL, BGI_VIS_FP16, CPT>(grid, q, s); break;
         default:
-            if (q.counter_mode >= 0) grid_kernel<POL, true, false, BGI_VIS_C64, false><<<grid, kThreads, 0, s>>>(q);
-            else launch_fmt<POL, BGI_VIS_C64>(grid, q, s);
+            if (q.counter_mode >= 0) grid_kernel<POL, true, false, BGI_VIS_C64, false, CPT><<<grid, kThreads, 0, s>>>(q);
+            else launch_fmt<POL, BGI_VIS_C64, CPT>(grid, q, s);
+    }
+}
+
+template <int CPT>
+void launch_cpt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
+    switch (q.pol) {
+        case BGI_POL_XX: launch_pol<BGI_POL_XX, CPT>(grid, q, s); break;
+        case BGI_POL_YY: launch_pol<BGI_POL_YY, CPT>(grid, q, s); break;
+        case BGI_POL_I: launch_pol<BGI_POL_I, CPT>(grid, q, s); break;
+        default: launch_pol<BGI_POL_V, CPT>(grid, q, s); break;
     }
 }
 
@@ -222,17 +236,14 @@ int launch_gridding(const GridParams &p, cudaStream_t s) {
         return set_error(BGI_ERR_UNSUPPORTED, "gridding: counter grids need complex64 visibilities");
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;
     const int max_groups = 65535;
-    for (int done = 0; done < p.img_count; done += max_groups * kCPT) {
+    const int cpt = images_per_thread(p.n_baselines);
+    for (int done = 0; done < p.img_count; done += max_groups * cpt) {
         GridParams q = p;
         q.img_begin = p.img_begin + done;
-        q.img_count = std::min(p.img_count - done, max_groups * kCPT);
-        const dim3 grid((unsigned)bx, (unsigned)((q.img_count + kCPT - 1) / kCPT));
-        switch (p.pol) {
-            case BGI_POL_XX: launch_pol<BGI_POL_XX>(grid, q, s); break;
-            case BGI_POL_YY: launch_pol<BGI_POL_YY>(grid, q, s); break;
-            case BGI_POL_I: launch_pol<BGI_POL_I>(grid, q, s); break;
-            default: launch_pol<BGI_POL_V>(grid, q, s); break;
-        }
+        q.img_count = std::min(p.img_count - done, max_groups * cpt);
+        const dim3 grid((unsigned)bx, (unsigned)((q.img_count + cpt - 1) / cpt));
+        if (cpt == 4) launch_cpt<4>(grid, q, s);
+        else launch_cpt<2>(grid, q, s);
         int st = check_launch("gridding");
         if (st) return st;
     }

@@ -528,3 +528,30 @@ def test_image_wcs_and_fits_output(im, tmp_path):
     data = np.frombuffer(raw[2880:2880 + 4 * 64 * 64], ">f4").reshape(64, 64)
     assert np.array_equal(data, out[1, 1].real)
     h.close()
+
+
+def test_image_buffers_off_16_byte_boundaries(im):
+    """The complex-to-real pass stores pixel pairs (16 bytes of complex, 8 of real pixels): a
+    complex image buffer aligned to 8 bytes but not 16 routes the block to the full plane, with
+    the same images; real images 8-byte aligned stay on the half plane; buffers not 8-byte
+    aligned are refused before any launch."""
+    obs = synth.small(seed=57, n_ant=32, n_intervals=1, n_channels=2, n_pixels=64)
+    h = _imager_for(im, obs, 64)
+    vis = dev(obs.vis_f32())
+    ref = h.image(vis).cpu().numpy()
+    npix = 2 * 64 * 64
+    raw = torch.empty(npix + 1, dtype=torch.complex64, device="cuda")
+    shifted = raw[1:].view(1, 2, 64, 64)            # 8 bytes past a 16-byte boundary
+    assert shifted.data_ptr() % 16 == 8
+    h.image(vis, out=shifted)
+    assert rel_l2(shifted.cpu().numpy(), ref) < 1e-6
+    raw_r = torch.empty(npix + 4, dtype=torch.float32, device="cuda")
+    real8 = raw_r[2:2 + npix].view(1, 2, 64, 64)      # real images, 8 bytes past 16
+    assert real8.data_ptr() % 16 == 8
+    h.image(vis, flags=im.APPLY_GEOMETRIC | im.APPLY_CABLE | im.OUTPUT_REAL, out=real8)
+    assert rel_l2(real8.cpu().numpy(), ref.real) < 1e-6
+    real4 = raw_r[1:1 + npix].view(1, 2, 64, 64)      # 4-byte aligned
+    with pytest.raises(capi.BgiError) as e:
+        h.image(vis, flags=im.APPLY_GEOMETRIC | im.APPLY_CABLE | im.OUTPUT_REAL, out=real4)
+    assert e.value.status == capi.ERR_INVALID
+    h.close()
