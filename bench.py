@@ -491,7 +491,12 @@ def precision_measure(args, stream, flush):
     t1.close()
     del d1, s1
     h.set_schedule(wave, lanes)
-    out = torch.empty((T, Cn, n, n), dtype=torch.complex64, device="cuda")
+    # complex images of the whole block (129 GB); real images (half) when the device has less free
+    free, _ = torch.cuda.mem_get_info()
+    need_complex = T * Cn * n * n * 8 + 4 * vis.numel() + (4 << 30)  # images, stored forms, margin
+    real_out = free < need_complex
+    flags = flags | (IM.OUTPUT_REAL if real_out else 0)
+    out = torch.empty((T, Cn, n, n), dtype=torch.float32 if real_out else torch.complex64, device="cuda")
     samples = ((0, 0), (T // 2, Cn // 2), (T - 1, Cn - 1))
     refs = {}
     for t, c in samples:
@@ -533,6 +538,8 @@ def precision_measure(args, stream, flush):
                         "phase reduced in double-float), 16-bit formats with one FP32 scale per 128 baselines",
             "images_per_step": n_images, "steps": k,
             "schedule": {"images_per_wave": wave or "auto", "lanes": lanes, "chosen_by": "bgi_autotune on interval 0"},
+            "images": "real (float32): the device had less free memory than the complex block needs" if real_out
+            else "complex64",
             "sampled_images": [f"interval {t}, channel {c}" for t, c in samples],
             "oracle": "FP64 oracle of the original complex64 visibilities",
             "fft": "FP32 Stockham passes of our own (no tensor-core DFT stages)",
@@ -724,9 +731,21 @@ def run_ours(args, rank, world, local_rank):
     if rank != 0:
         dist.destroy_process_group()
         return 0
-    serving = serving_measure(args) if (args.serving and world == 1) else None
-    batched = batched_measure(args, stream, flush) if (args.batched and world == 1) else None
-    precision = precision_measure(args, stream, flush) if (args.precision and world == 1) else None
+    def section(enabled, fn, *a):
+        """A workload section of the line; its failure is reported in the line instead of ending
+        the run (the headline above stands on its own)."""
+        if not (enabled and world == 1):
+            return None
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+            return {"error": f"{type(e).__name__}: {e}"[:400]}
+
+    serving = section(args.serving, serving_measure, args)
+    batched = section(args.batched, batched_measure, args, stream, flush)
+    precision = section(args.precision, precision_measure, args, stream, flush)
 
     images_per_s = world * n_images * args.steps / (ms / 1000.0)
     hbm_peak, peak_kind = measured_peaks()
