@@ -15,6 +15,7 @@ from . import build as _build
 HEADER = os.path.join(_build.ROOT, "include", "blink_imager_gb300.h")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_STATE = 0, -1, -2, -3, -4, -5
+ERR_BUSY, ERR_CANCELLED = -6, -7
 POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 COUNTERS_FIRST_INTERVAL, COUNTERS_PER_IMAGE = 0, 1
 APPLY_GEOMETRIC, APPLY_CABLE, OUTPUT_REAL = 0x1, 0x2, 0x4
@@ -35,7 +36,7 @@ class Config(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("max_slots", C.c_int), ("hbm_budget_bytes", C.c_size_t),
-                ("reserve_bytes", C.c_size_t), ("deterministic", C.c_int)]
+                ("reserve_bytes", C.c_size_t), ("deterministic", C.c_int), ("max_queued", C.c_int)]
 
 
 class ServerStats(C.Structure):
@@ -43,7 +44,8 @@ class ServerStats(C.Structure):
                 ("images", C.c_uint64), ("admission_waits", C.c_uint64), ("queued", C.c_uint64),
                 ("device_bytes_in_use", C.c_size_t), ("device_budget_bytes", C.c_size_t),
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double),
-                ("wall_s", C.c_double), ("images_per_s", C.c_double)]
+                ("wall_s", C.c_double), ("images_per_s", C.c_double), ("rejected", C.c_uint64),
+                ("cancelled", C.c_uint64)]
 
 
 class BatchItem(C.Structure):
@@ -109,6 +111,7 @@ _SIGNATURES = {
     "bgi_server_submit": (_i, [_vp, _i, _i, _vp, _vp, _i, C.c_uint, _vp, C.POINTER(C.c_uint64)]),
     "bgi_server_wait": (_i, [_vp, C.c_uint64, _i, C.POINTER(_i)]),
     "bgi_server_poll": (_i, [_vp, C.c_uint64, C.POINTER(_i), C.POINTER(_i)]),
+    "bgi_server_cancel": (_i, [_vp, C.c_uint64]),
     "bgi_server_get_stats": (_i, [_vp, C.POINTER(ServerStats)]),
     "bgi_server_reset_stats": (_i, [_vp]),
     "bgi_set_schedule": (_i, [_vp, _i, _i]),

@@ -94,6 +94,7 @@ struct bgi_server {
     // statistics since the last reset
     std::vector<double> latencies_ms;
     uint64_t n_submitted = 0, n_completed = 0, n_failed = 0, n_images = 0, n_admission_waits = 0;
+    uint64_t n_rejected = 0, n_cancelled = 0;
     Clock::time_point t_first_submit, t_last_done;
     bool any_submit = false;
 
@@ -122,7 +123,7 @@ struct bgi_server {
         r->status = status;
         if (status != BGI_OK) {
             r->error = msg ? msg : "";
-            ++n_failed;
+            if (status != BGI_ERR_CANCELLED) ++n_failed;
         } else {
             latencies_ms.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
             n_images += (uint64_t)r->n_images;
@@ -279,6 +280,7 @@ int bgi_server_create(const bgi_server_config *cfg, bgi_server **out) {
     if (!cfg || !out) return set_error(BGI_ERR_INVALID, "server_create: null argument");
     *out = nullptr;
     if (cfg->max_slots < 1 || cfg->max_slots > 64) return set_error(BGI_ERR_INVALID, "server_create: 1 <= max_slots <= 64");
+    if (cfg->max_queued < 0) return set_error(BGI_ERR_INVALID, "server_create: max_queued >= 0");
     int n_dev = 0;
     int st = check_cuda(cudaGetDeviceCount(&n_dev), "server_create: device count");
     if (st) return st;
@@ -386,6 +388,10 @@ int bgi_server_submit(bgi_server *sv, int array_id, int format, const void *vis_
     const ArrayState &a = *sv->arrays[(size_t)array_id];
     if (a.n_uvw_sets != 1 && a.n_uvw_sets != n_intervals)
         return set_error(BGI_ERR_INVALID, "server_submit: array has %d UVW sets for %d intervals", a.n_uvw_sets, n_intervals);
+    if (sv->cfg.max_queued > 0 && sv->queue.size() >= (size_t)sv->cfg.max_queued) {
+        ++sv->n_rejected;
+        return set_error(BGI_ERR_BUSY, "server_submit: %d requests already wait for admission", sv->cfg.max_queued);
+    }
     const size_t imgs = (size_t)n_intervals * a.n_channels, n = (size_t)a.cfg.n_pixels;
     r->array = sv->arrays[(size_t)array_id];
     r->array_id = array_id;
@@ -441,6 +447,24 @@ int bgi_server_wait(bgi_server *sv, uint64_t ticket, int timeout_ms, int *status
     return collect(sv, ticket, status, lk, true, timeout_ms, nullptr);
 }
 
+int bgi_server_cancel(bgi_server *sv, uint64_t ticket) {
+    if (!sv) return set_error(BGI_ERR_INVALID, "server_cancel: null server");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->requests.find(ticket);
+    if (it == sv->requests.end())
+        return set_error(BGI_ERR_INVALID, "server_cancel: unknown or already collected ticket %llu",
+                         (unsigned long long)ticket);
+    std::shared_ptr<Request> r = it->second;
+    auto q = std::find(sv->queue.begin(), sv->queue.end(), r);
+    if (q == sv->queue.end()) return set_error(BGI_ERR_STATE, "server_cancel: the request is already admitted");
+    sv->queue.erase(q);
+    r->t_done = Clock::now();
+    ++sv->n_cancelled;
+    sv->finish(r, BGI_ERR_CANCELLED, "server: the request was cancelled");
+    sv->cv_work.notify_one();  // the next request may be admitted now
+    return BGI_OK;
+}
+
 int bgi_server_poll(bgi_server *sv, uint64_t ticket, int *done, int *status) {
     if (!sv || !done || !status) return set_error(BGI_ERR_INVALID, "server_poll: null argument");
     std::unique_lock<std::mutex> lk(sv->mu);
@@ -459,6 +483,8 @@ int bgi_server_get_stats(bgi_server *sv, bgi_server_stats *out) {
     s.queued = sv->queue.size();
     s.device_bytes_in_use = sv->in_use;
     s.device_budget_bytes = sv->budget;
+    s.rejected = sv->n_rejected;
+    s.cancelled = sv->n_cancelled;
     std::vector<double> lat = sv->latencies_ms;
     if (!lat.empty()) {
         std::sort(lat.begin(), lat.end());
@@ -485,6 +511,7 @@ int bgi_server_reset_stats(bgi_server *sv) {
     std::lock_guard<std::mutex> lk(sv->mu);
     sv->latencies_ms.clear();
     sv->n_submitted = sv->n_completed = sv->n_failed = sv->n_images = sv->n_admission_waits = 0;
+    sv->n_rejected = sv->n_cancelled = 0;
     sv->any_submit = false;
     return BGI_OK;
 }

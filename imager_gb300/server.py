@@ -24,9 +24,9 @@ from .imager import _ptr
 
 class Server:
     def __init__(self, device: int = 0, max_slots: int = 4, hbm_budget_bytes: int = 0,
-                 reserve_bytes: int = 1 << 30, deterministic: bool = False):
+                 reserve_bytes: int = 1 << 30, deterministic: bool = False, max_queued: int = 0):
         cfg = capi.ServerConfig(int(device), int(max_slots), int(hbm_budget_bytes), int(reserve_bytes),
-                                int(bool(deterministic)))
+                                int(bool(deterministic)), int(max_queued))
         h = C.c_void_p()
         call("bgi_server_create", C.byref(cfg), C.byref(h))
         self._h = h
@@ -105,6 +105,15 @@ class Server:
         _, out = self._live.pop(ticket)
         capi.check(st.value)
         return out
+
+    def cancel(self, ticket: int) -> bool:
+        """Cancels a request not yet admitted (its wait then raises BgiError ERR_CANCELLED);
+        False when it is already on the GPU or finished."""
+        st = capi.lib().bgi_server_cancel(self._h, C.c_uint64(ticket))
+        if st == capi.ERR_STATE:
+            return False
+        capi.check(st)
+        return True
 
     def stats(self) -> dict:
         s = capi.ServerStats()

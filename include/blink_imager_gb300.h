@@ -50,7 +50,9 @@ enum bgi_status {
     BGI_ERR_CUDA = -2,        /* a CUDA call or launch failed */
     BGI_ERR_ALLOC = -3,       /* device or pinned allocation failed */
     BGI_ERR_UNSUPPORTED = -4, /* valid input this build does not handle (e.g. image side) */
-    BGI_ERR_STATE = -5        /* handle not ready (array or frequencies not set) */
+    BGI_ERR_STATE = -5,       /* handle not ready (array or frequencies not set) */
+    BGI_ERR_BUSY = -6,        /* serving: the request queue is full (bgi_server_config.max_queued) */
+    BGI_ERR_CANCELLED = -7    /* serving: the request was cancelled before it was admitted */
 };
 
 /* Polarisation to image; same order as the reference's enum class Polarization
@@ -419,6 +421,8 @@ typedef struct bgi_server_config {
     size_t hbm_budget_bytes;  /* request buffers at once; 0 = free memory at creation less the reserve */
     size_t reserve_bytes;     /* device memory left free at admission (handles' scratch, other users) */
     int deterministic;        /* 1: ordered gridding (results independent of the mix) */
+    int max_queued;           /* requests waiting for admission at most (0 = no limit); beyond it
+                                 bgi_server_submit fails with BGI_ERR_BUSY */
 } bgi_server_config;
 
 typedef struct bgi_server_stats {
@@ -426,6 +430,7 @@ typedef struct bgi_server_stats {
     size_t device_bytes_in_use, device_budget_bytes;
     double p50_ms, p99_ms, max_ms, mean_ms; /* submit-to-done latency of completed requests */
     double wall_s, images_per_s;            /* first submission to last completion */
+    uint64_t rejected, cancelled;           /* submissions refused by a full queue; cancellations */
 } bgi_server_stats;
 
 BGI_API int bgi_server_create(const bgi_server_config *cfg, bgi_server **out);
@@ -445,6 +450,10 @@ BGI_API int bgi_server_submit(bgi_server *sv, int array_id, int format, const vo
 /* Wait for (timeout_ms < 0: without limit) or poll a request; a finished request reports its
  * status once (BGI_OK or the failure, message in bgi_last_error) and its ticket is released. */
 BGI_API int bgi_server_wait(bgi_server *sv, uint64_t ticket, int timeout_ms, int *status);
+/* Cancels a request that has not been admitted yet: it leaves the queue and reports
+ * BGI_ERR_CANCELLED to its wait or poll.  A request already on the GPU (or finished) is not
+ * cancelled: BGI_ERR_STATE. */
+BGI_API int bgi_server_cancel(bgi_server *sv, uint64_t ticket);
 BGI_API int bgi_server_poll(bgi_server *sv, uint64_t ticket, int *done, int *status);
 BGI_API int bgi_server_get_stats(bgi_server *sv, bgi_server_stats *out);
 BGI_API int bgi_server_reset_stats(bgi_server *sv);

@@ -1,8 +1,9 @@
 """Serving runtime (bgi_server_*): requests of several arrays, sizes and storage formats
 submitted together overlap on the GPU, and each request's images are the same as when it runs
 alone (bit for bit with the ordered gridder, to summation order otherwise) and as the imager
-handle's; admission waits for memory under a small budget; a request larger than the budget
-fails cleanly; latency statistics are reported."""
+handle's; admission waits for memory under a small budget; faults injected on the host -- a
+request larger than the budget, malformed blocks, a full queue, a cancelled request -- fail
+cleanly while the server keeps serving; latency statistics are reported."""
 import numpy as np
 import pytest
 
@@ -118,3 +119,63 @@ def test_request_larger_than_budget_fails(mods):
         st = capi.lib().bgi_server_submit(sv._h, aid + 5, 0, buf.ctypes.data, None, 1, 3, buf.ctypes.data,
                                           C.byref(ticket))
         assert st == capi.ERR_INVALID
+
+
+def test_malformed_blocks_are_refused_at_submission(mods):
+    """Faults injected on the host: every malformed submission fails at once with
+    BGI_ERR_INVALID and leaves the server serving."""
+    import ctypes as C
+    imager, server = mods
+    obs = synth.small(seed=76, n_ant=16, n_intervals=2, n_channels=2, n_pixels=64)
+    with server.Server(max_slots=2) as sv:
+        aid = sv.add_array(64, obs.u, obs.v, obs.w, obs.flags, obs.cable, obs.freqs)
+        lib, buf, t = capi.lib(), np.zeros(64, np.float32), C.c_uint64(0)
+        p = buf.ctypes.data
+        bad = [
+            (aid, 0, None, None, 2, 3, p),      # no visibilities
+            (aid, 0, p, None, 2, 3, None),      # no image buffer
+            (aid, 9, p, None, 2, 3, p),         # unknown storage format
+            (aid, 1, p, None, 2, 3, p),         # 16-bit storage without scales
+            (aid, 0, p, None, 3, 3, p),         # 3 intervals for an array with 2 UVW sets
+            (aid, 0, p, None, 0, 3, p),         # no interval
+            (aid, 0, p, None, 2, 1 << 9, p),    # unknown flag
+        ]
+        for a, fmt, vis, sc, T, fl, img in bad:
+            assert lib.bgi_server_submit(sv._h, a, fmt, vis, sc, T, fl, img, C.byref(t)) == capi.ERR_INVALID
+        out = sv.wait(sv.submit(aid, obs.vis_f32())).numpy()   # still serving
+        assert np.isfinite(out).all() and sv.stats()["failed"] == 0
+
+
+def test_queue_limit_and_cancellation(mods):
+    """A full queue refuses submissions with BGI_ERR_BUSY; a request still waiting for
+    admission can be cancelled (its wait reports BGI_ERR_CANCELLED) and the others complete with
+    the images of the handle."""
+    imager, server = mods
+    obs = synth.small(seed=77, n_ant=64, n_intervals=1, n_channels=16, n_pixels=1024)
+    vis = obs.vis_f32()
+    req_bytes = vis.nbytes + 16 * 1024 * 1024 * 8
+    # one slot and memory for one request at a time: the others wait in the queue
+    with server.Server(max_slots=1, hbm_budget_bytes=int(req_bytes * 1.5), deterministic=True,
+                       max_queued=2) as sv:
+        aid = sv.add_array(1024, obs.u, obs.v, obs.w, obs.flags, obs.cable, obs.freqs)
+        tickets, busy = [], 0
+        for _ in range(8):
+            try:
+                tickets.append(sv.submit(aid, vis))
+            except capi.BgiError as e:
+                assert e.status == capi.ERR_BUSY
+                busy += 1
+        assert busy >= 1 and len(tickets) + busy == 8
+        assert len(tickets) >= 2                          # the second submission always fits
+        assert sv.cancel(tickets[-1])                     # behind at least one request: still queued
+        with pytest.raises(capi.BgiError) as e:
+            sv.wait(tickets[-1])
+        assert e.value.status == capi.ERR_CANCELLED
+        outs = [sv.wait(t).numpy() for t in tickets[:-1]]
+        st = sv.stats()
+        assert st["rejected"] == busy and st["cancelled"] == 1 and st["failed"] == 0
+        with pytest.raises(capi.BgiError):
+            sv.cancel(tickets[0])                         # already collected
+    ref = _handle_images(imager, obs, "XX", True)
+    for o in outs:
+        assert np.array_equal(o.view(np.uint32), ref.view(np.uint32))
