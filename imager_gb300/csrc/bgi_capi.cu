@@ -16,6 +16,8 @@
 #include <memory>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>  // header-only; ranges cost nothing without a profiler attached
+
 #include "bgi_internal.h"
 
 namespace bgi {
@@ -56,6 +58,16 @@ using namespace bgi;
         int _st = (expr);          \
         if (_st != BGI_OK) return _st; \
     } while (0)
+
+namespace {
+// An NVTX range over a scope (for timelines of Nsight Systems and similar tools).
+struct TraceRange {
+    explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+};
+}  // namespace
 
 namespace {
 
@@ -704,6 +716,7 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         *next = (*next + 1) % n_streams;
         cudaStream_t ls = streams[l];
         const int cnt = std::min(wave, img_first + count - img0);
+        TraceRange trace("wave");
         float2 *grid = im->grid[l].ptr;
         const size_t need = (size_t)cnt * (p.half_width > 0 ? (size_t)n * p.half_width : npix);
         if (need > im->grid[l].cap) return set_error(BGI_ERR_STATE, "grid scratch too small for a wave");
@@ -747,6 +760,7 @@ namespace {
 
 int image_impl(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals, unsigned flags,
                float *images, void *stream) {
+    TraceRange trace("bgi_image");
     BGI_TRY(image_checks(im, n_intervals, flags));
     const float *vis = static_cast<const float *>(data);
     if (!vis || !images || (format != BGI_VIS_C64 && !scales)) return set_error(BGI_ERR_INVALID, "image: null buffer");
@@ -874,6 +888,7 @@ int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi
 
 int bgi_batch_launch(bgi_batch *b, void *stream) {
     if (!b || !b->exec) return set_error(BGI_ERR_INVALID, "batch_launch: no batch");
+    TraceRange trace("bgi_batch_launch");
     int cur = -1;
     cudaGetDevice(&cur);
     if (cur != b->device) BGI_TRY(check_cuda(cudaSetDevice(b->device), "cudaSetDevice"));
@@ -1013,6 +1028,7 @@ int planes_for(int pol, int out[2]) {
 // different chunks overlap.
 int image_host_impl(bgi_imager *im, int format, const void *vis_host, const float *scales_host, int n_intervals,
                     unsigned flags, float *images_host, void *stream) {
+    TraceRange trace("bgi_image_host");
     BGI_TRY(image_checks(im, n_intervals, flags));
     if (!vis_host || !images_host || (format != BGI_VIS_C64 && !scales_host))
         return set_error(BGI_ERR_INVALID, "image_host: null buffer");

@@ -22,6 +22,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "bgi_internal.h"
 
 using bgi::check_cuda;
@@ -153,6 +155,13 @@ struct bgi_server {
 
     // Issues one admitted request on its slot's stream (outside mu).
     int launch(Request &r) {
+        nvtxRangePushA("bgi_server request");
+        const int st = launch_request(r);
+        nvtxRangePop();
+        return st;
+    }
+
+    int launch_request(Request &r) {
         Slot &slot = slots[(size_t)r.slot];
         cudaStream_t s = slot.stream;
         int st = BGI_OK;
