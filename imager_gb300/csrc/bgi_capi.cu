@@ -1185,12 +1185,7 @@ int bgi_gridding_kb_gpu(const float *vis, int n_ant, int n_channels, int n_inter
                             freqs_hz, delta_u, delta_v, n_pixels, min_uv, pol, counter_mode, counters, grids, &p));
     std::vector<float> table;
     kb_tables(kernel_size, with_sinc != 0, table);
-    int st = BGI_OK;
-    cudaStream_t s = as_stream(stream);
-    p.kb_table = kb_free_table(s, table, &st);
-    if (st) return st;
-    p.kb_size = kernel_size;
-    return launch_gridding(p, s);
+    return launch_gridding_kb_free(p, table, kernel_size, as_stream(stream));
 }
 
 int bgi_set_deterministic(bgi_imager *im, int enable) {

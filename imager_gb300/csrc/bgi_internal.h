@@ -67,8 +67,9 @@ constexpr int kMaxKernel = 16;
 // the reference's kernel rows [1023][ksize] as float
 void kb_tables(int ksize, bool with_sinc, std::vector<float> &out);
 int launch_gridding_kb(const GridParams &p, const float *table, int ksize, cudaStream_t s);
-// the free function's device table, filled with `table` (synchronous)
-float *kb_free_table(cudaStream_t s, const std::vector<float> &table, int *status);
+// the free function's gridding: `table` uploaded into stream-ordered memory of this call, used
+// by the launch and freed after it on `s`
+int launch_gridding_kb_free(GridParams p, const std::vector<float> &table, int ksize, cudaStream_t s);
 
 // ---- block-scaled 16-bit visibilities (bgi_compress.cu) -------------------------------------
 long long vis_blocks(long long n_baselines);

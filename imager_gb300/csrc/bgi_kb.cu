@@ -155,19 +155,21 @@ double bessel_i0(double x, double eps) {
     return sum;
 }
 
-// kernel table of the free function (bgi_gridding_kb_gpu), uploaded on its stream before use
-__device__ float g_kb_free_table[kOversampling * kMaxKernel];
-
 }  // namespace
 
-float *kb_free_table(cudaStream_t s, const std::vector<float> &table, int *status) {
-    float *ptr = nullptr;
-    *status = check_cuda(cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_kb_free_table), "kb table address");
-    if (*status) return nullptr;
-    *status = check_cuda(cudaMemcpyAsync(ptr, table.data(), sizeof(float) * table.size(), cudaMemcpyHostToDevice, s),
-                         "kb table upload");
-    if (!*status) *status = check_cuda(cudaStreamSynchronize(s), "kb table upload");  // the host vector is freed next
-    return *status ? nullptr : ptr;
+int launch_gridding_kb_free(GridParams p, const std::vector<float> &table, int ksize, cudaStream_t s) {
+    // the table in stream-ordered memory of this call: calls on other streams have their own
+    float *d_table = nullptr;
+    const size_t bytes = sizeof(float) * table.size();
+    int st = check_cuda(cudaMallocAsync(reinterpret_cast<void **>(&d_table), bytes, s), "kb table");
+    if (st) return st;
+    // pageable source: the copy has taken the host data when the call returns
+    st = check_cuda(cudaMemcpyAsync(d_table, table.data(), bytes, cudaMemcpyHostToDevice, s), "kb table upload");
+    p.kb_table = d_table;
+    p.kb_size = ksize;
+    if (!st) st = launch_gridding(p, s);
+    const int freed = check_cuda(cudaFreeAsync(d_table, s), "kb table free");
+    return st ? st : freed;
 }
 
 void kb_tables(int ksize, bool with_sinc, std::vector<float> &out) {

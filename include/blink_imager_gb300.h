@@ -140,10 +140,9 @@ BGI_API int bgi_gridding_sorted_gpu(const float *vis, int n_ant, int n_channels,
  * m_nConvolvingKernelSize > 0, src/pacer_imager.cpp:378-403 and 565-750; CPU only there): as
  * bgi_gridding_gpu, but each visibility and its conjugate are spread over kernel_size^2 cells
  * (1..16) with the reference's kernel (1023 oversampled rows, Kaiser-Bessel alpha 8.6, times a
- * sinc unless with_sinc == 0); counters count the nearest cells, as the reference's.  The kernel
- * table lives in one device array of the library, uploaded on `stream` by each call (the upload
- * is synchronous): calls with different kernels that overlap on the GPU race on it, so serialise
- * them (the handle's kernel mode keeps its own table and has no such limit). */
+ * sinc unless with_sinc == 0); counters count the nearest cells, as the reference's.  Each call
+ * uploads its kernel table into stream-ordered memory on `stream` (cudaMallocAsync, freed after
+ * the launch), so calls on different streams do not share it. */
 BGI_API int bgi_gridding_kb_gpu(const float *vis, int n_ant, int n_channels, int n_intervals,
                                 const float *u, const float *v, int n_uvw_sets,
                                 const int *baseline_flags, const double *freqs_hz, double delta_u,

@@ -132,3 +132,29 @@ def test_kb_imager_against_oracle(im):
     with pytest.raises(capi.BgiError):
         h.set_gridding_kernel(17)
     h.close()
+
+
+def test_kb_free_function_on_concurrent_streams(im):
+    """Calls with different kernel sizes issued on two streams at once each use their own
+    kernel table (stream-ordered memory of the call): the same counters and grids as alone."""
+    obs = synth.small(seed=103, n_ant=40, n_intervals=1, n_channels=2, n_pixels=64)
+    vis = dev(obs.vis_f32())
+    umax, vmax = O.uv_max(obs.u, obs.v, obs.flags)
+    du, dv = O.delta_uv(2.0, umax, 64), O.delta_uv(2.0, vmax, 64)
+    args = [dev(a) for a in (obs.u, obs.v, obs.flags, obs.freqs)]
+    alone = {k: _grid_kb(im, obs.vis_f32(), obs.u, obs.v, obs.flags, obs.freqs, du, dv, 64, k, -1000.0, "XX", 1)
+             for k in (5, 11)}
+    streams = {k: torch.cuda.Stream() for k in (5, 11)}
+    outs = {}
+    for rep in range(3):
+        for k in (5, 11):
+            g = torch.zeros((1, 2, 64, 64), dtype=torch.complex64, device="cuda")
+            c = torch.zeros((1, 2, 64, 64), dtype=torch.float32, device="cuda")
+            streams[k].wait_stream(torch.cuda.current_stream())  # inputs and zeroed outputs ready
+            im.gridding_kb(vis, *args, du, dv, 64, -1000.0, "XX", g, c, kernel_size=k, stream=streams[k])
+            outs[(rep, k)] = (g, c)
+    torch.cuda.synchronize()
+    for (rep, k), (g, c) in outs.items():
+        assert np.array_equal(c.cpu().numpy(), alone[k][1]), (rep, k)
+        ref = alone[k][0]
+        assert np.abs(g.cpu().numpy() - ref).max() <= GRID_TOL * np.abs(ref).max(), (rep, k)
