@@ -174,6 +174,10 @@ BGI_API int bgi_image_averaging_gpu(const float *images, int64_t image_size, int
  * 2. Imager handle: resident array state, fused whole-path imaging
  *    (CPacerImagerHip with its members, src/gpu/pacer_imager_hip.h:12-58)
  * ------------------------------------------------------------------------------------------ */
+/* A handle holds device state and per-call scratch: calls on one handle must not overlap (one
+ * host thread at a time, and a later call may reuse the scratch of an earlier one on its
+ * streams); different handles are independent.  The serving runtime (section 3) gives each of
+ * its slots its own handles. */
 typedef struct bgi_imager bgi_imager;
 
 typedef struct bgi_config {
@@ -193,10 +197,12 @@ BGI_API int bgi_create(const bgi_config *cfg, bgi_imager **out);
 BGI_API int bgi_destroy(bgi_imager *im);
 
 /* Resident array state from host arrays (copied).  u, v, w: float[n_uvw_sets][B];
- * baseline_flags: int[B] (nonzero = flagged; autos are flagged by the caller as in
- * CPacerImager::UpdateFlags, src/pacer_imager.cpp:60-86); cable_lengths: double[n_ant].
- * Computes u_max/v_max over unflagged baselines of every set and delta_u/delta_v
- * (src/pacer_imager.cpp:213-221, 497-499). */
+ * baseline_flags: int[B], flag > 0 = flagged as in the reference's GPU gridder
+ * (src/gpu/gridding_gpu.cpp:101; for the 0/1 flags of CPacerImager::UpdateFlags,
+ * src/pacer_imager.cpp:60-86, the CPU path's nonzero test agrees; autos are flagged by the
+ * caller); cable_lengths: double[n_ant].  Computes u_max/v_max over baselines with flag 0 in
+ * every set and delta_u/delta_v (src/pacer_imager.cpp:213-221, 497-499).  A negative flag
+ * (gridded, but outside u_max) keeps the handle's blocks on the full plane. */
 BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, const float *v,
                   const float *w, const int *baseline_flags, const double *cable_lengths);
 
