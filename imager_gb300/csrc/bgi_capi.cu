@@ -60,7 +60,9 @@ using namespace bgi;
     } while (0)
 
 namespace {
-// An NVTX range over a scope (for timelines of Nsight Systems and similar tools).
+// An NVTX range over a scope, named for the C-ABI call it covers: it shows the call on timelines
+// of Nsight Systems and similar tools, and `ncu --nvtx --nvtx-include "<name>/"` profiles only
+// the kernels that call launched.
 struct TraceRange {
     explicit TraceRange(const char *name) { nvtxRangePushA(name); }
     ~TraceRange() { nvtxRangePop(); }
@@ -238,6 +240,7 @@ int bgi_version(void) { return 100 * BGI_VERSION_MAJOR + BGI_VERSION_MINOR; }
 int bgi_apply_geometric_corrections_gpu(float *vis, int n_ant, int n_channels, int n_intervals,
                                         const float *w, int n_uvw_sets, const double *freqs_hz,
                                         void *stream) {
+    TraceRange trace("bgi_apply_geometric_corrections_gpu");
     if (!vis || !w || !freqs_hz || n_ant < 1 || n_channels < 1 || n_intervals < 0)
         return set_error(BGI_ERR_INVALID, "apply_geometric_corrections: bad arguments");
     if (n_uvw_sets != 1 && n_uvw_sets != n_intervals)
@@ -250,6 +253,7 @@ int bgi_apply_geometric_corrections_gpu(float *vis, int n_ant, int n_channels, i
 int bgi_apply_cable_lengths_corrections_gpu(float *vis, int n_ant, int n_channels,
                                             int n_intervals, const double *cable_lengths,
                                             const double *freqs_hz, void *stream) {
+    TraceRange trace("bgi_apply_cable_lengths_corrections_gpu");
     if (!vis || !cable_lengths || !freqs_hz || n_ant < 1 || n_channels < 1 || n_intervals < 0)
         return set_error(BGI_ERR_INVALID, "apply_cable_lengths_corrections: bad arguments");
     if (!aligned16(vis)) return set_error(BGI_ERR_INVALID, "apply_cable_lengths_corrections: vis must be 16-byte aligned");
@@ -308,6 +312,7 @@ int bgi_gridding_gpu(const float *vis, int n_ant, int n_channels, int n_interval
                      double delta_v, int n_pixels, double min_uv, int pol, int counter_mode,
                      float *counters, float *grids, void *stream) {
     (void)antenna_weights;
+    TraceRange trace("bgi_gridding_gpu");
     GridParams p;
     BGI_TRY(gridding_params("gridding", vis, n_ant, n_channels, n_intervals, u, v, n_uvw_sets, baseline_flags,
                             freqs_hz, delta_u, delta_v, n_pixels, min_uv, pol, counter_mode, counters, grids, &p));
@@ -326,6 +331,7 @@ int bgi_gridding_sorted_gpu(const float *vis, int n_ant, int n_channels, int n_i
                             const double *freqs_hz, double delta_u, double delta_v, int n_pixels,
                             double min_uv, int pol, int counter_mode, float *counters, float *grids,
                             void *workspace, size_t workspace_bytes, void *stream) {
+    TraceRange trace("bgi_gridding_sorted_gpu");
     if (n_ant > kSortedMaxAnt)
         return set_error(BGI_ERR_INVALID, "gridding_sorted: at most %d antennas", kSortedMaxAnt);
     if (!workspace || !aligned16(workspace))
@@ -339,6 +345,7 @@ int bgi_gridding_sorted_gpu(const float *vis, int n_ant, int n_channels, int n_i
 
 int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_images,
                         void *stream) {
+    TraceRange trace("bgi_fft_inverse_gpu");
     if (!grids || !images || n_images < 0) return set_error(BGI_ERR_INVALID, "fft_inverse: bad arguments");
     if (!fft_size_supported(n_pixels))
         return set_error(BGI_ERR_UNSUPPORTED, "fft_inverse: image side %d (powers of two 16..4096)", n_pixels);
@@ -352,6 +359,7 @@ int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_i
 
 int bgi_fft_shift_and_norm_gpu(float *images, int x_side, int y_side, int n_images,
                                const float *fnorm, int fnorm_size, void *stream) {
+    TraceRange trace("bgi_fft_shift_and_norm_gpu");
     if (x_side % 2 != 0)  // src/gpu/gpu_utils.cpp:129-131
         return set_error(BGI_ERR_INVALID, "fft_shift_and_norm: only even image size is handled");
     if (!images || !fnorm || fnorm_size < 1 || x_side < 0 || y_side < 0 || n_images < 0)
