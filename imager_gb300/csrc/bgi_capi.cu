@@ -135,6 +135,17 @@ struct bgi_imager {
         const double vp = v_max * freq_max / (kVelLight * delta_v);
         return up < cfg.n_pixels - 1 && vp < cfg.n_pixels - 1;
     }
+    // Bound on the pixel coordinates |u|, |v| of every gridded point, for pruning the half-plane
+    // column pass: rounding u_max * nu_max / (c * delta_u) reaches at most its floor + 1; one more
+    // pixel of margin.  N/2 (no pruning) when the bound reaches the half plane's edge, where the
+    // cell indices wrap.
+    void half_plane_extent(int *eu, int *ev) const {
+        const int h = cfg.n_pixels / 2;
+        const double up = u_max * freq_max / (kVelLight * delta_u);
+        const double vp = v_max * freq_max / (kVelLight * delta_v);
+        *eu = up + 2.0 < h ? (int)up + 2 : h;
+        *ev = vp + 2.0 < h ? (int)vp + 2 : h;
+    }
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
     DevBuf<ChannelConst> d_cc; // per-channel gridding constants for the current delta_u/v
@@ -744,7 +755,9 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
             BGI_TRY(launch_gridding(p, ls));
         BGI_TRY(im->mark(ls));
         if (p.half_width > 0) {
-            BGI_TRY(launch_fft_cols_half(grid, n, cnt, ls));                   // in place, rows shifted
+            int eu, ev;
+            im->half_plane_extent(&eu, &ev);
+            BGI_TRY(launch_fft_cols_half(grid, n, cnt, eu, ev, ls));           // in place, rows shifted
             BGI_TRY(im->mark(ls));
             BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, ls, real));  // clears the scratch
         } else {

@@ -448,19 +448,24 @@ constexpr int half_width_of() {
 
 // Column pass of half-plane grids [img][N][W], in place: tiles of COLS adjacent columns, lanes
 // across the columns (coalesced row segments), transforms stepping together (block barriers);
-// row y is stored at (y + N/2) mod N, the fftshift of rows.
+// row y is stored at (y + N/2) mod N, the fftshift of rows.  Pruned by the uv coverage: the
+// launch covers the first `tiles` tiles of each image (the columns beyond are zero, and so are
+// their transforms), and rows ext_v < y < N - ext_v, which hold no gridded value, read as zero
+// without a load.
 template <int N>
-__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_half_kernel(float2 *grids) {
+__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_half_kernel(float2 *grids, int tiles,
+                                                                                        int ext_v) {
     using S = ColShape<N>;
-    constexpr int COLS = S::COLS, W = half_width_of<N>(), TILES = W / COLS;
+    constexpr int COLS = S::COLS, W = half_width_of<N>();
     extern __shared__ float2 smem[];
     const float2 *tw = twiddles<N, S::R>();
-    const size_t img = blockIdx.x / TILES;
-    const int x0 = (blockIdx.x % TILES) * COLS;
+    const size_t img = blockIdx.x / tiles;
+    const int x0 = (blockIdx.x % tiles) * COLS;
     const int c = threadIdx.x % COLS, t = threadIdx.x / COLS;
     float2 *g = grids + img * (size_t)N * W + x0 + c;
     fft_transform<N, S::R, false, false>(
-        t, smem + c * S::STRIDE, tw, [&](int i) { return g[(size_t)i * W]; },
+        t, smem + c * S::STRIDE, tw,
+        [&](int i) { return (i <= ext_v || i >= N - ext_v) ? g[(size_t)i * W] : make_float2(0.f, 0.f); },
         [&](int i, float2 v) { g[(size_t)((i + N / 2) & (N - 1)) * W] = v; });
 }
 
@@ -613,14 +618,18 @@ int cols_n(float2 *src, float2 *dst, int n_images, const unsigned int *wsum, boo
 }
 
 template <int N>
-int cols_half_n(float2 *grids, int n_images, cudaStream_t s) {
+int cols_half_n(float2 *grids, int n_images, int ext_u, int ext_v, cudaStream_t s) {
     using S = ColShape<N>;
+    constexpr int TILES = half_width_of<N>() / S::COLS;
+    const int eu = ext_u < 0 ? 0 : (ext_u > N / 2 ? N / 2 : ext_u);
+    const int ev = ext_v < 0 ? 0 : (ext_v > N / 2 ? N / 2 : ext_v);
+    const int tiles = std::min(TILES, eu / S::COLS + 1);  // tiles holding columns 0..eu
     const size_t smem = sizeof(float2) * ((size_t)S::COLS * S::STRIDE);
-    const unsigned blocks = (unsigned)((size_t)n_images * (half_width_of<N>() / S::COLS));
+    const unsigned blocks = (unsigned)((size_t)n_images * tiles);
     auto k = fft_cols_half_kernel<N>;
     int st = prepare(k, smem);
     if (st) return st;
-    k<<<blocks, S::COLS * S::P, smem, s>>>(grids);
+    k<<<blocks, S::COLS * S::P, smem, s>>>(grids, tiles, ev);
     return check_launch("fft cols (half plane)");
 }
 
@@ -754,16 +763,16 @@ int half_plane_width(int n) {
     }
 }
 
-int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s) {
+int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s) {
     if (n_images <= 0) return BGI_OK;
     switch (n) {
-        case 64: return cols_half_n<64>(grids, n_images, s);
-        case 128: return cols_half_n<128>(grids, n_images, s);
-        case 256: return cols_half_n<256>(grids, n_images, s);
-        case 512: return cols_half_n<512>(grids, n_images, s);
-        case 1024: return cols_half_n<1024>(grids, n_images, s);
-        case 2048: return cols_half_n<2048>(grids, n_images, s);
-        case 4096: return cols_half_n<4096>(grids, n_images, s);
+        case 64: return cols_half_n<64>(grids, n_images, ext_u, ext_v, s);
+        case 128: return cols_half_n<128>(grids, n_images, ext_u, ext_v, s);
+        case 256: return cols_half_n<256>(grids, n_images, ext_u, ext_v, s);
+        case 512: return cols_half_n<512>(grids, n_images, ext_u, ext_v, s);
+        case 1024: return cols_half_n<1024>(grids, n_images, ext_u, ext_v, s);
+        case 2048: return cols_half_n<2048>(grids, n_images, ext_u, ext_v, s);
+        case 4096: return cols_half_n<4096>(grids, n_images, ext_u, ext_v, s);
         default: return set_error(BGI_ERR_UNSUPPORTED, "half-plane image side %d", n);
     }
 }

@@ -104,8 +104,11 @@ int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsi
 // Half-plane imaging (real images of Hermitian grids): grids [img][N][W] hold columns
 // u = 0..N/2 (W = half_plane_width(N), padding columns stay zero).
 int half_plane_width(int n);
-// Column pass in place on half-plane grids, storing row y at (y + N/2) mod N.
-int launch_fft_cols_half(float2 *grids, int n, int n_images, cudaStream_t s);
+// Column pass in place on half-plane grids, storing row y at (y + N/2) mod N.  Only columns
+// 0..ext_u and rows 0..ext_v, N-ext_v..N-1 may hold gridded values (the caller's bound on the
+// pixel coordinates; N/2 for no bound): the columns beyond are left as they are (zero, so their
+// transforms are zero) and the rows between read as zero.
+int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s);
 // Complex-to-real row pass: half-plane rows -> image rows (fftshift of columns and
 // (float)(1/wsum) applied), clearing the grid rows it read.  Images are complex with zero
 // imaginary parts and must be 16-byte aligned.

@@ -410,6 +410,33 @@ def test_half_plane_falls_back_when_pixels_reach_the_side(im):
     h.close()
 
 
+@pytest.mark.parametrize("n,extent", [(64, 10.5), (64, 11.0 - 1e-9), (64, 11.0 + 1e-9), (64, 27.5), (64, 29.5),
+                                      (64, 30.0), (64, 31.5), (512, 109.5), (512, 110.5), (512, 126.0 - 1e-9),
+                                      (512, 253.5)])
+def test_half_plane_pruning_at_the_coverage_edge(im, n, extent):
+    """The half-plane column pass transforms only the columns and loads only the rows that the
+    uv coverage can reach: |pixel| <= floor(u_max * nu_max / (c * delta_u)) + 2, N/2 when that
+    reaches the half plane's edge.  With delta_u = osf * u_max / N the longest baselines at the
+    top frequency land on pixel round(N * nu_max / (c * osf)); the top frequency is chosen so
+    that this coordinate is a tie, just below or just above an integer, or near N/2, and the
+    images must still match the oracle (one baseline lost would move them by about 1e-1)."""
+    osf = 2.0
+    f_top = extent * C_LIGHT * osf / n
+    obs = synth.small(seed=53, n_ant=24, n_intervals=2, n_channels=3, n_pixels=n, f0=f_top - 2e6, df=1e6)
+    assert abs(obs.freqs.max() - f_top) < 1e-3
+    vis = obs.vis_f32()
+    _, _, counters, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n,
+                                             osf=osf, n_uvw_sets=2)
+    h = _imager_for(im, obs, n)
+    assert h.half_plane
+    out = h.image(dev(vis)).cpu().numpy()
+    for i in range(2):
+        for j in range(3):
+            assert rel_l2(out[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+    assert np.array_equal(h.weight_sums(6), counters.reshape(6, -1).sum(1).astype(np.uint32))
+    h.close()
+
+
 def test_negative_flag_keeps_blocks_off_the_half_plane(im):
     """A baseline flag below zero is gridded (the GPU gridder's flags <= 0, as
     src/gpu/gridding_gpu.cpp:101) but u_max / v_max cover flag 0 only
