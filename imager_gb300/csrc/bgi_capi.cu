@@ -759,7 +759,7 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
             im->half_plane_extent(&eu, &ev);
             BGI_TRY(launch_fft_cols_half(grid, n, cnt, eu, ev, ls));           // in place, rows shifted
             BGI_TRY(im->mark(ls));
-            BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, ls, real));  // clears the scratch
+            BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, eu, ls, real));  // clears the scratch
         } else {
             BGI_TRY(launch_fft_rows(grid, grid, n, cnt, false, ls));  // in place in the scratch
             BGI_TRY(im->mark(ls));

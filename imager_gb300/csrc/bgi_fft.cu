@@ -487,9 +487,11 @@ struct C2RShape {
 };
 
 // Complex-to-real pass: half-plane row y (already at its fftshifted position) -> image row y.
-// One thread stages the block's rows (N/2 + 1 values each, rounded up to 16 bytes) in shared
-// memory with bulk asynchronous copies completing on an mbarrier, then clears them in the grid
-// with bulk stores from a zero row once they have landed; the first pass forms Z[k] from X[k]
+// One thread stages the block's rows in shared memory with bulk asynchronous copies completing
+// on an mbarrier, then clears them in the grid with bulk stores from a zero row once they have
+// landed.  Only the first copy_bytes of a row (the columns the uv coverage reaches, rounded up
+// to 16 bytes; at most N/2 + 1 values rounded up) are copied and cleared: the rest of the row is
+// zero in the grid and is zeroed in the row buffer instead.  The first pass forms Z[k] from X[k]
 // and X[M-k]; the stores apply the fftshift of columns (x -> (x + N/2) mod N keeps pairs
 // 2m, 2m+1 together) and (float)(1/sum(w)), and write each pair of complex pixels (zero
 // imaginary parts) as one 16-byte store streaming past L2: two 8-byte stores would each
@@ -516,7 +518,8 @@ constexpr size_t c2r_smem_bytes() {
 
 template <int N, bool REAL>
 __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
-                                                                                    const unsigned int *wsum) {
+                                                                                    const unsigned int *wsum,
+                                                                                    unsigned copy_bytes) {
     using S = C2RShape<N>;
     constexpr int M = S::M, W = half_width_of<N>();
     constexpr unsigned ROW_BYTES = c2r_row_bytes<N>();
@@ -541,13 +544,19 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     }
     for (int i = threadIdx.x; i < (int)(ROW_BYTES / 16); i += blockDim.x)
         reinterpret_cast<float4 *>(zeros)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    {  // the part of each row buffer that no copy fills
+        constexpr int Q = (int)(ROW_BYTES / 16);
+        const int q0 = (int)(copy_bytes / 16), tail = Q - q0;
+        for (int i = threadIdx.x; i < S::ROWS * tail; i += blockDim.x)
+            reinterpret_cast<float4 *>(smem + (i / tail) * S::BUF)[q0 + i % tail] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_arrive_expect_tx(bar, S::ROWS * ROW_BYTES + TW_BYTES + WZ_BYTES);
+        mbar_arrive_expect_tx(bar, S::ROWS * copy_bytes + TW_BYTES + WZ_BYTES);
         bulk_load(tw, twiddles<M, S::R>(), TW_BYTES, bar);
         bulk_load(wz, g_z_twiddles<N>.v, WZ_BYTES, bar);
-        for (int r = 0; r < S::ROWS; ++r) bulk_load(smem + r * S::BUF, grids + (row0 + r) * W, ROW_BYTES, bar);
+        for (int r = 0; r < S::ROWS; ++r) bulk_load(smem + r * S::BUF, grids + (row0 + r) * W, copy_bytes, bar);
         // one FP64 reciprocal per block (all its rows are one image's), while the copies fly
         *s_scale = (float)(1.0 / (double)wsum[(row0 / N) * kWsumStride]);
     }
@@ -556,7 +565,7 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
         return;
     }
     if (threadIdx.x == 0) {  // the rows have been read: clear them for the next wave
-        for (int r = 0; r < S::ROWS; ++r) bulk_store(grids + (row0 + r) * W, zeros, ROW_BYTES);
+        for (int r = 0; r < S::ROWS; ++r) bulk_store(grids + (row0 + r) * W, zeros, copy_bytes);
         bulk_commit();
     }
     const float scale = *s_scale;
@@ -634,14 +643,18 @@ int cols_half_n(float2 *grids, int n_images, int ext_u, int ext_v, cudaStream_t 
 }
 
 template <int N>
-int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, bool real, cudaStream_t s) {
+int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, int ext_u, bool real,
+          cudaStream_t s) {
     using S = C2RShape<N>;
     const size_t smem = c2r_smem_bytes<N>();
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
+    // columns 0..ext_u, rounded up to 16 bytes: a multiple of 16 no larger than the staged row
+    const int eu = ext_u < 0 ? 0 : (ext_u > N / 2 ? N / 2 : ext_u);
+    const unsigned copy_bytes = std::min(c2r_row_bytes<N>(), (unsigned)(((eu + 1) * sizeof(float2) + 15) & ~(size_t)15));
     auto k = real ? c2r_rows_kernel<N, true> : c2r_rows_kernel<N, false>;
     int st = prepare(k, smem);
     if (st) return st;
-    k<<<blocks, S::ROWS * S::P, smem, s>>>(grids, images, wsum);
+    k<<<blocks, S::ROWS * S::P, smem, s>>>(grids, images, wsum, copy_bytes);
     return check_launch("fft rows (complex to real)");
 }
 
@@ -777,17 +790,17 @@ int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_
     }
 }
 
-int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
+int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum, int ext_u,
                     cudaStream_t s, bool real) {
     if (n_images <= 0) return BGI_OK;
     switch (n) {
-        case 64: return c2r_n<64>(grids, images, n_images, wsum, real, s);
-        case 128: return c2r_n<128>(grids, images, n_images, wsum, real, s);
-        case 256: return c2r_n<256>(grids, images, n_images, wsum, real, s);
-        case 512: return c2r_n<512>(grids, images, n_images, wsum, real, s);
-        case 1024: return c2r_n<1024>(grids, images, n_images, wsum, real, s);
-        case 2048: return c2r_n<2048>(grids, images, n_images, wsum, real, s);
-        case 4096: return c2r_n<4096>(grids, images, n_images, wsum, real, s);
+        case 64: return c2r_n<64>(grids, images, n_images, wsum, ext_u, real, s);
+        case 128: return c2r_n<128>(grids, images, n_images, wsum, ext_u, real, s);
+        case 256: return c2r_n<256>(grids, images, n_images, wsum, ext_u, real, s);
+        case 512: return c2r_n<512>(grids, images, n_images, wsum, ext_u, real, s);
+        case 1024: return c2r_n<1024>(grids, images, n_images, wsum, ext_u, real, s);
+        case 2048: return c2r_n<2048>(grids, images, n_images, wsum, ext_u, real, s);
+        case 4096: return c2r_n<4096>(grids, images, n_images, wsum, ext_u, real, s);
         default: return set_error(BGI_ERR_UNSUPPORTED, "half-plane image side %d", n);
     }
 }

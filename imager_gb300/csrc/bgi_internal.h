@@ -111,9 +111,10 @@ int half_plane_width(int n);
 int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s);
 // Complex-to-real row pass: half-plane rows -> image rows (fftshift of columns and
 // (float)(1/wsum) applied), clearing the grid rows it read.  Images are complex with zero
-// imaginary parts and must be 16-byte aligned.
+// imaginary parts and must be 16-byte aligned.  Columns beyond ext_u are zero in the grid (the
+// bound of launch_fft_cols_half; N/2 for none): they are neither read nor cleared.
 // real: images are float[N][N] (8-byte aligned) instead of complex.
-int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum,
+int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum, int ext_u,
                     cudaStream_t s, bool real = false);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
                           const float *fnorm, int fnorm_size, cudaStream_t s);
