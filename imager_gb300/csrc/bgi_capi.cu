@@ -158,12 +158,12 @@ struct bgi_imager {
     // alternate waves, each with its own grid scratch, so one wave's
     // FFT passes overlap the next wave's gridding; the scratch of a lane is reused wave after
     // wave and sized to stay in L2.
-    static constexpr int kLanes = 4;  // at most; `lanes` are in use (bgi_set_schedule, bgi_autotune)
+    static constexpr int kLanes = 8;  // at most; `lanes` are in use (bgi_set_schedule, bgi_autotune)
     int lanes = 2;
     DevBuf<float2> grid[kLanes];  // wave scratch: images x N*N, zero between waves
-    bool grid_dirty[kLanes] = {false, false, false, false};
-    cudaStream_t lane[kLanes] = {nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {nullptr, nullptr, nullptr, nullptr};
+    bool grid_dirty[kLanes] = {};
+    cudaStream_t lane[kLanes] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {};
     // Deterministic mode: gridding by sort and ordered per-cell sums (full plane), with a
     // workspace per lane for one wave.
     bool deterministic = false;
@@ -799,7 +799,8 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     GridParams p = block_params(im, vis, n_intervals, flags, images, format, scales);
     BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
     p.chan_consts = im->d_cc.ptr;
-    cudaStream_t streams[bgi_imager::kLanes] = {s, s, s, s};
+    cudaStream_t streams[bgi_imager::kLanes];
+    std::fill(streams, streams + bgi_imager::kLanes, s);
     if (n_lanes > 1) {
         BGI_TRY(im->ensure_lanes());
         BGI_TRY(check_cuda(cudaEventRecord(im->ev_fork, s), "fork record"));

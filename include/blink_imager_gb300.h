@@ -345,9 +345,9 @@ BGI_API int bgi_device_fault(int device, unsigned int *fault_bits, int clear);
 BGI_API int bgi_selftest_wait_timeout(int device, void *stream);
 
 /* Launch schedule of the bgi_image* calls: images per wave (0 = auto: about 26 MiB of grid
- * per lane, 24 half-plane images at 512^2) and lanes (1..4 streams that image alternate waves,
+ * per lane, 24 half-plane images at 512^2) and lanes (1..8 streams that image alternate waves,
  * each with its own grid scratch; 2 by default).  bgi_autotune times every wave size in
- * {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to the block's image count) with 1-4
+ * {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to the block's image count) with 1-8
  * lanes on the caller's own block (4 calls each: one to size the scratch, three timed with CUDA
  * events on the stream), keeps the fastest on the handle, frees the candidates' scratch and
  * writes the best milliseconds per call to *best_ms (may be NULL).  Synchronous; `images`

@@ -496,16 +496,16 @@ def test_schedule_and_autotune(im):
     h = _imager_for(im, obs, n, "XX")
     h.set_deterministic(True)
     ref = h.image(vis).cpu().numpy()
-    for wave, lanes in ((1, 1), (5, 3), (12, 4), (0, 2)):
+    for wave, lanes in ((1, 1), (5, 3), (12, 4), (1, 8), (0, 2)):
         h.set_schedule(wave, lanes)
         assert h.schedule == (wave, lanes)
         out = h.image(vis).cpu().numpy()
         assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), (wave, lanes)
     with pytest.raises(capi.BgiError):
-        h.set_schedule(8, 5)
+        h.set_schedule(8, 9)
     h.set_deterministic(False)
     wave, lanes, ms = h.autotune(vis)
-    assert wave in (0, 4, 8, 12) and 1 <= lanes <= 4 and ms > 0
+    assert wave in (0, 4, 8, 12) and 1 <= lanes <= 8 and ms > 0
     assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6
     h.close()
 
