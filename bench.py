@@ -767,9 +767,14 @@ def run_ours(args, rank, world, local_rank):
     # for the 16-bit formats the one pol plane XX needs and its block scales
     vis_bytes = B * 32 if fmt == "c64" else B * 4 + int(stored[fmt][1].shape[-1]) * 4
     half = im.half_plane
+    ext_u, ext_v = im.uv_extent
     if half:
-        hw = N * (N // 2 + 1) * 8  # half-plane grid of one image
-        alg = {"gridding": vis_bytes + hw, "fft_pass1": 2 * hw, "fft_pass2": hw + 8 * N * N}
+        # the half-plane passes are pruned to the uv coverage: columns 0..ext_u, rows within
+        # ext_v of row 0; gridding writes that region, the column pass reads its rows and writes
+        # every row of its columns, the complex-to-real pass reads those columns of every row
+        cols, rows_in = ext_u + 1, min(N, 2 * ext_v + 1)
+        alg = {"gridding": vis_bytes + 8 * cols * rows_in, "fft_pass1": 8 * cols * (rows_in + N),
+               "fft_pass2": 8 * cols * N + 8 * N * N}
         kernel_names = {"gridding": "grid_kernel", "fft_pass1": "fft_cols_half_kernel", "fft_pass2": "c2r_rows_kernel"}
     else:
         alg = {"gridding": vis_bytes + 8 * N * N, "fft_pass1": 16 * N * N, "fft_pass2": 16 * N * N}
@@ -808,7 +813,8 @@ def run_ours(args, rank, world, local_rank):
             "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
             "traffic": traffic,
             "algorithmic_bytes_per_image": alg[dom],
-            "path": "half plane (complex-to-real)" if half else "full plane", "step": step_roof}
+            "path": "half plane (complex-to-real)" if half else "full plane",
+            "uv_extent_pixels": [ext_u, ext_v], "step": step_roof}
 
     cpu_rate, cpu_times, cpu_threads = cpu_sample_rate(obs, 16, args.cpu_seconds)
     d2h = n_images * N * N * 8

@@ -626,6 +626,15 @@ int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, doub
     return BGI_OK;
 }
 
+int bgi_get_uv_extent(const bgi_imager *im, int *ext_u, int *ext_v) {
+    if (!im || !ext_u || !ext_v) return set_error(BGI_ERR_INVALID, "get_uv_extent: bad arguments");
+    if (im->n_ant == 0 || im->n_channels == 0)
+        return set_error(BGI_ERR_STATE, "get_uv_extent: set_array and set_frequencies first");
+    if (im->half_plane()) im->half_plane_extent(ext_u, ext_v);
+    else *ext_u = *ext_v = im->cfg.n_pixels / 2;
+    return BGI_OK;
+}
+
 static int image_checks(bgi_imager *im, int n_intervals, unsigned flags) {
     if (!im) return set_error(BGI_ERR_INVALID, "image: null handle");
     if (im->n_ant == 0 || im->n_channels == 0)

@@ -275,6 +275,14 @@ class Imager:
         call("bgi_get_uv_cell", self._h, C.byref(du), C.byref(dv), C.byref(um), C.byref(vm))
         return du.value, dv.value, um.value, vm.value
 
+    @property
+    def uv_extent(self):
+        """(ext_u, ext_v): bound on the |u|, |v| pixel coordinates of every gridded point; the
+        half-plane FFT passes skip the grid beyond it (n_pixels/2 each on the full plane)."""
+        eu, ev = C.c_int(), C.c_int()
+        call("bgi_get_uv_extent", self._h, C.byref(eu), C.byref(ev))
+        return eu.value, ev.value
+
     def image(self, vis: torch.Tensor, flags: int = APPLY_GEOMETRIC | APPLY_CABLE, out=None,
               stream=None) -> torch.Tensor:
         """Dirty images complex64 [T][C][N][N] of device visibilities."""

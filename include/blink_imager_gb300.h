@@ -222,6 +222,14 @@ BGI_API int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v);
 BGI_API int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, double *u_max,
                     double *v_max);
 
+/* Bound on the pixel coordinates |u| and |v| of every point the half-plane path grids for the
+ * current array, frequencies and uv cell: floor(u_max * nu_max / (c * delta_u)) + 2, and the
+ * same in v, capped at N/2 (no addition of the reference; with delta_u = osf * u_max / N it is
+ * about N * nu_max / (c * osf)).  The half-plane FFT passes transform and stage only columns
+ * 0..ext_u and load only rows 0..ext_v and N-ext_v..N-1: the rest of the grid is zero.  N/2 in
+ * both when bgi_half_plane is 0. */
+BGI_API int bgi_get_uv_extent(const bgi_imager *im, int *ext_u, int *ext_v);
+
 /* Pointed-observation UVW on the device (CAntennaPositions::CalculateUVW with metadata,
  * src/antenna_positions.cpp:23-92; PacerGeometry::CalcUVW_NEW, precXYZ and CalcUVW,
  * src/pacer_geometry.h).  A timestep is what the reference derives once per timestep with PAL

@@ -402,6 +402,7 @@ def test_half_plane_falls_back_when_pixels_reach_the_side(im):
     h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
     h.set_frequencies(obs.freqs)
     assert not h.half_plane
+    assert h.uv_extent == (32, 32)
     out = h.image(dev(obs.vis_f32())).cpu().numpy()
     _, _, _, ref, _ = O.full_pipeline(obs.vis_f32(), obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, 64,
                                       osf=1.0)
@@ -429,6 +430,21 @@ def test_half_plane_pruning_at_the_coverage_edge(im, n, extent):
                                              osf=osf, n_uvw_sets=2)
     h = _imager_for(im, obs, n)
     assert h.half_plane
+    du, dv, um, vm = h.uv_cell
+    fmax = float(obs.freqs.max())
+
+    def bound(m, d):  # the handle's bound, in the same FP64 operations
+        x = m * fmax / (C_LIGHT * d)
+        return math.floor(x) + 2 if x + 2.0 < n // 2 else n // 2
+
+    assert h.uv_extent == (bound(um, du), bound(vm, dv))
+    # every gridded point's pixel coordinate (the reference's rounding) lies within the bound,
+    # which is at most two pixels loose
+    lam = C_LIGHT / obs.freqs
+    for coord, d, b in ((obs.u, du, h.uv_extent[0]), (obs.v, dv, h.uv_extent[1])):
+        x = (coord[:, obs.flags <= 0][:, None, :].astype(np.float64) / lam[None, :, None]) / d
+        top = np.floor(np.abs(x) + 0.5).max()
+        assert top <= b and (b == n // 2 or top >= b - 2), (top, b)
     out = h.image(dev(vis)).cpu().numpy()
     for i in range(2):
         for j in range(3):
