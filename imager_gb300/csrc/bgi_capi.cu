@@ -135,6 +135,9 @@ struct bgi_imager {
         const double vp = v_max * freq_max / (kVelLight * delta_v);
         return up < cfg.n_pixels - 1 && vp < cfg.n_pixels - 1;
     }
+    // Whether bgi_image grids the half plane (images 16-byte aligned): the exactness condition
+    // above, and neither the ordered gridder nor a convolution kernel (both full plane).
+    bool half_plane_path() const { return half_plane() && !deterministic && kb_size == 0; }
     // Bound on the pixel coordinates |u|, |v| of every gridded point, for pruning the half-plane
     // column pass: rounding u_max * nu_max / (c * delta_u) reaches at most its floor + 1; one more
     // pixel of margin.  N/2 (no pruning) when the bound reaches the half plane's edge, where the
@@ -587,7 +590,7 @@ int bgi_half_plane(const bgi_imager *im) {
     if (!im) return set_error(BGI_ERR_INVALID, "half_plane: null handle");
     if (im->n_ant == 0 || im->n_channels == 0)
         return set_error(BGI_ERR_STATE, "half_plane: set_array and set_frequencies first");
-    return im->half_plane() ? 1 : 0;
+    return im->half_plane_path() ? 1 : 0;
 }
 
 int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v) {
@@ -630,7 +633,7 @@ int bgi_get_uv_extent(const bgi_imager *im, int *ext_u, int *ext_v) {
     if (!im || !ext_u || !ext_v) return set_error(BGI_ERR_INVALID, "get_uv_extent: bad arguments");
     if (im->n_ant == 0 || im->n_channels == 0)
         return set_error(BGI_ERR_STATE, "get_uv_extent: set_array and set_frequencies first");
-    if (im->half_plane()) im->half_plane_extent(ext_u, ext_v);
+    if (im->half_plane_path()) im->half_plane_extent(ext_u, ext_v);
     else *ext_u = *ext_v = im->cfg.n_pixels / 2;
     return BGI_OK;
 }
@@ -717,7 +720,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.n_pixels = im->cfg.n_pixels;
     p.pol = im->cfg.pol;
     p.counter_mode = -1;
-    p.half_width = im->half_plane() && !im->deterministic && im->kb_size == 0 ? half_plane_width(im->cfg.n_pixels) : 0;
+    p.half_width = im->half_plane_path() ? half_plane_width(im->cfg.n_pixels) : 0;
     p.kb_size = im->kb_size;
     p.kb_table = im->kb_table.ptr;
     // the complex-to-real pass stores pixel pairs: 16 bytes of complex or 8 bytes of real pixels

@@ -210,7 +210,9 @@ BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float
 BGI_API int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz);
 
 /* 1 when bgi_image would take the half-plane path for the current array, frequencies and
- * configuration, 0 when it would transform the full plane; negative status on error. */
+ * configuration (16-byte aligned complex images; not with bgi_set_deterministic or a
+ * convolution kernel, which grid the full plane), 0 when it would transform the full plane;
+ * negative status on error. */
 BGI_API int bgi_half_plane(const bgi_imager *im);
 
 /* Overrides delta_u and delta_v (metres) of the current array state, e.g. with the values of

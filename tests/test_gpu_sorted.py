@@ -171,7 +171,10 @@ def test_deterministic_imager(im):
         h = im.Imager(n, 2.0, "I", -1000.0, max_images_per_wave=wave)
         h.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
         h.set_frequencies(obs.freqs)
+        assert h.half_plane
         h.set_deterministic(True)
+        # the ordered gridder grids the full plane, which is not pruned
+        assert not h.half_plane and h.uv_extent == (n // 2, n // 2)
         a = h.image(dev(vis)).cpu().numpy()
         b = h.image(dev(vis)).cpu().numpy()
         assert np.array_equal(_bits(a), _bits(b))
