@@ -92,6 +92,7 @@ _SIGNATURES = {
     "bgi_set_uv_cell": (_i, [_vp, _d, _d]),
     "bgi_get_uv_cell": (_i, [_vp, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     "bgi_get_uv_extent": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
+    "bgi_uv_extent": (_i, [_d, _d, _d, _d, _d, _i, C.POINTER(_i), C.POINTER(_i)]),
     "bgi_image": (_i, [_vp, _vp, _i, _u, _vp, _vp]),
     "bgi_image_host": (_i, [_vp, _vp, _i, _u, _vp, _vp]),
     "bgi_last_weight_sums": (_i, [_vp, _vp, _i, _vp]),

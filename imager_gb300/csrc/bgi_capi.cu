@@ -138,16 +138,10 @@ struct bgi_imager {
     // Whether bgi_image grids the half plane (images 16-byte aligned): the exactness condition
     // above, and neither the ordered gridder nor a convolution kernel (both full plane).
     bool half_plane_path() const { return half_plane() && !deterministic && kb_size == 0; }
-    // Bound on the pixel coordinates |u|, |v| of every gridded point, for pruning the half-plane
-    // column pass: rounding u_max * nu_max / (c * delta_u) reaches at most its floor + 1; one more
-    // pixel of margin.  N/2 (no pruning) when the bound reaches the half plane's edge, where the
-    // cell indices wrap.
+    // Bound on the pixel coordinates |u|, |v| of every gridded point (bgi_uv_extent), for
+    // pruning the half-plane FFT passes.
     void half_plane_extent(int *eu, int *ev) const {
-        const int h = cfg.n_pixels / 2;
-        const double up = u_max * freq_max / (kVelLight * delta_u);
-        const double vp = v_max * freq_max / (kVelLight * delta_v);
-        *eu = up + 2.0 < h ? (int)up + 2 : h;
-        *ev = vp + 2.0 < h ? (int)vp + 2 : h;
+        bgi_uv_extent(u_max, v_max, delta_u, delta_v, freq_max, cfg.n_pixels, eu, ev);
     }
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
@@ -626,6 +620,22 @@ int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta_v, doub
     if (delta_v) *delta_v = im->delta_v;
     if (u_max) *u_max = im->u_max;
     if (v_max) *v_max = im->v_max;
+    return BGI_OK;
+}
+
+// Rounding u_max * nu_max / (c * delta_u) (half away from zero) reaches at most its floor + 1;
+// one more pixel of margin covers the FP64 error of the quotient.  N/2 (no pruning) when the
+// bound reaches the half plane's edge, where the cell indices wrap.
+int bgi_uv_extent(double u_max, double v_max, double delta_u, double delta_v, double freq_max_hz,
+                  int n_pixels, int *ext_u, int *ext_v) {
+    if (!ext_u || !ext_v || n_pixels < 2 || !(delta_u > 0) || !(delta_v > 0) || !(u_max >= 0) ||
+        !(v_max >= 0) || !(freq_max_hz >= 0))
+        return set_error(BGI_ERR_INVALID, "uv_extent: bad arguments");
+    const int h = n_pixels / 2;
+    const double up = u_max * freq_max_hz / (kVelLight * delta_u);
+    const double vp = v_max * freq_max_hz / (kVelLight * delta_v);
+    *ext_u = up + 2.0 < h ? (int)up + 2 : h;
+    *ext_v = vp + 2.0 < h ? (int)vp + 2 : h;
     return BGI_OK;
 }
 

@@ -232,6 +232,11 @@ BGI_API int bgi_get_uv_cell(const bgi_imager *im, double *delta_u, double *delta
  * both when bgi_half_plane is 0. */
 BGI_API int bgi_get_uv_extent(const bgi_imager *im, int *ext_u, int *ext_v);
 
+/* The same bound for given values (host only, no handle): u_max, v_max and delta_u, delta_v in
+ * metres, the highest channel frequency in Hz, the image side. */
+BGI_API int bgi_uv_extent(double u_max, double v_max, double delta_u, double delta_v,
+                          double freq_max_hz, int n_pixels, int *ext_u, int *ext_v);
+
 /* Pointed-observation UVW on the device (CAntennaPositions::CalculateUVW with metadata,
  * src/antenna_positions.cpp:23-92; PacerGeometry::CalcUVW_NEW, precXYZ and CalcUVW,
  * src/pacer_geometry.h).  A timestep is what the reference derives once per timestep with PAL
