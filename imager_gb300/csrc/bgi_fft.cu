@@ -16,6 +16,11 @@
 //                partner at x + N/2, so shifted stores never race with another block's loads.
 //                In the fused path the stores apply the fftshift and the 1/sum(weights)
 //                normalisation (src/pacer_imager.cpp:171-179).
+//
+// The imager's default is the half-plane pair instead (real images of Hermitian grids): a
+// column pass over columns 0..N/2 in place, then a complex-to-real row pass into the images.
+// Both are pruned to the uv coverage: columns beyond the caller's bound are zero and skipped,
+// rows beyond it read as zero without a load.
 #include "bgi_async.cuh"
 #include "bgi_internal.h"
 
