@@ -141,7 +141,11 @@ struct bgi_imager {
     // Bound on the pixel coordinates |u|, |v| of every gridded point (bgi_uv_extent), for
     // pruning the half-plane FFT passes.
     void half_plane_extent(int *eu, int *ev) const {
-        bgi_uv_extent(u_max, v_max, delta_u, delta_v, freq_max, cfg.n_pixels, eu, ev);
+        int u = cfg.n_pixels / 2, v = cfg.n_pixels / 2;  // no pruning unless the bound is known
+        if (bgi_uv_extent(u_max, v_max, delta_u, delta_v, freq_max, cfg.n_pixels, &u, &v) != BGI_OK)
+            u = v = cfg.n_pixels / 2;
+        *eu = u;
+        *ev = v;
     }
     float *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
