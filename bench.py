@@ -249,11 +249,13 @@ def time_steps(step, k, stream, flush, pre=None):
     return timed_steps(step, k, stream, flush, pre) / k
 
 
-def plain_dropin_step(obs, vis, du, dv, out):
+def plain_dropin_step(obs, vis, du, dv, out, cufft=False):
     """The reference GPU imager's call sequence (src/gpu/pacer_imager_hip.cpp:36-146) through
     the free functions: corrections in place, grids and counters zeroed, atomic gridding with
     per-channel counters, unfused inverse FFT into the images, counter sums, fftshift and
-    normalisation -- FP32 and complex64 throughout, full plane, no fusion."""
+    normalisation -- FP32 and complex64 throughout, full plane, no fusion.  cufft: the FFT stage
+    is cuFFT (torch.fft.ifft2, unnormalised), as the reference's gpufftExecC2C call -- a timing
+    arm only; the product's FFT is its own."""
     import torch
     from imager_gb300 import capi
     from imager_gb300 import imager as IM
@@ -273,7 +275,10 @@ def plain_dropin_step(obs, vis, du, dv, out):
         counters.zero_()
         IM.gridding(work, u, v, flags, freqs, du, dv, N, -1000.0, "XX", grids, counters,
                     counter_mode=capi.COUNTERS_FIRST_INTERVAL, n_uvw_sets=T)
-        IM.fft_inverse(grids, out)
+        if cufft:
+            torch.fft.ifft2(grids, norm="forward", out=out)
+        else:
+            IM.fft_inverse(grids, out)
         IM.vector_sum(counters, N * N, Cn, fnorm)
         IM.fft_shift_and_norm(out, fnorm)
 
@@ -383,6 +388,8 @@ def serving_measure(args):
         st = sv.stats()
         res["poisson"] = {"mean_interarrival_ms": args.serve_interarrival_ms, "requests": st["completed"],
                           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                          "p99_note": "p99 over >= 1000 requests" if st["completed"] >= 1000 else
+                                      f"only {st['completed']} requests: p99 is close to the maximum",
                           "images_per_s": st["images_per_s"], "failed": st["failed"],
                           "client_latency_by_array": per_array()}
         # phase 2: closed loop, K outstanding per array
@@ -558,7 +565,24 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     capi.lib(build_if_missing=True)
-    obs = synth.config2(device="cuda", n_intervals=args.intervals)
+    whole_cell = None
+    if world == 1:
+        obs = synth.config2(device="cuda", n_intervals=args.intervals)
+    else:
+        # N GPUs: one observation of N blocks' intervals, split by the library's shard plan (each
+        # rank images its own intervals with the whole observation's uv cell; no collective on
+        # the data path) -- weak scaling, the same 64 x args.intervals images per GPU
+        import dataclasses
+        from imager_gb300 import shard as SH
+        whole = synth.config2(device="cuda", n_intervals=args.intervals * world)
+        probe = Imager(whole.n_pixels, 2.0, "XX", -1000.0)
+        probe.set_array(whole.u, whole.v, whole.w, whole.flags, whole.cable)
+        whole_cell = probe.uv_cell[:2]
+        probe.close()
+        part = SH.plan_shard(whole.n_intervals, whole.n_channels, world, rank)
+        vis_s, u_s, v_s, w_s, f_s = SH.shard_inputs(whole, part)
+        obs = dataclasses.replace(whole, vis=vis_s, u=u_s, v=v_s, w=w_s, freqs=f_s)
+        del whole
     T, Cn, B = obs.vis.shape[:3]
     N = obs.n_pixels
     n_images = T * Cn
@@ -572,6 +596,8 @@ def run_ours(args, rank, world, local_rank):
     im = Imager(N, 2.0, "XX", -1000.0, max_images_per_wave=args.wave)
     im.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
     im.set_frequencies(obs.freqs)
+    if whole_cell:
+        im.set_uv_cell(*whole_cell)
     flags = APPLY_GEOMETRIC | APPLY_CABLE
     stream = torch.cuda.current_stream()
 
@@ -643,6 +669,8 @@ def run_ours(args, rank, world, local_rank):
         full = Imager(N, 2.0, "XX", -1000.0, max_images_per_wave=args.wave, full_plane=True)
         full.set_array(obs.u, obs.v, obs.w, obs.flags, obs.cable)
         full.set_frequencies(obs.freqs)
+        if whole_cell:
+            full.set_uv_cell(*whole_cell)
         v_ms = time_steps(step_for(full, fmt), k, stream, flush)
         full.close()
         variants["full_plane_atomic_gridding"] = {"images_per_s": world * n_images / (v_ms / 1000.0),
@@ -665,6 +693,13 @@ def run_ours(args, rank, world, local_rank):
             "images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms, "steps": k,
             "what": "reference GPU call order through the free functions: corrections in place, gridding "
                     "with counters, unfused FFT, vector sum, fftshift+norm; complex64/FP32, full plane",
+            **({"errors_vs_fp64_interval0": image_errors(out, refs0)} if rank == 0 else {})}
+        plain_step, plain_fresh = plain_dropin_step(obs, vis, du, dv, out, cufft=True)
+        v_ms = time_steps(plain_step, k, stream, flush, pre=plain_fresh)
+        variants["plain_fp32_dropin_cufft"] = {
+            "images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms, "steps": k,
+            "what": "the same call order with the FFT stage done by cuFFT (torch.fft.ifft2, unnormalised) as "
+                    "the reference's gpufftExecC2C -- timing arm only, never in the product",
             **({"errors_vs_fp64_interval0": image_errors(out, refs0)} if rank == 0 else {})}
 
         # the reference's gridding call alone (bgi_gridding_gpu, gridding_gpu.cpp:130): complex64
@@ -704,36 +739,55 @@ def run_ours(args, rank, world, local_rank):
                     "written back)"}
         del cnt
 
-    # end to end through the host-buffer entry point: pinned input, pinned output
-    out_h = torch.empty((T, Cn, N, N), dtype=torch.complex64).pin_memory()
+    # end to end through the host-buffer entry points: pinned input, pinned output, the uploads
+    # and downloads inside the timed region.  The headline uploads the stored block (for the
+    # 16-bit formats only the XX plane and its scales) and downloads real images: XX images are
+    # real (BGI_OUTPUT_REAL stores the real part; the half-plane path makes no imaginary part).
+    # Beside it: complex images back (the reference's Images type), and the reference caller's
+    # own input -- complex64 records -- with real and with complex images back.
+    e2e_steps = max(3, min(args.steps, 20))
+
+    def e2e_time(fn):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(e2e_steps):
+            fn()
+        return (time.perf_counter() - t) / e2e_steps
+
+    out_hr = torch.empty((T, Cn, N, N), dtype=torch.float32).pin_memory()
+    vis_h = torch.from_numpy(vis_np).pin_memory()
+    h2d_c64 = vis_np.nbytes
     if fmt == "c64":
-        vis_h = torch.from_numpy(vis_np).pin_memory()
-        e2e_step = lambda: im.image_host(vis_h, flags=flags, out=out_h)  # noqa: E731
-        h2d = vis_np.nbytes
+        e2e_step = lambda: im.image_host(vis_h, flags=flags | IM.OUTPUT_REAL, out=out_hr)  # noqa: E731
+        h2d = h2d_c64
     else:
         d_h = stored[fmt][0].cpu().pin_memory()
         s_h = stored[fmt][1].cpu().pin_memory()
-        e2e_step = lambda: im.image_compressed_host(d_h, s_h, fmt, flags=flags, out=out_h)  # noqa: E731
+        e2e_step = lambda: im.image_compressed_host(d_h, s_h, fmt, flags=flags | IM.OUTPUT_REAL, out=out_hr)  # noqa: E731
         n_planes = 1  # pol XX reads one plane
         h2d = n_images * n_planes * (B * 4 + int(s_h.shape[-1]) * 4)
-    e2e_steps = max(3, min(args.steps, 20))
-    e2e_step()
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_s = (time.perf_counter() - t2) / e2e_steps
-    if args.variants:  # the same through the host entry point with real images coming back
-        out_hr = torch.empty((T, Cn, N, N), dtype=torch.float32).pin_memory()
-        e2e_real = (lambda: im.image_host(vis_h, flags=flags | IM.OUTPUT_REAL, out=out_hr)) if fmt == "c64" else \
-            (lambda: im.image_compressed_host(d_h, s_h, fmt, flags=flags | IM.OUTPUT_REAL, out=out_hr))
-        e2e_real()
-        t4 = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_real()
-        e2e_real_s = (time.perf_counter() - t4) / e2e_steps
-        variants["e2e_real_output"] = {"images_per_s": world * n_images / e2e_real_s, "h2d_bytes_per_step": h2d,
-                                       "d2h_bytes_per_step": n_images * N * N * 4}
+    e2e_s = e2e_time(e2e_step)
+    d2h_real, d2h_complex = n_images * N * N * 4, n_images * N * N * 8
+    e2e_variants = {}
+    if args.variants:
+        out_h = torch.empty((T, Cn, N, N), dtype=torch.complex64).pin_memory()
+        cplx = (lambda: im.image_host(vis_h, flags=flags, out=out_h)) if fmt == "c64" else \
+            (lambda: im.image_compressed_host(d_h, s_h, fmt, flags=flags, out=out_h))
+        e2e_variants[f"{fmt}_input_complex_output"] = {
+            "images_per_s": world * n_images / e2e_time(cplx), "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h_complex}
+        if fmt != "c64":
+            e2e_variants["c64_input_real_output"] = {
+                "images_per_s": world * n_images / e2e_time(lambda: im.image_host(vis_h, flags=flags | IM.OUTPUT_REAL,
+                                                                                  out=out_hr)),
+                "h2d_bytes_per_step": h2d_c64, "d2h_bytes_per_step": d2h_real,
+                "what": "the reference caller's complex64 records uploaded whole (4 pols, 32 B per baseline)"}
+            e2e_variants["c64_input_complex_output"] = {
+                "images_per_s": world * n_images / e2e_time(lambda: im.image_host(vis_h, flags=flags, out=out_h)),
+                "h2d_bytes_per_step": h2d_c64, "d2h_bytes_per_step": d2h_complex,
+                "what": "the reference caller's input and output types end to end"}
+        del out_h
     t3 = time.monotonic()
     clocks.stop()
     if dist:
@@ -819,27 +873,35 @@ def run_ours(args, rank, world, local_rank):
     cpu_rate, cpu_times, cpu_threads = cpu_sample_rate(obs, 16, args.cpu_seconds)
     d2h = n_images * N * N * 8
     plain = variants.get("plain_fp32_dropin", {}).get("images_per_s")
+    plain_cufft = variants.get("plain_fp32_dropin_cufft", {}).get("images_per_s")
     line = {
         "metric": METRIC, "value": images_per_s, "unit": "images/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 arithmetic" + ("" if fmt == "c64" else f", {fmt} storage"),
         "storage": {"c64": "complex64 (the reference's layout)",
                     "s16": "16-bit block floating point: int16 pol planes, one FP32 scale per 128 baselines",
                     "bf16": "bfloat16 pol planes, one FP32 scale per 128 baselines",
                     "fp16": "binary16 pol planes, one FP32 scale per 128 baselines"}[fmt],
         "vs_plain_fp32_dropin": images_per_s / plain if plain else None,
+        "vs_plain_fp32_dropin_cufft": images_per_s / plain_cufft if plain_cufft else None,
         "data": "synthetic (seeded; shapes and distributions of the workload)",
         "config": {"workload": WORKLOAD if T == 10 else WORKLOAD.replace("10 intervals", f"{T} intervals"),
                    "images_per_step": n_images, "n_pixels": N, "baselines": B,
                    "schedule": {"images_per_wave": im.schedule[0] or "auto", "lanes": im.schedule[1],
                                 "chosen_by": "bgi_autotune on this block" if tuned else "default"},
                    "l2": "flushed before every timed step (512 MB written outside the step's events)",
+                   "storage": fmt,
                    "bytes_per_step": {"stored_visibilities_read": n_images * vis_bytes, "images_written": d2h},
-                   "parallelism": "one block per GPU, no collective" if world > 1 else "single GPU"},
+                   "parallelism": (f"one observation of {world} blocks sharded by interval "
+                                   "(imager_gb300.shard.plan_shard, whole-observation uv cell), no collective")
+                                  if world > 1 else "single GPU"},
         "vis_per_s": world * gridded_vis * args.steps / (ms / 1000.0),
         "e2e": {"value": world * n_images / e2e_s, "unit": "images/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h,
-                "api": ("bgi_image_host" if fmt == "c64" else "bgi_image_compressed_host") + " (pinned host buffers)"},
+                "d2h_bytes_per_step": d2h_real,
+                "api": ("bgi_image_host" if fmt == "c64" else "bgi_image_compressed_host") +
+                       " with BGI_OUTPUT_REAL (pinned host buffers; XX images are real)",
+                "variants": e2e_variants},
         "roofline": roof,
         "stages": stage_info,
         "cpu_baseline": {"value": cpu_rate, "unit": "images/s", "cores": cpu_threads, "kind": "port",
@@ -878,7 +940,8 @@ def main():
     ap.add_argument("--no-batched", dest="batched", action="store_false", help="skip the uneven-batch measurement")
     ap.add_argument("--no-precision", dest="precision", action="store_false",
                     help="skip the precision-form measurement (768 channels x 20 intervals at 1024^2)")
-    ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--serve-requests", type=int, default=1000,
+                    help="Poisson-phase requests (p99 needs >= 1000; the closed loop runs 3x as many)")
     ap.add_argument("--serve-interarrival-ms", type=float, default=100.0)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-outstanding", type=int, default=3)

@@ -18,7 +18,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_STATE = 0, -1, -2, -3
 ERR_BUSY, ERR_CANCELLED = -6, -7
 POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 COUNTERS_FIRST_INTERVAL, COUNTERS_PER_IMAGE = 0, 1
-APPLY_GEOMETRIC, APPLY_CABLE, OUTPUT_REAL = 0x1, 0x2, 0x4
+APPLY_GEOMETRIC, APPLY_CABLE, OUTPUT_REAL, WEIGHT_UNIFORM = 0x1, 0x2, 0x4, 0x8
 VIS_FORMAT = {"c64": 0, "s16": 1, "bf16": 2, "fp16": 3}
 
 
@@ -83,6 +83,7 @@ _SIGNATURES = {
     "bgi_image_compressed_host": (_i, [_vp, _i, _vp, _vp, _i, C.c_uint, _vp, _vp]),
     "bgi_fft_shift_and_norm_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp]),
     "bgi_vector_sum_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
+    "bgi_uniform_weighting_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_create": (_i, [C.POINTER(Config), C.POINTER(_vp)]),
     "bgi_destroy": (_i, [_vp]),

@@ -163,6 +163,9 @@ struct bgi_imager {
     int lanes = 2;
     DevBuf<float2> grid[kLanes];  // wave scratch: images x N*N, zero between waves
     bool grid_dirty[kLanes] = {};
+    // counter grids of a wave (uniform weighting only): images x N*N, zero between waves
+    DevBuf<float> cnt[kLanes];
+    bool cnt_dirty[kLanes] = {};
     cudaStream_t lane[kLanes] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {};
     // Deterministic mode: gridding by sort and ordered per-cell sums (full plane), with a
@@ -360,7 +363,7 @@ int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_i
     TraceRange trace("bgi_fft_inverse_gpu");
     if (!grids || !images || n_images < 0) return set_error(BGI_ERR_INVALID, "fft_inverse: bad arguments");
     if (!fft_size_supported(n_pixels))
-        return set_error(BGI_ERR_UNSUPPORTED, "fft_inverse: image side %d (powers of two 16..4096)", n_pixels);
+        return set_error(BGI_ERR_UNSUPPORTED, "fft_inverse: image side %d (1..4096)", n_pixels);
     if ((const void *)grids == (const void *)images)
         return set_error(BGI_ERR_INVALID, "fft_inverse: out of place only (grids != images)");
     cudaStream_t s = as_stream(stream);
@@ -378,6 +381,16 @@ int bgi_fft_shift_and_norm_gpu(float *images, int x_side, int y_side, int n_imag
         return set_error(BGI_ERR_INVALID, "fft_shift_and_norm: bad arguments");
     return launch_shift_and_norm(reinterpret_cast<float2 *>(images), x_side, y_side, n_images, fnorm,
                                  fnorm_size, as_stream(stream));
+}
+
+int bgi_uniform_weighting_gpu(float *grids, const float *counters, int n_pixels, int n_images, void *stream) {
+    TraceRange trace("bgi_uniform_weighting_gpu");
+    if (!grids || !counters || n_pixels < 1 || n_pixels > 46340 || n_images < 0)
+        return set_error(BGI_ERR_INVALID, "uniform_weighting: bad arguments");
+    if ((reinterpret_cast<uintptr_t>(grids) & 7u) != 0 || (reinterpret_cast<uintptr_t>(counters) & 3u) != 0)
+        return set_error(BGI_ERR_INVALID, "uniform_weighting: grids must be 8-byte and counters 4-byte aligned");
+    return launch_uniform_weighting(reinterpret_cast<float2 *>(grids), const_cast<float *>(counters),
+                                    (long long)n_pixels * n_pixels * n_images, false, as_stream(stream));
 }
 
 int bgi_vector_sum_gpu(const float *data, int64_t image_size, int n_images, float *sums,
@@ -402,7 +415,7 @@ int bgi_create(const bgi_config *cfg, bgi_imager **out) {
     if (!cfg || !out) return set_error(BGI_ERR_INVALID, "create: null argument");
     *out = nullptr;
     if (!fft_size_supported(cfg->n_pixels))
-        return set_error(BGI_ERR_UNSUPPORTED, "create: image side %d (powers of two 16..4096)", cfg->n_pixels);
+        return set_error(BGI_ERR_UNSUPPORTED, "create: image side %d (1..4096)", cfg->n_pixels);
     if (!(cfg->oversampling_factor > 0.0f)) return set_error(BGI_ERR_INVALID, "create: oversampling_factor must be > 0");
     if (cfg->pol < BGI_POL_XX || cfg->pol > BGI_POL_V) return set_error(BGI_ERR_INVALID, "create: bad pol %d", cfg->pol);
     if (cfg->max_images_per_wave < 0) return set_error(BGI_ERR_INVALID, "create: max_images_per_wave < 0");
@@ -426,6 +439,7 @@ int bgi_destroy(bgi_imager *im) {
         if (im->lane[l]) cudaStreamDestroy(im->lane[l]);
         if (im->ev_join[l]) cudaEventDestroy(im->ev_join[l]);
         im->grid[l].release();
+        im->cnt[l].release();
         im->sorted_ws[l].release();
     }
     im->d_cc.release();
@@ -659,7 +673,7 @@ static int image_checks(bgi_imager *im, int n_intervals, unsigned flags) {
     if (n_intervals < 1) return set_error(BGI_ERR_INVALID, "image: n_intervals must be >= 1");
     if (im->n_uvw_sets != 1 && im->n_uvw_sets != n_intervals)
         return set_error(BGI_ERR_INVALID, "image: array has %d UVW sets for %d intervals", im->n_uvw_sets, n_intervals);
-    if (flags & ~(BGI_APPLY_GEOMETRIC | BGI_APPLY_CABLE | BGI_OUTPUT_REAL))
+    if (flags & ~(BGI_APPLY_GEOMETRIC | BGI_APPLY_CABLE | BGI_OUTPUT_REAL | BGI_WEIGHT_UNIFORM))
         return set_error(BGI_ERR_INVALID, "image: unknown flags");
     if (!(im->delta_u > 0) || !(im->delta_v > 0))
         return set_error(BGI_ERR_STATE, "image: u_max/v_max is zero (no unflagged baseline?)");
@@ -672,7 +686,8 @@ namespace {
 
 // Per-call set-up on stream s: wave size, grid scratch of the lanes in use (cleared when new or
 // left dirty by a failed call), weight counters of every image cleared.
-int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *wave_out, int *lanes_out) {
+int prepare_call(bgi_imager *im, int n_images, bool half, bool uniform, cudaStream_t s, int *wave_out,
+                 int *lanes_out) {
     const int n = im->cfg.n_pixels;
     const size_t npix = (size_t)n * n;
     int wave = im->cfg.max_images_per_wave;
@@ -693,6 +708,14 @@ int prepare_call(bgi_imager *im, int n_images, bool half, cudaStream_t s, int *w
             BGI_TRY(check_cuda(cudaMemsetAsync(im->grid[l].ptr, 0, sizeof(float2) * im->grid[l].cap, s),
                                "grid scratch clear"));
             im->grid_dirty[l] = false;
+        }
+        if (uniform) {
+            BGI_TRY(im->cnt[l].ensure((size_t)wave * npix, "counter scratch", &fresh));
+            if (fresh || im->cnt_dirty[l]) {
+                BGI_TRY(check_cuda(cudaMemsetAsync(im->cnt[l].ptr, 0, sizeof(float) * im->cnt[l].cap, s),
+                                   "counter scratch clear"));
+                im->cnt_dirty[l] = false;
+            }
         }
         if (im->deterministic)
             BGI_TRY(im->sorted_ws[l].ensure(sorted_workspace_bytes(im->n_baselines, n, wave), "gridding workspace"));
@@ -739,6 +762,8 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.kb_table = im->kb_table.ptr;
     // the complex-to-real pass stores pixel pairs: 16 bytes of complex or 8 bytes of real pixels
     if ((reinterpret_cast<uintptr_t>(images) & ((flags & BGI_OUTPUT_REAL) ? 7u : 15u)) != 0) p.half_width = 0;
+    // uniform weighting divides cells by their counters: full-plane grids with counter grids
+    if (flags & BGI_WEIGHT_UNIFORM) p.half_width = 0;
     p.apply_geom = (flags & BGI_APPLY_GEOMETRIC) ? 1 : 0;
     p.apply_cable = (flags & BGI_APPLY_CABLE) ? 1 : 0;
     return p;
@@ -753,7 +778,7 @@ float2 *image_ptr(float2 *out, int img, size_t npix, bool real) {
 // streams[0..n_streams) starting at stream *next.  Per wave: gridding into the stream's grid
 // scratch, the row pass in place, the column pass into the images (clearing the scratch).
 int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int count, int wave,
-              cudaStream_t *streams, int n_streams, int *next, bool real) {
+              cudaStream_t *streams, int n_streams, int *next, bool real, bool uniform) {
     const int n = im->cfg.n_pixels;
     const size_t npix = (size_t)n * n;
     for (int img0 = img_first; img0 < img_first + count; img0 += wave) {
@@ -772,6 +797,13 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         p.img_base = img0;
         p.wsum = ws;  // indexed img - img_base
         im->grid_dirty[l] = true;
+        if (uniform) {
+            if ((size_t)cnt * npix > im->cnt[l].cap) return set_error(BGI_ERR_STATE, "counter scratch too small for a wave");
+            p.counters = im->cnt[l].ptr;
+            p.counter_mode = BGI_COUNTERS_PER_IMAGE;
+            p.counter_base = img0;
+            im->cnt_dirty[l] = true;
+        }
         BGI_TRY(im->mark(ls));
         if (im->deterministic) {
             p.grids_zero = 1;  // the wave scratch is zero between waves
@@ -779,6 +811,8 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         }
         else
             BGI_TRY(launch_gridding(p, ls));
+        if (uniform)  // weighting "U": cells divided by their counters, counters cleared
+            BGI_TRY(launch_uniform_weighting(grid, im->cnt[l].ptr, (long long)cnt * (long long)npix, true, ls));
         BGI_TRY(im->mark(ls));
         if (p.half_width > 0) {
             int eu, ev;
@@ -793,6 +827,7 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         }
         BGI_TRY(im->mark(ls));
         im->grid_dirty[l] = false;
+        if (uniform) im->cnt_dirty[l] = false;
     }
     return BGI_OK;
 }
@@ -823,7 +858,8 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     const int n_images = n_intervals * im->n_channels;
     int wave = 0, n_lanes = 0;
     GridParams p = block_params(im, vis, n_intervals, flags, images, format, scales);
-    BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
+    const bool uniform = (flags & BGI_WEIGHT_UNIFORM) != 0;
+    BGI_TRY(prepare_call(im, n_images, p.half_width > 0, uniform, s, &wave, &n_lanes));
     p.chan_consts = im->d_cc.ptr;
     cudaStream_t streams[bgi_imager::kLanes];
     std::fill(streams, streams + bgi_imager::kLanes, s);
@@ -837,7 +873,7 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
     }
     int next = 0;
     BGI_TRY(run_waves(im, p, reinterpret_cast<float2 *>(images), 0,
-                      n_images, wave, streams, n_lanes, &next, (flags & BGI_OUTPUT_REAL) != 0));
+                      n_images, wave, streams, n_lanes, &next, (flags & BGI_OUTPUT_REAL) != 0, uniform));
     if (n_lanes > 1) {
         for (int l = 0; l < n_lanes; ++l) {
             BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[l], im->lane[l]), "join record"));
@@ -1010,6 +1046,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     BGI_TRY(check_cuda(cudaStreamSynchronize(s), "autotune sync"));
     for (int l = 0; l < bgi_imager::kLanes; ++l) {
         im->grid[l].release();
+        im->cnt[l].release();
         im->sorted_ws[l].release();
         im->grid_dirty[l] = false;
     }
@@ -1095,7 +1132,8 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     int wave = 0, n_lanes = 0;
     GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, format,
                                       planar ? im->io_scales.ptr : nullptr);
-    BGI_TRY(prepare_call(im, n_images, p.half_width > 0, s, &wave, &n_lanes));
+    const bool uniform = (flags & BGI_WEIGHT_UNIFORM) != 0;
+    BGI_TRY(prepare_call(im, n_images, p.half_width > 0, uniform, s, &wave, &n_lanes));
     p.chan_consts = im->d_cc.ptr;
     BGI_TRY(im->ensure_lanes());
     BGI_TRY(im->ensure_copy_streams());
@@ -1138,7 +1176,7 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
         for (int l = 0; l < n_lanes; ++l)
             BGI_TRY(check_cuda(cudaStreamWaitEvent(im->lane[l], im->ev_in[c], 0), "chunk in wait"));
         BGI_TRY(run_waves(im, p, reinterpret_cast<float2 *>(im->io_img.ptr), img0, cnt, wave, im->lane, n_lanes,
-                          &next, real));
+                          &next, real, uniform));
         for (int l = 0; l < n_lanes; ++l) {
             BGI_TRY(check_cuda(cudaEventRecord(im->ev_done[c * bgi_imager::kLanes + l], im->lane[l]), "chunk done"));
             BGI_TRY(check_cuda(cudaStreamWaitEvent(im->copy_out, im->ev_done[c * bgi_imager::kLanes + l], 0),

@@ -725,8 +725,6 @@ __global__ void average_kernel(const float2 *images, int64_t n_pix, int n_images
 
 }  // namespace
 
-bool fft_size_supported(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
-
 int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool zero_src,
                     cudaStream_t s) {
     if (n_images <= 0) return BGI_OK;
@@ -740,7 +738,7 @@ int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool ze
         case 1024: return rows_n<1024>(src, dst, n_images, zero_src, s);
         case 2048: return rows_n<2048>(src, dst, n_images, zero_src, s);
         case 4096: return rows_n<4096>(src, dst, n_images, zero_src, s);
-        default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
+        default: return launch_fft_any_rows(src, dst, n, n_images, zero_src, s);  // bgi_fft_any.cu
     }
 }
 
@@ -764,7 +762,7 @@ int launch_fft_cols_to(float2 *src, float2 *dst, int n, int n_images, const unsi
         case 1024: return cols_n<1024>(src, dst, n_images, wsum, zero_src, real, s);
         case 2048: return cols_n<2048>(src, dst, n_images, wsum, zero_src, real, s);
         case 4096: return cols_n<4096>(src, dst, n_images, wsum, zero_src, real, s);
-        default: return set_error(BGI_ERR_UNSUPPORTED, "image side %d: powers of two 16..4096 only", n);
+        default: return launch_fft_any_cols(src, dst, n, n_images, wsum, zero_src, real, s);  // bgi_fft_any.cu
     }
 }
 

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_kernel(const GridPa
                 float *cnt = nullptr;
                 if (COUNTERS) {
                     if (p.counter_mode == BGI_COUNTERS_PER_IMAGE || img < p.n_channels)
-                        cnt = p.counters + (size_t)img * npix;
+                        cnt = p.counters + (size_t)(img - p.counter_base) * npix;
                 }
                 if (pos >= 0) {
                     atomicAdd(grid + pos, z);
@@ -192,13 +192,20 @@ void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
 
 template <int POL, int CPT>
 void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
+    if (q.counter_mode >= 0) {  // counter grids: full plane
+        switch (q.vis_format) {
+            case BGI_VIS_S16: grid_kernel<POL, true, false, BGI_VIS_S16, false, CPT><<<grid, kThreads, 0, s>>>(q); break;
+            case BGI_VIS_BF16: grid_kernel<POL, true, false, BGI_VIS_BF16, false, CPT><<<grid, kThreads, 0, s>>>(q); break;
+            case BGI_VIS_FP16: grid_kernel<POL, true, false, BGI_VIS_FP16, false, CPT><<<grid, kThreads, 0, s>>>(q); break;
+            default: grid_kernel<POL, true, false, BGI_VIS_C64, false, CPT><<<grid, kThreads, 0, s>>>(q);
+        }
+        return;
+    }
     switch (q.vis_format) {
         case BGI_VIS_S16: launch_fmt<POL, BGI_VIS_S16, CPT>(grid, q, s); break;
         case BGI_VIS_BF16: launch_fmt<POL, BGI_VIS_BF16, CPT>(grid, q, s); break;
         case BGI_VIS_FP16: launch_fmt<POL, BGI_VIS_FP16, CPT>(grid, q, s); break;
-        default:
-            if (q.counter_mode >= 0) grid_kernel<POL, true, false, BGI_VIS_C64, false, CPT><<<grid, kThreads, 0, s>>>(q);
-            else launch_fmt<POL, BGI_VIS_C64, CPT>(grid, q, s);
+        default: launch_fmt<POL, BGI_VIS_C64, CPT>(grid, q, s);
     }
 }
 
@@ -209,6 +216,16 @@ void launch_cpt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
         case BGI_POL_YY: launch_pol<BGI_POL_YY, CPT>(grid, q, s); break;
         case BGI_POL_I: launch_pol<BGI_POL_I, CPT>(grid, q, s); break;
         default: launch_pol<BGI_POL_V, CPT>(grid, q, s); break;
+    }
+}
+
+__global__ void uniform_weighting_kernel(float2 *grids, float *counters, long long n_cells, bool clear) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_cells;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float c = counters[i];
+        const float2 g = grids[i];
+        grids[i] = make_float2(__fdiv_rn(g.x, c), __fdiv_rn(g.y, c));
+        if (clear) counters[i] = 0.f;
     }
 }
 
@@ -226,14 +243,19 @@ int launch_channel_consts(const double *freqs, int n_channels, double du, double
     return check_launch("channel constants");
 }
 
+int launch_uniform_weighting(float2 *grids, float *counters, long long n_cells, bool clear_counters, cudaStream_t s) {
+    if (n_cells <= 0) return BGI_OK;
+    const long long blocks = std::min<long long>((n_cells + 255) / 256, (long long)sm_count() * 16);
+    uniform_weighting_kernel<<<(unsigned)blocks, 256, 0, s>>>(grids, counters, n_cells, clear_counters);
+    return check_launch("uniform weighting");
+}
+
 int launch_gridding(const GridParams &p, cudaStream_t s) {
     if (p.img_count <= 0 || p.n_baselines <= 0) return BGI_OK;
     if (p.kb_size > 0) {
         if (p.half_width > 0) return set_error(BGI_ERR_INVALID, "kb gridding: full-plane grids only");
         return launch_gridding_kb(p, p.kb_table, p.kb_size, s);
     }
-    if (p.vis_format != BGI_VIS_C64 && p.counter_mode >= 0)
-        return set_error(BGI_ERR_UNSUPPORTED, "gridding: counter grids need complex64 visibilities");
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;
     const int max_groups = 65535;
     const int cpt = images_per_thread(p.n_baselines);

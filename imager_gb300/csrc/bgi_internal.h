@@ -34,7 +34,7 @@ struct GridParams {
     const ChannelConst *chan_consts;  // [C] make_channel_const(freqs[c], du, dv), or null (then
                                       // the gridding kernels compute them)
     float2 *grids;           // images [img - img_base][N*N]
-    float *counters;         // optional counter grids
+    float *counters;         // optional counter grids, image img at counters[(img - counter_base) * N*N]
     unsigned int *wsum;      // optional per-image weight counts at wsum[(img - img_base) * kWsumStride]
     double du, dv, min_uv;
     long long n_baselines;
@@ -42,6 +42,7 @@ struct GridParams {
     int img_begin, img_count;  // images [img_begin, img_begin + img_count) of the block
     int img_base;              // grids/wsum index = img - img_base
     int counter_mode;          // -1 none, 0 first interval, 1 per image
+    int counter_base;          // counter grid index = img - counter_base (0: the block's layout)
     int half_width;            // 0: full N x N grids; W > 0: half-plane grids [N][W], u <= N/2
     int apply_geom, apply_cable;
     int grids_zero;            // 1: grids hold zeros on entry (the ordered gridder then writes
@@ -53,6 +54,9 @@ int launch_gridding(const GridParams &p, cudaStream_t s);
 // table[c] = make_channel_const(freqs[c], du, dv) for c < n_channels
 int launch_channel_consts(const double *freqs, int n_channels, double du, double dv, ChannelConst *table,
                           cudaStream_t s);
+// Weighting "U" of the CPU path (src/pacer_imager.cpp:419-428): every cell divided by its
+// counter (empty cells become 0/0, as there); clear_counters zeroes the counters after reading.
+int launch_uniform_weighting(float2 *grids, float *counters, long long n_cells, bool clear_counters, cudaStream_t s);
 
 // ---- pointed-observation UVW (bgi_geometry.cu) -------------------------------------------------
 // steps: double[n_steps][17] (bgi_uvw_step); u, v, w: float[n_steps][B]
@@ -88,7 +92,16 @@ size_t sorted_workspace_bytes(long long n_baselines, int n_pixels, int n_images)
 int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaStream_t s);
 
 // ---- FFT and image epilogues (bgi_fft.cu) --------------------------------------------------
+// Image sides of the FFT: any side 1..4096 (powers of two 16..4096 with the compile-time passes of
+// bgi_fft.cu, every other side with the mixed-radix passes of bgi_fft_any.cu, which keep one
+// twiddle table per device and side, allocated at its first use).
 bool fft_size_supported(int n);
+bool fft_pow2_size(int n);
+// Mixed-radix passes (bgi_fft_any.cu), the same contracts as launch_fft_rows and
+// launch_fft_cols_to; an fftshift (wsum given) needs src != dst.
+int launch_fft_any_rows(const float2 *src, float2 *dst, int n, int n_images, bool zero_src, cudaStream_t s);
+int launch_fft_any_cols(float2 *src, float2 *dst, int n, int n_images, const unsigned int *wsum, bool zero_src,
+                        bool real, cudaStream_t s);
 // Row pass: src rows -> dst rows (inverse DFT along x); zero_src clears src after reading.
 int launch_fft_rows(const float2 *src, float2 *dst, int n, int n_images, bool zero_src,
                     cudaStream_t s);

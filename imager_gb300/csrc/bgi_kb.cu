@@ -75,7 +75,7 @@ __device__ __forceinline__ KbPoint kb_point(const GridParams &p, size_t img, lon
     const int img_i = (int)img;
     float *cnt = nullptr;
     if (p.counters && (p.counter_mode == BGI_COUNTERS_PER_IMAGE || img_i < p.n_channels))
-        cnt = p.counters + (size_t)img * npix;
+        cnt = p.counters + (size_t)(img - p.counter_base) * npix;
     if (pos >= 0) {
         if (cnt) atomicAdd(cnt + pos, 1.0f);
         ++*counted;

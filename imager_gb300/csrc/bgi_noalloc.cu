@@ -9,14 +9,24 @@
 // library holds statically in this file: a 32 MiB grid and per-image weight counters for up
 // to 1024 images per wave.  The caller still passes its inputs and its output images.
 //
-// The cost of that convenience: every GPU that loads the library holds these 32.1 MiB until
-// the process exits, whether or not it ever calls this function.
+// The cost of that convenience: every GPU on which the library's code is loaded holds these
+// 32.1 MiB until the process exits.  CUDA loads a library's device code lazily by default (at
+// the first use of each of its modules), so the scratch is committed on a device by the first
+// call of this function there -- its address look-up loads this file's module -- and the
+// gridding and FFT modules load at their first launches.  A caller that budgets device memory
+// up front makes one warm-up call per device when it sets its budget (or runs with
+// CUDA_MODULE_LOADING=EAGER, which loads every module, and so commits the scratch, when the
+// library's first CUDA call creates the context).
 //
 // Limits and behaviour:
 //  * one N x N complex grid must fit the scratch: N <= 2048 (an image side of 4096 is
 //    rejected); larger blocks are processed in waves of as many images as fit;
 //  * the first call on each device looks up the scratch's device address
-//    (cudaGetSymbolAddress) and should come before any stream capture on that device;
+//    (cudaGetSymbolAddress), which loads the module and commits the scratch; make it before
+//    any stream capture on that device and before the device's memory is budgeted;
+//  * the address is cached per device for the life of the process: after cudaDeviceReset (or
+//    any other teardown of the device's primary context) the library must not be used again
+//    in that process, as every device pointer it holds is then stale;
 //  * every call shares the one scratch and leaves its last contents there; each call clears the
 //    part it uses before gridding, so no state carries over from an earlier call, but calls
 //    whose work overlaps on the GPU (different streams, or different host threads) race on
@@ -91,7 +101,10 @@ extern "C" BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_chan
     if (!(delta_u > 0) || !(delta_v > 0)) return set_error(BGI_ERR_INVALID, "image_noalloc: delta_u/v must be > 0");
     if ((reinterpret_cast<uintptr_t>(vis) & 15u) || (reinterpret_cast<uintptr_t>(images) & 7u))
         return set_error(BGI_ERR_INVALID, "image_noalloc: vis must be 16-byte and images 8-byte aligned");
-    if (!fft_size_supported(n_pixels))
+    if ((long long)n_intervals * n_channels > 2147483647LL)
+        return set_error(BGI_ERR_INVALID, "image_noalloc: n_intervals * n_channels exceeds 2^31 - 1");
+    // powers of two only: the mixed-radix passes of other sides allocate a twiddle table
+    if (!fft_pow2_size(n_pixels))
         return set_error(BGI_ERR_UNSUPPORTED, "image_noalloc: image side %d (powers of two 16..2048)", n_pixels);
     const size_t npix = (size_t)n_pixels * n_pixels;
     if (npix > kNoAllocGridElems)

@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, in
     }
     *cell = acc;
     if (p.counter_mode == BGI_COUNTERS_PER_IMAGE || (p.counter_mode == BGI_COUNTERS_FIRST_INTERVAL && img < p.n_channels)) {
-        float *cnt = p.counters + (size_t)img * cells + c;
+        float *cnt = p.counters + (size_t)(img - p.counter_base) * cells + c;
         float f = *cnt;
         for (unsigned i = 0; i < len; ++i) f = __fadd_rn(f, 1.0f);
         *cnt = f;
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, 
             *cell = acc;
             if (p.counter_mode == BGI_COUNTERS_PER_IMAGE ||
                 (p.counter_mode == BGI_COUNTERS_FIRST_INTERVAL && img < p.n_channels)) {
-                float *cnt = p.counters + (size_t)img * cells + c;
+                float *cnt = p.counters + (size_t)(img - p.counter_base) * cells + c;
                 float f = *cnt;
                 for (unsigned i = 0; i < len; ++i) f = __fadd_rn(f, 1.0f);
                 *cnt = f;

@@ -13,11 +13,11 @@ import numpy as np
 import torch
 
 from . import capi
-from .capi import APPLY_CABLE, APPLY_GEOMETRIC, OUTPUT_REAL, POL, VIS_FORMAT, call
+from .capi import APPLY_CABLE, APPLY_GEOMETRIC, OUTPUT_REAL, POL, VIS_FORMAT, WEIGHT_UNIFORM, call
 
 __all__ = ["Imager", "apply_geometric_corrections", "apply_cable_corrections", "gridding",
-           "fft_inverse", "fft_shift_and_norm", "vector_sum", "image_averaging",
-           "APPLY_GEOMETRIC", "APPLY_CABLE", "POL"]
+           "fft_inverse", "fft_shift_and_norm", "uniform_weighting", "vector_sum", "image_averaging",
+           "APPLY_GEOMETRIC", "APPLY_CABLE", "OUTPUT_REAL", "WEIGHT_UNIFORM", "POL"]
 
 
 def _ptr(t):
@@ -192,6 +192,14 @@ def fft_shift_and_norm(images, fnorm, stream=None):
     ys, xs = int(images.shape[-2]), int(images.shape[-1])
     call("bgi_fft_shift_and_norm_gpu", _ptr(images), xs, ys, images.numel() // (xs * ys), _ptr(fnorm),
          int(fnorm.numel()), _stream(stream))
+
+
+def uniform_weighting(grids, counters, stream=None):
+    """Weighting "U" of the CPU gridder (src/pacer_imager.cpp:419-428): grids (complex64
+    [..., N, N]) divided cell by cell by counters (float32, same shape), in place."""
+    n = int(grids.shape[-1])
+    n_images = grids.numel() // (n * n)
+    call("bgi_uniform_weighting_gpu", _ptr(grids), _ptr(counters), n, n_images, _stream(stream))
 
 
 def vector_sum(data, image_size, n_images, sums, stream=None):

@@ -292,13 +292,14 @@ def serving_arrays(device="cpu", n_channels=32):
 
 
 
-def batched_bands(device="cpu", n_intervals=5):
+def batched_bands(device="cpu", n_intervals=5, n_channels=64):
     """The uneven batch workload: 512 antennas in 16 clustered sub-stations over 3 km, 256 channels
     over 100-200 MHz in four bands of 64 imaged at 256, 512, 1024 and 2048 pixels, 5 intervals,
     400 point sources and a diffuse power-law background (seed 1238).  One Observation per band
-    (the same array)."""
+    (the same array).  n_channels < 64 keeps the first channels of each band (a slice of the
+    workload with its array, image sides and sky)."""
     rng = np.random.Generator(np.random.PCG64(1238))
     enu = layout_substations(rng, 512, 16)
     freqs = 100e6 + np.arange(256) * (100e6 / 256)
-    return [make_observation(1238 + k, 512, enu, n_intervals, freqs[64 * k:64 * (k + 1)], 256 << k, n_src=400,
-                             device=device, fast=True, diffuse=(10.0, 2.0)) for k in range(4)]
+    return [make_observation(1238 + k, 512, enu, n_intervals, freqs[64 * k:64 * k + n_channels], 256 << k,
+                             n_src=400, device=device, fast=True, diffuse=(10.0, 2.0)) for k in range(4)]

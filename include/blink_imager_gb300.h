@@ -88,6 +88,12 @@ enum bgi_counter_mode {
  * half the output bytes.  (On the half-plane path the images are real by construction; on the
  * full plane the imaginary parts, rounding noise of a Hermitian grid, are dropped.) */
 #define BGI_OUTPUT_REAL 0x4u
+/* Weighting "U" of the CPU path (src/pacer_imager.cpp:419-428): after gridding, every cell of an
+ * image's grid is divided by its counter (the number of points gridded into it), before the
+ * transform; the normalisation stays 1/sum(counters).  As there, every cell is divided, so an
+ * empty cell becomes 0/0 = NaN and so does every pixel of that image's transform.  Grids the full
+ * plane, with per-image counter grids in the handle's scratch. */
+#define BGI_WEIGHT_UNIFORM 0x8u
 
 BGI_API const char *bgi_last_error(void);
 BGI_API int bgi_version(void); /* 100 * major + minor */
@@ -151,8 +157,10 @@ BGI_API int bgi_gridding_kb_gpu(const float *vis, int n_ant, int n_channels, int
                                 void *stream);
 
 /* gpufftPlanMany + gpufftExecC2C(..., BACKWARD) (src/gpu/pacer_imager_hip.cpp:83-99): batched
- * unnormalised inverse 2D FFT, out of place, our own kernels.  n_pixels: power of two,
- * 16..4096. */
+ * unnormalised inverse 2D FFT, out of place, our own kernels.  n_pixels: any side 1..4096
+ * (powers of two 16..4096 with compile-time radix-8/16/32 passes; every other side with
+ * mixed-radix passes -- radices 2, 3, 4, 5, 8 in registers, other primes as direct sums -- whose
+ * twiddle table is allocated once per device and side, at its first use, and kept until exit). */
 BGI_API int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels, int n_images,
                         void *stream);
 
@@ -160,6 +168,12 @@ BGI_API int bgi_fft_inverse_gpu(const float *grids, float *images, int n_pixels,
  * divide every pixel of image i by fnorm[i % fnorm_size].  x_side must be even. */
 BGI_API int bgi_fft_shift_and_norm_gpu(float *images, int x_side, int y_side, int n_images,
                                const float *fnorm, int fnorm_size, void *stream);
+
+/* The CPU gridder's weighting "U" step (src/pacer_imager.cpp:419-428; no GPU counterpart in the
+ * reference): grids[i] /= counters[i] for every cell of n_images complex grids of n_pixels^2
+ * cells (IEEE division, so empty cells become 0/0 = NaN as in the reference).  In place. */
+BGI_API int bgi_uniform_weighting_gpu(float *grids, const float *counters, int n_pixels, int n_images,
+                                      void *stream);
 
 /* vector_sum_gpu (src/gpu/gpu_utils.cpp:62-71): sums[i] = sum of data[i*image_size ...]. */
 BGI_API int bgi_vector_sum_gpu(const float *data, int64_t image_size, int n_images, float *sums,
@@ -181,7 +195,8 @@ BGI_API int bgi_image_averaging_gpu(const float *images, int64_t image_size, int
 typedef struct bgi_imager bgi_imager;
 
 typedef struct bgi_config {
-    int n_pixels;              /* image side N (power of two, 16..4096) */
+    int n_pixels;              /* image side N, 1..4096 (sides that are not powers of two from 16
+                                  up are imaged on the full plane with mixed-radix FFT passes) */
     float oversampling_factor; /* delta_u = osf * u_max / N (src/pacer_imager.cpp:497) */
     int pol;                   /* enum bgi_pol */
     double min_uv;             /* uv distance cut in wavelengths (strictly greater passes) */
@@ -210,8 +225,8 @@ BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float
 BGI_API int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz);
 
 /* 1 when bgi_image would take the half-plane path for the current array, frequencies and
- * configuration (16-byte aligned complex images; not with bgi_set_deterministic or a
- * convolution kernel, which grid the full plane), 0 when it would transform the full plane;
+ * configuration (16-byte aligned complex images; not with bgi_set_deterministic, a convolution
+ * kernel or BGI_WEIGHT_UNIFORM, which grid the full plane), 0 when it would transform the full plane;
  * negative status on error. */
 BGI_API int bgi_half_plane(const bgi_imager *im);
 
@@ -341,8 +356,11 @@ BGI_API int bgi_write_fits_block(const char *dir, const char *prefix, const floa
  * (the CPU path's normalisation): vis float[T][C][B][4][2] in, images float[T][C][N][N][2] out.
  * Scratch is a static 32 MiB grid plus weight counters that every GPU loading the library
  * holds until exit; the image side is limited to 2048 (larger sides return
- * BGI_ERR_UNSUPPORTED).  The first call on a device looks up the scratch address and should
- * come before any stream capture.  All calls share the scratch: each clears what it uses, but
+ * BGI_ERR_UNSUPPORTED).  CUDA loads device code lazily by default, so the scratch is committed
+ * on a device by the first call there (which looks up its address and loads the modules it
+ * uses): make one warm-up call per device when setting a memory budget and before any stream
+ * capture, or run with CUDA_MODULE_LOADING=EAGER to commit it when the context is created.
+ * The address is cached per device: do not use the library after a cudaDeviceReset.  All calls share the scratch: each clears what it uses, but
  * calls that overlap on the GPU race -- serialise them.  Makes no allocating call. */
 BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n_intervals,
                               const float *u, const float *v, int n_uvw_sets,

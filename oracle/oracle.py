@@ -18,7 +18,18 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libblink_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libpacer_ref.so")
-REF_SRC = "/root/reference/src"
+# The reference checkout's src/ (only for compiling the reference's CPU sources): the
+# BGI_REFERENCE_SRC environment variable, else a checkout named "reference" beside this
+# repository; empty when neither exists.
+def _find_ref_src() -> str:
+    env = os.environ.get("BGI_REFERENCE_SRC", "")
+    if env:
+        return env
+    sibling = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src")
+    return sibling if os.path.isfile(os.path.join(sibling, "pacer_imager.cpp")) else ""
+
+
+REF_SRC = _find_ref_src()
 
 POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 
@@ -36,8 +47,8 @@ def build(ref: bool = False) -> None:
     """Compile the oracle (and, when the reference checkout exists and ref is set, the
     reference CPU build)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir(REF_SRC):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if ref and REF_SRC and os.path.isdir(REF_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={REF_SRC}"], check=True)
 
 
 def library():

@@ -7,6 +7,8 @@ pin the oracle: tests/test_oracle_golden.py checks the oracle against these file
 without the reference checkout.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(the reference checkout's src/ is found through BGI_REFERENCE_SRC, or as a checkout named
+"reference" beside this repository).
 """
 from __future__ import annotations
 
@@ -53,7 +55,7 @@ def ref_run(obs, vis, n_pixels, pol, min_uv=-1000.0, weighting=b"N", geom=1, cab
 def main():
     O.build(ref=True)
     if O.ref_library() is None:
-        raise SystemExit("reference build missing: needs the reference checkout")
+        raise SystemExit("reference build missing: set BGI_REFERENCE_SRC to the reference checkout's src/")
     cases = {}
 
     # 1) corrections on their own (src/corrections.cpp), one UVW set

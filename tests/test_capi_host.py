@@ -31,8 +31,12 @@ def test_host_side_argument_checks(lib):
     # odd x side is rejected as in src/gpu/gpu_utils.cpp:129-131
     assert lib.bgi_fft_shift_and_norm_gpu(C.c_void_p(16), 3, 2, 1, C.c_void_p(16), 1, None) == capi.ERR_INVALID
     assert b"even" in lib.bgi_last_error()
-    # unsupported FFT size
-    assert lib.bgi_fft_inverse_gpu(C.c_void_p(16), C.c_void_p(32), 100, 1, None) == capi.ERR_UNSUPPORTED
+    # unsupported FFT sizes: every side 1..4096 is taken (powers of two and mixed radix)
+    for side in (0, 4097, 5000):
+        assert lib.bgi_fft_inverse_gpu(C.c_void_p(16), C.c_void_p(32), side, 1, None) == capi.ERR_UNSUPPORTED
+    # uniform weighting: null and misaligned buffers
+    assert lib.bgi_uniform_weighting_gpu(None, C.c_void_p(16), 32, 1, None) == capi.ERR_INVALID
+    assert lib.bgi_uniform_weighting_gpu(C.c_void_p(12), C.c_void_p(16), 32, 1, None) == capi.ERR_INVALID
     # in-place FFT is refused
     assert lib.bgi_fft_inverse_gpu(C.c_void_p(16), C.c_void_p(16), 64, 1, None) == capi.ERR_INVALID
     # null buffers
@@ -50,7 +54,8 @@ def test_host_side_argument_checks(lib):
 
 def test_create_rejects_bad_config(lib):
     h = C.c_void_p()
-    for cfg in (capi.Config(100, 2.0, 0, -1.0, 0, 0), capi.Config(512, 0.0, 0, -1.0, 0, 0),
+    for cfg in (capi.Config(5000, 2.0, 0, -1.0, 0, 0), capi.Config(0, 2.0, 0, -1.0, 0, 0),
+                capi.Config(512, 0.0, 0, -1.0, 0, 0),
                 capi.Config(512, 2.0, 9, -1.0, 0, 0), capi.Config(512, 2.0, 0, -1.0, -3, 0)):
         st = lib.bgi_create(C.byref(cfg), C.byref(h))
         assert st in (capi.ERR_UNSUPPORTED, capi.ERR_INVALID), (cfg.n_pixels, st)

@@ -207,3 +207,44 @@ def test_pointed_uvw_golden(oracle_lib):
     u, v, w = O.pointed_uvw(g["xyz"], g["steps"])
     for a, b in ((u, g["u"]), (v, g["v"]), (w, g["w"])):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_cpu_runnable_plain_case_against_reference_build(oracle_lib):
+    """The oracle against the reference's own CPU imager (CPacerImager::run,
+    src/pacer_imager.cpp:440-526, compiled from its sources with the stand-ins in oracle/ref_shim)
+    on the CPU-runnable plain case: 256 antennas in a 35 m disk, one channel at 159.375 MHz, one
+    interval, 256 x 256, both corrections.  Corrected visibilities, grids and counters are the
+    same bits; images agree to FP32-vs-FP64 transform rounding.  Needs the reference build
+    (oracle/_ref, made only where the reference checkout is found); skipped elsewhere."""
+    O = oracle_lib
+    ref = O.ref_library()
+    if ref is None:
+        pytest.skip("reference CPU build (oracle/_ref) not present")
+    from imager_gb300 import synth
+    obs = synth.config1()
+    vis = np.ascontiguousarray(obs.vis_f32())
+    T, Cn, nb = vis.shape[:3]
+    n = obs.n_pixels
+    npix = n * n * T * Cn
+    vout = np.zeros(vis.size, np.float32)
+    g = np.zeros(npix * 2, np.float32)
+    c = np.zeros(npix, np.float32)
+    im = np.zeros(npix * 2, np.float32)
+    sc = np.zeros(4)
+    no_flagged = np.zeros(1, np.int32)  # the case flags only the autocorrelations
+    ref.ref_set_kernel_size(0)
+    # obsInfo fields are unused with the frequency override (159.375 MHz)
+    ref.ref_run(vis.reshape(-1), T, Cn, obs.n_ant, np.ascontiguousarray(obs.u[0]),
+                np.ascontiguousarray(obs.v[0]), np.ascontiguousarray(obs.w[0]), obs.cable, no_flagged, 0,
+                0.04, 4, 1.28, 118, 159.375, n, 2.0, -1000.0, 0, b"N", 1, 1, vout, g, c, im, sc)
+    flags = O.update_flags(obs.n_ant, [])
+    assert np.array_equal(flags, obs.flags)
+    vis_c, grids, counters, images, (du, dv) = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, flags,
+                                                               obs.freqs, n)
+    assert du == sc[0] and dv == sc[1]
+    assert np.array_equal(_bits(vis_c.reshape(-1)), _bits(vout))
+    assert np.array_equal(_bits(grids.reshape(-1)), _bits(g))
+    assert np.array_equal(counters.reshape(-1), c)
+    ref_img = im.view(np.complex64).reshape(n, n)
+    err = np.linalg.norm(images[0, 0] - ref_img) / np.linalg.norm(images[0, 0])
+    assert err < 1e-6, err

@@ -47,20 +47,38 @@ def test_no_alloc_matches_image_on_two_calls():
     du, dv = h.uv_cell[:2]
     h.close()
 
+    # the oracle of the same block (no corrections), for a check that does not go through the
+    # allocating entry point
+    from oracle import oracle as O
+    vis_np = np.ascontiguousarray(obs.vis_f32())
+    grids, counters, _ = O.gridding(vis_np, obs.u, obs.v, obs.flags, obs.freqs, du, dv, n, n_uvw_sets=T)
+    oracle_images = O.image_f64(grids, counters)
+
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    outs = [torch.full((T, Cn, n, n), float("nan"), dtype=torch.complex64, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    free_after_first = None
     for call in range(2):
-        out = torch.full((T, Cn, n, n), float("nan"), dtype=torch.complex64, device="cuda")
+        out = outs[call]
         st = lib.bgi_image_noalloc(C.c_void_p(vis.data_ptr()), obs.n_ant, Cn, T, C.c_void_p(u.data_ptr()),
                                    C.c_void_p(v.data_ptr()), T, C.c_void_p(flags.data_ptr()),
                                    C.c_void_p(freqs.data_ptr()), du, dv, n, -1000.0, capi.POL["XX"],
                                    C.c_void_p(out.data_ptr()), stream)
         assert st == capi.OK, lib.bgi_last_error()
         torch.cuda.synchronize()
+        # driver-level free memory: the first call may load the library's modules (and so commit
+        # the static scratch); the second call must take no device memory at all
+        free_now = torch.cuda.mem_get_info()[0]
+        if call == 0:
+            free_after_first = free_now
+        else:
+            assert free_now == free_after_first, (free_after_first, free_now)
         got = out.cpu().numpy()
         assert np.isfinite(got).all(), call
         for i in range(T):
             for j in range(Cn):
                 assert _rel_l2(got[i, j], ref[i, j]) < IMAGE_TOL, (call, i, j)
+                assert _rel_l2(got[i, j], oracle_images[i, j]) < IMAGE_TOL, (call, i, j)
 
 
 def test_no_alloc_rejects_grid_beyond_scratch():
