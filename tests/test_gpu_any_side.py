@@ -69,7 +69,7 @@ def test_image_any_side_against_oracle(im, n, pol):
             assert rel_l2(out[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
     assert np.array_equal(h.weight_sums(4), counters.reshape(4, -1).sum(1).astype(np.uint32))
     real = h.image(dev(vis), flags=im.APPLY_GEOMETRIC | im.APPLY_CABLE | im.OUTPUT_REAL).cpu().numpy()
-    assert np.array_equal(real, out.real)
+    assert rel_l2(real, out.real) < 1e-6  # separate calls: atomic sums may round differently
     host = h.image_host(np.ascontiguousarray(vis))
     assert rel_l2(host, out) < 1e-6
     h.close()
@@ -117,6 +117,10 @@ def test_uniform_weighting_full_coverage(im, n):
     # twice in a row: the counter scratch is clean for the second call
     again = h.image(dev(vis), flags=fl).cpu().numpy()
     assert rel_l2(again, out) < 1e-6
+    data, scales = im.compress_visibilities(dev(vis), "s16")
+    s16 = h.image_compressed(data, scales, "s16", flags=fl).cpu().numpy()
+    for j in range(2):
+        assert rel_l2(s16[0, j], ref[0, j]) < IMAGE_TOL, j
     # natural weighting on the same handle afterwards is unaffected
     _, _, _, nat, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n, osf=0.5)
     natural = h.image(dev(vis)).cpu().numpy()
