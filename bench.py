@@ -660,6 +660,23 @@ def run_ours(args, rank, world, local_rank):
             v_ms = time_steps(step_for(im, f), k, stream, flush)
             variants[f"storage_{f}"] = {"images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms,
                                         "steps": k, **({"errors_vs_fp64": image_errors(out, refs)} if rank == 0 else {})}
+        # the complex-to-real pass on the tensor cores (split-FP16 DFT products), same step
+        im.set_fft_mode("tensor_split16")
+        v_ms = time_steps(step, k, stream, flush)
+        tc_errs = image_errors(out, refs) if rank == 0 else {}
+        im.set_stage_timing(True)
+        timed_steps(step, stage_steps, stream, flush)
+        tc_stages = im.stage_times()
+        im.set_stage_timing(False)
+        im.set_fft_mode("simt")
+        tc_pass2 = tc_stages.get("fft_pass2", (0.0, 0))
+        variants["fft_tensor_split16"] = {
+            "images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms, "steps": k, "storage": fmt,
+            "fft_pass2_ms_per_launch": tc_pass2[0] / tc_pass2[1] if tc_pass2[1] else None,
+            "what": "complex-to-real row pass with its length-256 transforms as two 16-point DFT products on "
+                    "the tensor cores (mma.sync m16n8k16, FP16 hi+lo operand splits, three products, FP32 "
+                    "accumulation)",
+            **({"errors_vs_fp64": tc_errs} if rank == 0 else {})}
         im.set_deterministic(True)
         v_ms = time_steps(step, k, stream, flush)
         im.set_deterministic(False)

@@ -20,6 +20,7 @@ POL = {"XX": 0, "YY": 1, "I": 2, "V": 3}
 COUNTERS_FIRST_INTERVAL, COUNTERS_PER_IMAGE = 0, 1
 APPLY_GEOMETRIC, APPLY_CABLE, OUTPUT_REAL, WEIGHT_UNIFORM = 0x1, 0x2, 0x4, 0x8
 VIS_FORMAT = {"c64": 0, "s16": 1, "bf16": 2, "fp16": 3}
+FFT_MODE = {"simt": 0, "tensor_split16": 1}
 
 
 class BgiError(RuntimeError):
@@ -84,6 +85,8 @@ _SIGNATURES = {
     "bgi_fft_shift_and_norm_gpu": (_i, [_vp, _i, _i, _i, _vp, _i, _vp]),
     "bgi_vector_sum_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_uniform_weighting_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
+    "bgi_set_fft_mode": (_i, [_vp, _i]),
+    "bgi_get_fft_mode": (_i, [_vp, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_create": (_i, [C.POINTER(Config), C.POINTER(_vp)]),
     "bgi_destroy": (_i, [_vp]),

@@ -151,6 +151,7 @@ struct bgi_imager {
     float2 *d_dl = nullptr;  // cable delay L[a2]-L[a1] per baseline as (hi, lo) floats
     DevBuf<ChannelConst> d_cc; // per-channel gridding constants for the current delta_u/v
     int kb_size = 0;           // Kaiser-Bessel kernel size (0: nearest neighbour)
+    int fft_mode = BGI_FFT_SIMT;  // enum bgi_fft_mode
     DevBuf<float> kb_table;    // its rows [1023][kb_size]
     bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
@@ -819,7 +820,8 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
             im->half_plane_extent(&eu, &ev);
             BGI_TRY(launch_fft_cols_half(grid, n, cnt, eu, ev, ls));           // in place, rows shifted
             BGI_TRY(im->mark(ls));
-            BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, eu, ls, real));  // clears the scratch
+            BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, eu, ls, real,
+                                    im->fft_mode == BGI_FFT_TENSOR_SPLIT16));  // clears the scratch
         } else {
             BGI_TRY(launch_fft_rows(grid, grid, n, cnt, false, ls));  // in place in the scratch
             BGI_TRY(im->mark(ls));
@@ -984,6 +986,23 @@ int bgi_batch_destroy(bgi_batch *b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     delete b;
+    return BGI_OK;
+}
+
+int bgi_set_fft_mode(bgi_imager *im, int mode) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_fft_mode: null handle");
+    if (mode != BGI_FFT_SIMT && mode != BGI_FFT_TENSOR_SPLIT16)
+        return set_error(BGI_ERR_INVALID, "set_fft_mode: bad mode %d", mode);
+    if (mode == BGI_FFT_TENSOR_SPLIT16 && !c2r_tensor_supported(im->cfg.n_pixels))
+        return set_error(BGI_ERR_UNSUPPORTED, "set_fft_mode: no tensor-core stage for image side %d (512 only)",
+                         im->cfg.n_pixels);
+    im->fft_mode = mode;
+    return BGI_OK;
+}
+
+int bgi_get_fft_mode(const bgi_imager *im, int *mode) {
+    if (!im || !mode) return set_error(BGI_ERR_INVALID, "get_fft_mode: bad arguments");
+    *mode = im->fft_mode;
     return BGI_OK;
 }
 

@@ -595,6 +595,242 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     if (threadIdx.x == 0) bulk_wait_all();
 }
 
+// ---- complex-to-real rows on the tensor cores (N = 512) ------------------------------------
+// The same pass as c2r_rows_kernel with its length-256 complex transform done as two dense 16-point
+// DFT products on the tensor cores (warp-level mma.sync m16n8k16, FP16 operands, FP32
+// accumulation).  With z[16 n1 + n2] = X[n1][n2] (the Z values formed from the staged row):
+//   Y = F16 X             (16-point inverse DFTs down the columns n1, for each n2)
+//   Y'[k1][n2] = Y[k1][n2] exp(+2 pi i k1 n2 / 256)
+//   Z = Y' F16            (16-point inverse DFTs along the rows), z_out[k1 + 16 k2] = Z[k1][k2]
+// with F16[j][k] = exp(+2 pi i j k / 16), symmetric.  Complex products are real products of the
+// stacked parts: [Yr; Yi] = [[Fr, -Fi], [Fi, Fr]] [Xr; Xi] and [Zr | Zi] = [Y'r | Y'i] [[Fr, Fi],
+// [-Fi, Fr]].  The accumulator fragments of the first product are the operand fragments of the
+// second (rows k1, columns n2 in both), so the two products exchange no data through shared memory.
+//
+// Precision: every operand is split into FP16 hi + lo parts (hi = fp16(x), lo = fp16(x - hi)) and
+// each product is Alo Bhi + Ahi Blo + Ahi Bhi, accumulated in FP32 (the lo x lo term, 2^-22 of the
+// product, is dropped): about 22 significant bits per operand instead of FP16's 11.  Each row is
+// scaled by a power of two so that its largest component lies in [2^9, 2^10) before the first
+// product (the second product's operands then stay below 2^14, inside FP16's range), and scaled back
+// exactly in the stores.
+constexpr int kTcRows = 8;        // rows per block: 4 warps, 2 rows each
+constexpr int kTcThreads = 128;
+struct alignas(16) W256Data {  // exp(+2 pi i q / 256), q < 256
+    TwEntry v[256];
+};
+constexpr W256Data make_w256() {
+    W256Data d{};
+    for (int q = 0; q < 256; ++q) d.v[q] = twiddle_exact(q, 256);
+    return d;
+}
+__device__ const W256Data g_w256 = make_w256();
+
+__device__ __forceinline__ uint32_t h2_bits(__half2 h) { return *reinterpret_cast<uint32_t *>(&h); }
+
+// hi and lo FP16 pairs of (a, b); a in the low half (the lower row or column index)
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t &hi, uint32_t &lo) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    hi = h2_bits(h);
+    lo = h2_bits(__floats2half2_rn(a - hf.x, b - hf.y));
+}
+
+__device__ __forceinline__ void mma_f16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// d += A B with split operands: Alo Bhi + Ahi Blo + Ahi Bhi (small terms first)
+__device__ __forceinline__ void mma_split(float (&d)[4], const uint32_t (&ahi)[4], const uint32_t (&alo)[4],
+                                          uint32_t bh0, uint32_t bh1, uint32_t bl0, uint32_t bl1) {
+    mma_f16_16816(d, alo, bh0, bh1);
+    mma_f16_16816(d, ahi, bl0, bl1);
+    mma_f16_16816(d, ahi, bh0, bh1);
+}
+
+__device__ __forceinline__ void neg4(const uint32_t (&a)[4], uint32_t (&o)[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) o[i] = a[i] ^ 0x80008000u;
+}
+
+template <int N>
+constexpr size_t c2r_tc_smem_bytes() {
+    return sizeof(float2) * (size_t)kTcRows * (c2r_row_bytes<N>() / sizeof(float2)) + c2r_row_bytes<N>() +
+           c2r_wz_bytes<N>() + sizeof(W256Data) + sizeof(uint64_t) + sizeof(float);
+}
+
+template <int N, bool REAL>
+__global__ void __launch_bounds__(kTcThreads) c2r_rows_tc_kernel(float2 *grids, float2 *images,
+                                                                 const unsigned int *wsum, unsigned copy_bytes) {
+    static_assert(N == 512, "the tensor-core row pass is the 16 x 16 factorisation of N/2 = 256");
+    constexpr int M = N / 2, W = half_width_of<N>();
+    constexpr unsigned ROW_BYTES = c2r_row_bytes<N>();
+    constexpr int BUF = (int)(ROW_BYTES / sizeof(float2));  // >= M + 1 values, 16-byte multiple
+    static_assert(BUF >= M + 1 && ROW_BYTES % 16 == 0, "row buffers hold X[0..M] and stay 16-byte aligned");
+    static_assert(ROW_BYTES <= W * sizeof(float2), "rows copied whole");
+    constexpr unsigned WZ_BYTES = c2r_wz_bytes<N>(), W256_BYTES = sizeof(W256Data);
+    static_assert(WZ_BYTES % 16 == 0 && W256_BYTES % 16 == 0, "tables copied whole");
+    extern __shared__ __align__(16) float2 smem[];
+    float2 *zeros = smem + kTcRows * BUF;
+    float2 *wz = zeros + BUF;
+    float2 *w256 = wz + WZ_BYTES / sizeof(float2);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(w256 + 256);
+    float *s_scale = reinterpret_cast<float *>(bar + 1);
+    const size_t row0 = (size_t)blockIdx.x * kTcRows;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    for (int i = threadIdx.x; i < (int)(ROW_BYTES / 16); i += blockDim.x)
+        reinterpret_cast<float4 *>(zeros)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    {  // the part of each row buffer that no copy fills
+        constexpr int Q = (int)(ROW_BYTES / 16);
+        const int q0 = (int)(copy_bytes / 16), tail = Q - q0;
+        for (int i = threadIdx.x; i < kTcRows * tail; i += blockDim.x)
+            reinterpret_cast<float4 *>(smem + (i / tail) * BUF)[q0 + i % tail] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(bar, kTcRows * copy_bytes + WZ_BYTES + W256_BYTES);
+        bulk_load(wz, g_z_twiddles<N>.v, WZ_BYTES, bar);
+        bulk_load(w256, g_w256.v, W256_BYTES, bar);
+        for (int r = 0; r < kTcRows; ++r) bulk_load(smem + r * BUF, grids + (row0 + r) * W, copy_bytes, bar);
+        *s_scale = (float)(1.0 / (double)wsum[(row0 / N) * kWsumStride]);
+    }
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
+        mbar_wait_bounded(bar, 0);  // let copies still in flight land before the block exits
+        return;
+    }
+    if (threadIdx.x == 0) {  // the rows have been read: clear them for the next wave
+        for (int r = 0; r < kTcRows; ++r) bulk_store(grids + (row0 + r) * W, zeros, copy_bytes);
+        bulk_commit();
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    // F16 fragments, hi and lo: A layout (rows j = g, g+8; columns k = 2t, 2t+1, 2t+8, 2t+9) and B
+    // layout per column tile nt (rows j = 2t, 2t+1, 2t+8, 2t+9; column k = 8 nt + g)
+    uint32_t frA_h[4], frA_l[4], fiA_h[4], fiA_l[4];
+    uint32_t frB_h[2][2], frB_l[2][2], fiB_h[2][2], fiB_l[2][2];
+    {
+        auto f16 = [&](int j, int k) { return w256[16 * ((j * k) & 15)]; };
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = g + 8 * (r & 1), k = 2 * t + 8 * (r >> 1);
+            const float2 e0 = f16(j, k), e1 = f16(j, k + 1);
+            split_pair(e0.x, e1.x, frA_h[r], frA_l[r]);
+            split_pair(e0.y, e1.y, fiA_h[r], fiA_l[r]);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int j = 2 * t + 8 * r, k = 8 * nt + g;
+                const float2 e0 = f16(j, k), e1 = f16(j + 1, k);
+                split_pair(e0.x, e1.x, frB_h[nt][r], frB_l[nt][r]);
+                split_pair(e0.y, e1.y, fiB_h[nt][r], fiB_l[nt][r]);
+            }
+    }
+    uint32_t nfiA_h[4], nfiA_l[4];
+    neg4(fiA_h, nfiA_h);
+    neg4(fiA_l, nfiA_l);
+    const float img_scale = *s_scale;
+    for (int slot = warp; slot < kTcRows; slot += kTcThreads / 32) {
+        const float2 *buf = smem + slot * BUF;
+        const size_t row = row0 + slot;
+        // z at n1 = 2t + (j & 1) + 8 (j >> 1), n2 = 8 nt + g: Z[k] = 2 conj(b) + P[k] (a - conj(b))
+        float2 z[2][4];
+        float mx = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = 16 * (2 * t + (j & 1) + 8 * (j >> 1)) + 8 * nt + g;
+                const float2 a = buf[k], b = buf[M - k], P = wz[k];
+                const float dx = a.x - b.x, dy = a.y + b.y;
+                z[nt][j] = make_float2(fmaf(P.x, dx, fmaf(-P.y, dy, 2.f * b.x)), fmaf(P.x, dy, fmaf(P.y, dx, -2.f * b.y)));
+                mx = fmaxf(mx, fmaxf(fabsf(z[nt][j].x), fabsf(z[nt][j].y)));
+            }
+        // power-of-two row scale: largest component into [2^9, 2^10)
+        const unsigned mbits = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+        const int ex = (int)((mbits >> 23) & 0xffu);  // biased exponent of the row maximum
+        const int sh = ex == 0 ? 0 : min(max(136 - ex, -126), 126);  // 2^sh: 2^(9 - (ex - 127))
+        const float s_in = __int_as_float((127 + sh) << 23);
+        const float s_out = __int_as_float((127 - sh) << 23) * img_scale;
+        // B fragments of [Xr; Xi]: k-step 0 real parts, k-step 1 imaginary parts
+        uint32_t xb_h[2][2][2], xb_l[2][2][2];  // [k-step][n-tile][reg]
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const float2 lo = z[nt][2 * r], hi = z[nt][2 * r + 1];
+                split_pair(lo.x * s_in, hi.x * s_in, xb_h[0][nt][r], xb_l[0][nt][r]);
+                split_pair(lo.y * s_in, hi.y * s_in, xb_h[1][nt][r], xb_l[1][nt][r]);
+            }
+        // Y = F16 X: rows k1 (m-tile 0 real, m-tile 1 imaginary), columns n2
+        float yr[2][4] = {}, yi[2][4] = {};
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+            mma_split(yr[nt], frA_h, frA_l, xb_h[0][nt][0], xb_h[0][nt][1], xb_l[0][nt][0], xb_l[0][nt][1]);
+            mma_split(yr[nt], nfiA_h, nfiA_l, xb_h[1][nt][0], xb_h[1][nt][1], xb_l[1][nt][0], xb_l[1][nt][1]);
+            mma_split(yi[nt], fiA_h, fiA_l, xb_h[0][nt][0], xb_h[0][nt][1], xb_l[0][nt][0], xb_l[0][nt][1]);
+            mma_split(yi[nt], frA_h, frA_l, xb_h[1][nt][0], xb_h[1][nt][1], xb_l[1][nt][0], xb_l[1][nt][1]);
+        }
+        // twiddles exp(+2 pi i k1 n2 / 256); element e: k1 = g + 8 (e >> 1), n2 = 8 nt + 2t + (e & 1)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int k1 = g + 8 * (e >> 1), n2 = 8 * nt + 2 * t + (e & 1);
+                const float2 w = w256[(k1 * n2) & 255];
+                const float re = yr[nt][e], im = yi[nt][e];
+                yr[nt][e] = re * w.x - im * w.y;
+                yi[nt][e] = re * w.y + im * w.x;
+            }
+        // A fragments of [Y'r | Y'i] (k-step 0 real, 1 imaginary): the accumulators as they lie
+        uint32_t ya_h[2][4], ya_l[2][4];
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+            const float(*y)[4] = ks ? yi : yr;
+            split_pair(y[0][0], y[0][1], ya_h[ks][0], ya_l[ks][0]);
+            split_pair(y[0][2], y[0][3], ya_h[ks][1], ya_l[ks][1]);
+            split_pair(y[1][0], y[1][1], ya_h[ks][2], ya_l[ks][2]);
+            split_pair(y[1][2], y[1][3], ya_h[ks][3], ya_l[ks][3]);
+        }
+        // Z = Y' F16: column tiles q = 0, 1 real parts (k2 = 8q + ..), q = 2, 3 imaginary parts
+        float zo[4][4] = {};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            // real: Y'r Fr - Y'i Fi
+            mma_split(zo[q], ya_h[0], ya_l[0], frB_h[q][0], frB_h[q][1], frB_l[q][0], frB_l[q][1]);
+            mma_split(zo[q], ya_h[1], ya_l[1], fiB_h[q][0] ^ 0x80008000u, fiB_h[q][1] ^ 0x80008000u,
+                      fiB_l[q][0] ^ 0x80008000u, fiB_l[q][1] ^ 0x80008000u);
+            // imaginary: Y'r Fi + Y'i Fr
+            mma_split(zo[q + 2], ya_h[0], ya_l[0], fiB_h[q][0], fiB_h[q][1], fiB_l[q][0], fiB_l[q][1]);
+            mma_split(zo[q + 2], ya_h[1], ya_l[1], frB_h[q][0], frB_h[q][1], frB_l[q][0], frB_l[q][1]);
+        }
+        // z_out[m], m = k1 + 16 k2 -> pixels 2m, 2m+1 (fftshift of columns: x -> (x + N/2) mod N)
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int k1 = g + 8 * (e >> 1), k2 = 8 * q + 2 * t + (e & 1);
+                const int m = k1 + 16 * k2;
+                const int x = (2 * m + N / 2) & (N - 1);
+                const float vr = zo[q][e] * s_out, vi = zo[q + 2][e] * s_out;
+                if (REAL)
+                    __stcs(reinterpret_cast<float2 *>(reinterpret_cast<float *>(images) + row * N + x),
+                           make_float2(vr, vi));
+                else
+                    __stcs(reinterpret_cast<float4 *>(images + row * N + x), make_float4(vr, 0.f, vi, 0.f));
+            }
+    }
+    if (threadIdx.x == 0) bulk_wait_all();
+}
+
 template <class K>
 int prepare(K kernel, size_t smem) {
     if (smem > 48 * 1024) {
@@ -649,13 +885,21 @@ int cols_half_n(float2 *grids, int n_images, int ext_u, int ext_v, cudaStream_t 
 
 template <int N>
 int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum, int ext_u, bool real,
-          cudaStream_t s) {
+          cudaStream_t s, bool tensor = false) {
     using S = C2RShape<N>;
     const size_t smem = c2r_smem_bytes<N>();
     const unsigned blocks = (unsigned)((size_t)n_images * N / S::ROWS);
     // columns 0..ext_u, rounded up to 16 bytes: a multiple of 16 no larger than the staged row
     const int eu = ext_u < 0 ? 0 : (ext_u > N / 2 ? N / 2 : ext_u);
     const unsigned copy_bytes = std::min(c2r_row_bytes<N>(), (unsigned)(((eu + 1) * sizeof(float2) + 15) & ~(size_t)15));
+    if constexpr (N == 512) {
+        if (tensor) {  // the length-256 transforms on the tensor cores
+            auto kt = real ? c2r_rows_tc_kernel<N, true> : c2r_rows_tc_kernel<N, false>;
+            kt<<<(unsigned)((size_t)n_images * N / kTcRows), kTcThreads, c2r_tc_smem_bytes<N>(), s>>>(grids, images, wsum,
+                                                                                                  copy_bytes);
+            return check_launch("fft rows (complex to real, tensor cores)");
+        }
+    }
     auto k = real ? c2r_rows_kernel<N, true> : c2r_rows_kernel<N, false>;
     int st = prepare(k, smem);
     if (st) return st;
@@ -793,14 +1037,16 @@ int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_
     }
 }
 
+bool c2r_tensor_supported(int n) { return n == 512; }
+
 int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum, int ext_u,
-                    cudaStream_t s, bool real) {
+                    cudaStream_t s, bool real, bool tensor) {
     if (n_images <= 0) return BGI_OK;
     switch (n) {
         case 64: return c2r_n<64>(grids, images, n_images, wsum, ext_u, real, s);
         case 128: return c2r_n<128>(grids, images, n_images, wsum, ext_u, real, s);
         case 256: return c2r_n<256>(grids, images, n_images, wsum, ext_u, real, s);
-        case 512: return c2r_n<512>(grids, images, n_images, wsum, ext_u, real, s);
+        case 512: return c2r_n<512>(grids, images, n_images, wsum, ext_u, real, s, tensor);
         case 1024: return c2r_n<1024>(grids, images, n_images, wsum, ext_u, real, s);
         case 2048: return c2r_n<2048>(grids, images, n_images, wsum, ext_u, real, s);
         case 4096: return c2r_n<4096>(grids, images, n_images, wsum, ext_u, real, s);

@@ -127,8 +127,11 @@ int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_
 // imaginary parts and must be 16-byte aligned.  Columns beyond ext_u are zero in the grid (the
 // bound of launch_fft_cols_half; N/2 for none): they are neither read nor cleared.
 // real: images are float[N][N] (8-byte aligned) instead of complex.
+// tensor: the length-N/2 transforms as split-FP16 DFT products on the tensor cores (sides with
+// c2r_tensor_supported only; others ignore it).
 int launch_c2r_rows(float2 *grids, float2 *images, int n, int n_images, const unsigned int *wsum, int ext_u,
-                    cudaStream_t s, bool real = false);
+                    cudaStream_t s, bool real = false, bool tensor = false);
+bool c2r_tensor_supported(int n);
 int launch_shift_and_norm(float2 *images, int x_side, int y_side, int n_images,
                           const float *fnorm, int fnorm_size, cudaStream_t s);
 int launch_vector_sum(const float *data, int64_t image_size, int n_images, float *sums,

@@ -360,6 +360,17 @@ class Imager:
         """0: nearest neighbour; 1..16: the reference's Kaiser-Bessel convolution kernel."""
         call("bgi_set_gridding_kernel", self._h, int(kernel_size), int(bool(with_sinc)))
 
+    def set_fft_mode(self, mode: str = "simt"):
+        """"simt" (FP32 passes) or "tensor_split16" (the complex-to-real pass's transforms as
+        split-FP16 DFT products on the tensor cores; image side 512)."""
+        call("bgi_set_fft_mode", self._h, capi.FFT_MODE[mode])
+
+    @property
+    def fft_mode(self) -> str:
+        m = C.c_int()
+        call("bgi_get_fft_mode", self._h, C.byref(m))
+        return {v: k for k, v in capi.FFT_MODE.items()}[m.value]
+
     def set_deterministic(self, enable: bool = True):
         """Grid by sort and ordered per-cell sums (full plane): the same image bits on every run."""
         call("bgi_set_deterministic", self._h, int(bool(enable)))

@@ -377,6 +377,18 @@ BGI_API int bgi_image_noalloc(const float *vis, int n_ant, int n_channels, int n
 BGI_API int bgi_device_fault(int device, unsigned int *fault_bits, int clear);
 BGI_API int bgi_selftest_wait_timeout(int device, void *stream);
 
+/* Arithmetic of the inverse FFT's last pass on the half-plane path (no reference counterpart).
+ * BGI_FFT_SIMT (default): FP32 radix-16/32 Stockham passes on the CUDA cores.
+ * BGI_FFT_TENSOR_SPLIT16: the complex-to-real row pass's length-N/2 transforms as two dense
+ *   16-point DFT products on the tensor cores (warp-level mma.sync, FP16 operands, FP32
+ *   accumulation), every operand split into FP16 hi + lo parts (three products: lo*hi, hi*lo,
+ *   hi*hi), each row scaled by a power of two into FP16's range; about 22 significant bits per
+ *   operand, so images stay within ~1e-6 relative L2 of the FP32 passes.  Image side 512 only
+ *   (BGI_ERR_UNSUPPORTED otherwise); full-plane calls keep the FP32 passes. */
+enum bgi_fft_mode { BGI_FFT_SIMT = 0, BGI_FFT_TENSOR_SPLIT16 = 1 };
+BGI_API int bgi_set_fft_mode(bgi_imager *im, int mode);
+BGI_API int bgi_get_fft_mode(const bgi_imager *im, int *mode);
+
 /* Launch schedule of the bgi_image* calls: images per wave (0 = auto: about 26 MiB of grid
  * per lane, 24 half-plane images at 512^2) and lanes (1..8 streams that image alternate waves,
  * each with its own grid scratch; 2 by default).  bgi_autotune times every wave size in
