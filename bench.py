@@ -572,16 +572,13 @@ def run_ours(args, rank, world, local_rank):
         # N GPUs: one observation of N blocks' intervals, split by the library's shard plan (each
         # rank images its own intervals with the whole observation's uv cell; no collective on
         # the data path) -- weak scaling, the same 64 x args.intervals images per GPU
-        import dataclasses
         from imager_gb300 import shard as SH
         whole = synth.config2(device="cuda", n_intervals=args.intervals * world)
         probe = Imager(whole.n_pixels, 2.0, "XX", -1000.0)
         probe.set_array(whole.u, whole.v, whole.w, whole.flags, whole.cable)
         whole_cell = probe.uv_cell[:2]
         probe.close()
-        part = SH.plan_shard(whole.n_intervals, whole.n_channels, world, rank)
-        vis_s, u_s, v_s, w_s, f_s = SH.shard_inputs(whole, part)
-        obs = dataclasses.replace(whole, vis=vis_s, u=u_s, v=v_s, w=w_s, freqs=f_s)
+        _, obs = SH.shard_observation(whole, world, rank)
         del whole
     T, Cn, B = obs.vis.shape[:3]
     N = obs.n_pixels

@@ -8,6 +8,7 @@ needs communication.
 """
 from __future__ import annotations
 
+import dataclasses
 from dataclasses import dataclass
 
 import numpy as np
@@ -60,3 +61,13 @@ def assemble(parts, shards, n_intervals: int, n_channels: int, n_pixels: int):
     for img, s in zip(parts, shards):
         out[s.t0:s.t1, s.c0:s.c1] = img
     return out
+
+
+def shard_observation(obs, world: int, rank: int):
+    """(shard, the observation restricted to it): rank `rank`'s share of `obs` as an Observation
+    of its own (visibilities, UVW sets and frequencies of the shard; array, flags and cable
+    lengths unchanged).  The rank images it with the whole observation's uv cell
+    (Imager.set_uv_cell), so its images are the whole observation's images of that share."""
+    sh = plan_shard(obs.n_intervals, obs.n_channels, world, rank)
+    vis, u, v, w, freqs = shard_inputs(obs, sh)
+    return sh, dataclasses.replace(obs, vis=vis, u=u, v=v, w=w, freqs=freqs)
