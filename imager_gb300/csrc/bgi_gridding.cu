@@ -178,9 +178,157 @@ bool one_set(const GridParams &q, int cpt) {
     return q.n_uvw_sets == 1 || (q.n_channels % cpt == 0 && q.img_begin % cpt == 0);
 }
 
+// ---- the half-plane gridding of the imaging handle, lean form ---------------------------------
+// The same work as grid_kernel<HALF, ONE_SET> for the handle's common case -- half-plane grids,
+// the CPT images of a block sharing one UVW set, the channel-constant table, no min_uv cut, no
+// counter grids -- with fewer instructions per visibility:
+//  * 64-bit addresses are formed once per block (the block's first image); a thread adds 32-bit
+//    offsets (j * 4 * B + b < 2^31 and (j * N + v) * W + u < 2^31, checked on the host);
+//  * rounding to the nearest integer (ties to even, as rintf) and the conversion to int use the
+//    exact FP32 addition of 1.5 * 2^23 (valid for |x| < 2^22; larger values take the exact FP64
+//    path), so no rounding or float-to-int conversion instruction is issued;
+//  * the weight count of a thread is the number of its gridded visibilities times two.
+// The cell indices are the same integers (the same filter, the same exact fallback).
+#ifndef GRID_LEAN
+#define GRID_LEAN 1
+#endif
+constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
+
+// rint(x) as a float and as an int, and whether it is certainly the reference's rounding of the
+// exact value (x within |x| * 2^-21 of it; see round_certain)
+__device__ __forceinline__ bool round_certain_lean(float x, int *i) {
+    const float t = __fadd_rn(x, kRoundMagic);
+    const float r = __fsub_rn(t, kRoundMagic);  // rint(x) for |x| < 2^22
+    *i = __float_as_int(t) - 0x4B400000;
+    const float d = 0.5f - fabsf(x - r);
+    return d > fabsf(x) * 4.76837158e-7f + 1e-30f && fabsf(x) < 4194304.0f;  // 2^-21, |x| < 2^22
+}
+
+template <int POL, int FMT, int CPT>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) grid_half_lean_kernel(const GridParams p) {
+    __shared__ unsigned int s_count[CPT][kThreads / 32];
+    constexpr int P0 = POL == BGI_POL_XX ? 0 : POL == BGI_POL_YY ? 3 : POL == BGI_POL_I ? 0 : 1;  // planes
+    constexpr int P1 = POL == BGI_POL_I ? 3 : 2;
+    constexpr bool TWO = POL == BGI_POL_I || POL == BGI_POL_V;
+    const int img_first = p.img_begin + blockIdx.y * CPT;
+    const int n_here = min(CPT, p.img_begin + p.img_count - img_first);
+    const int nb = (int)p.n_baselines;
+    const int b = blockIdx.x * kThreads + threadIdx.x;
+    const bool in_range = b < nb;
+    const int ch_first = img_first % p.n_channels;
+    const int t_first = img_first / p.n_channels;
+    const int n = p.n_pixels, w = p.half_width;
+    // ---- loads -------------------------------------------------------------------------------
+    int flag = 1;
+    float2 pa[CPT], pb[CPT];
+    float4 hot[CPT];
+    float u = 0.f, v = 0.f, wv = 0.f;
+    float2 dl = make_float2(0.f, 0.f);
+    if (in_range) {
+        flag = p.flags[b];
+        if (p.apply_cable) dl = p.dl[b];
+        const size_t set_off = p.n_uvw_sets > 1 ? (size_t)t_first * nb : 0;
+        u = p.u[set_off + b];
+        v = p.v[set_off + b];
+        if (p.apply_geom) wv = p.w[set_off + b];
+        if (FMT == BGI_VIS_C64) {
+            const float2 *rec = reinterpret_cast<const float2 *>(p.vis) + (size_t)img_first * nb * 4;
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                pa[j] = pb[j] = make_float2(0.f, 0.f);
+                if (j < n_here) load_pols<POL>(rec + (unsigned)(j * nb + b) * 4u, pa[j], pb[j]);
+            }
+        } else {
+            const uint32_t *d = reinterpret_cast<const uint32_t *>(p.vis) + (size_t)img_first * 4 * nb;
+            const int nblk = (int)p.vis_blocks;
+            const float *sc = p.vis_scales + (size_t)img_first * 4 * nblk;
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                pa[j] = pb[j] = make_float2(0.f, 0.f);
+                if (j < n_here) {
+                    const unsigned o = (unsigned)(j * 4 * nb + b), os = (unsigned)(j * 4 * nblk + (b >> 7));
+                    pa[j] = decode_vis<FMT>(__ldcs(d + o + P0 * nb), __ldg(sc + os + P0 * nblk));
+                    if (TWO) pb[j] = decode_vis<FMT>(__ldcs(d + o + P1 * nb), __ldg(sc + os + P1 * nblk));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+        int ch = ch_first + j;
+        if (ch >= p.n_channels) ch %= p.n_channels;
+        hot[j] = __ldg(reinterpret_cast<const float4 *>(p.chan_consts + ch));
+    }
+    const bool corr = p.apply_geom || p.apply_cable;
+    float d_hi = 0.f, d_lo = 0.f;
+    if (corr) delay_df(wv, dl.x, dl.y, d_hi, d_lo);
+    float2 *gbase = p.grids + (size_t)(img_first - p.img_base) * n * w;
+    unsigned int counted[CPT];
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+        counted[j] = 0;
+        if (j >= n_here) break;  // uniform across the block
+        if (in_range && flag <= 0) {
+            float2 z = combine_pols<POL>(pa[j], pb[j]);
+            if (corr) z = rotate(z, phasor_df(d_hi, d_lo, hot[j].z, hot[j].w));
+            const float xu = u * hot[j].x, xv = v * hot[j].y;
+            int ui, vi;
+            const bool cu = round_certain_lean(xu, &ui), cv = round_certain_lean(xv, &vi);
+            bool ok = !isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis;
+            if (ok && !(cu && cv)) {  // within the FP32 bound of a half-integer: the exact recipe
+                int ch = ch_first + j;
+                if (ch >= p.n_channels) ch %= p.n_channels;
+                double up, vp;
+                const ChannelConst *ccp = p.chan_consts + ch;
+                ok = uv_pixels_exact(u, v, ccp->wavelength, p.du, p.dv, p.min_uv, &up, &vp) &&
+                     fabs(up) < 1073741824.0 && fabs(vp) < 1073741824.0;
+                ui = (int)up;
+                vi = (int)vp;
+            }
+            if (ok) {
+                // both mirror cells exist (every pixel coordinate is below N on this path)
+                const int u1 = ui + (n & (ui >> 31)), v1 = vi + (n & (vi >> 31));
+                const int u2 = -ui + (n & (-ui >> 31)), v2 = -vi + (n & (-vi >> 31));
+                float2 *g = gbase + (unsigned)(j * n * w);
+                if (u1 <= n / 2) atomicAdd(g + (unsigned)(v1 * w + u1), z);
+                if (u2 <= n / 2) atomicAdd(g + (unsigned)(v2 * w + u2), make_float2(z.x, -z.y));
+                counted[j] = 2;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+        if (j >= n_here) break;
+        const unsigned int warp_total = __reduce_add_sync(0xffffffffu, counted[j]);
+        if ((threadIdx.x & 31) == 0) s_count[j][threadIdx.x >> 5] = warp_total;
+    }
+    __syncthreads();
+    if (threadIdx.x < n_here) {
+        unsigned int total = 0;
+#pragma unroll
+        for (int k = 0; k < kThreads / 32; ++k) total += s_count[threadIdx.x][k];
+        if (total) atomicAdd(p.wsum + (size_t)(img_first + threadIdx.x - p.img_base) * kWsumStride, total);
+    }
+}
+
+// whether the lean kernel applies to a launch (its preconditions; else grid_kernel runs)
+bool lean_applies(const GridParams &q, int cpt) {
+    if (!GRID_LEAN || q.half_width <= 0 || !q.chan_consts || q.min_uv >= 0.0 || q.counter_mode >= 0 || !q.wsum ||
+        q.kb_size > 0)
+        return false;
+    const long long nb = q.n_baselines;
+    const long long per_image_grid = (long long)q.n_pixels * q.half_width;
+    const bool one = q.n_uvw_sets == 1 || (q.n_channels % cpt == 0 && q.img_begin % cpt == 0);
+    return one && nb < (1LL << 27) && (long long)cpt * 4 * nb < (1LL << 31) && cpt * per_image_grid < (1LL << 31);
+}
+
 template <int POL, int FMT, int CPT>
 void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
     const bool one = one_set(q, CPT);
+    if (lean_applies(q, CPT)) {
+        grid_half_lean_kernel<POL, FMT, CPT><<<grid, kThreads, 0, s>>>(q);
+        return;
+    }
     if (q.half_width > 0) {
         if (one) grid_kernel<POL, false, true, FMT, true, CPT><<<grid, kThreads, 0, s>>>(q);
         else grid_kernel<POL, false, true, FMT, false, CPT><<<grid, kThreads, 0, s>>>(q);
