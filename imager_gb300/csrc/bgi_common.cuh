@@ -156,8 +156,12 @@ __device__ __forceinline__ float2 decode_vis(uint32_t e, float scale) {
     const uint16_t r = (uint16_t)(e & 0xffffu), i = (uint16_t)(e >> 16);
     float x, y;
     if (FMT == BGI_VIS_S16) {
-        x = r == 0x8000u ? __int_as_float(0x7fc00000) : (float)(int16_t)r;
-        y = i == 0x8000u ? __int_as_float(0x7fc00000) : (float)(int16_t)i;
+        // int16 -> float without a conversion instruction: the float whose bits are
+        // 0x4B400000 + k is 1.5 * 2^23 + k for |k| < 2^22, so subtracting 1.5 * 2^23 is exact
+        const float xf = __fsub_rn(__int_as_float(0x4B400000 + (int)(int16_t)r), 12582912.0f);
+        const float yf = __fsub_rn(__int_as_float(0x4B400000 + (int)(int16_t)i), 12582912.0f);
+        x = r == 0x8000u ? __int_as_float(0x7fc00000) : xf;
+        y = i == 0x8000u ? __int_as_float(0x7fc00000) : yf;
     } else if (FMT == BGI_VIS_BF16) {
         x = __uint_as_float((uint32_t)r << 16);
         y = __uint_as_float((uint32_t)i << 16);
@@ -237,7 +241,10 @@ __device__ __forceinline__ float2 phasor_df(float d_hi, float d_lo, float f_hi, 
     float e = fmaf(d_hi, f_hi, -p);
     e = fmaf(d_hi, f_lo, e);
     e = fmaf(d_lo, f_hi, e);
-    const float r = (p - rintf(p)) + e;
+    // p - rint(p), with rint by the exact addition of 1.5 * 2^23 (valid for |p| < 2^22 turns, a
+    // delay of thousands of kilometres; beyond it rintf)
+    const float ip = fabsf(p) < 4194304.0f ? __fsub_rn(__fadd_rn(p, 12582912.0f), 12582912.0f) : rintf(p);
+    const float r = (p - ip) + e;
     // |2*pi*r| <= pi: the SFU sine/cosine is accurate to 2^-21.4 absolute on [-pi, pi]
     float s, c;
     __sincosf(6.28318530717958648f * r, &s, &c);

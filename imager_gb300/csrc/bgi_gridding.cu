@@ -31,7 +31,10 @@ constexpr int kMinBlocks = 768 / GRID_THREADS;  // resident blocks per SM the re
 // 4 above (512 antennas, the uneven batch: 9.26 ms against 9.77 with 2) -- small arrays need the
 // extra blocks, large ones the loads shared by more visibilities.
 constexpr long long kCpt4Baselines = 65536;
-int images_per_thread(long long n_baselines) { return n_baselines >= kCpt4Baselines ? 4 : 2; }
+#ifndef GRID_CPT_SMALL
+#define GRID_CPT_SMALL 2
+#endif
+int images_per_thread(long long n_baselines) { return n_baselines >= kCpt4Baselines ? 4 : GRID_CPT_SMALL; }
 
 // CPT: images per thread.  ONE_SET: the CPT images of every block share one UVW set (one set, or
 // blocks that start at multiples of CPT with CPT dividing the channel count), so a thread loads
