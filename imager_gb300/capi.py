@@ -86,6 +86,8 @@ _SIGNATURES = {
     "bgi_vector_sum_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_uniform_weighting_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
     "bgi_set_fft_mode": (_i, [_vp, _i]),
+    "bgi_set_gridding_images_per_thread": (_i, [_vp, _i]),
+    "bgi_get_gridding_images_per_thread": (_i, [_vp, _vp]),
     "bgi_get_fft_mode": (_i, [_vp, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_create": (_i, [C.POINTER(Config), C.POINTER(_vp)]),

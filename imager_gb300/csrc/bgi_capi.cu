@@ -152,6 +152,7 @@ struct bgi_imager {
     DevBuf<ChannelConst> d_cc; // per-channel gridding constants for the current delta_u/v
     int kb_size = 0;           // Kaiser-Bessel kernel size (0: nearest neighbour)
     int fft_mode = BGI_FFT_SIMT;  // enum bgi_fft_mode
+    int grid_cpt = 0;             // gridding images per thread (0: by array size)
     DevBuf<float> kb_table;    // its rows [1023][kb_size]
     bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
@@ -761,6 +762,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.half_width = im->half_plane_path() ? half_plane_width(im->cfg.n_pixels) : 0;
     p.kb_size = im->kb_size;
     p.kb_table = im->kb_table.ptr;
+    p.cpt = im->grid_cpt;
     // the complex-to-real pass stores pixel pairs: 16 bytes of complex or 8 bytes of real pixels
     if ((reinterpret_cast<uintptr_t>(images) & ((flags & BGI_OUTPUT_REAL) ? 7u : 15u)) != 0) p.half_width = 0;
     // uniform weighting divides cells by their counters: full-plane grids with counter grids
@@ -1033,26 +1035,63 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     BGI_TRY(check_cuda(cudaEventCreate(&e0), "autotune event"));
     int st = check_cuda(cudaEventCreate(&e1), "autotune event");
+    // milliseconds per call of the handle's current schedule: one call to size the scratch, then
+    // three timed with CUDA events on the stream
+    auto time_current = [&](float *ms) {
+        int r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+        if (!r) r = check_cuda(cudaEventRecord(e0, s), "autotune record");
+        for (int rep = 0; !r && rep < 3; ++rep) r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+        if (!r) r = check_cuda(cudaEventRecord(e1, s), "autotune record");
+        if (!r) r = check_cuda(cudaEventSynchronize(e1), "autotune sync");
+        float t = 0.f;
+        if (!r) r = check_cuda(cudaEventElapsedTime(&t, e0, e1), "autotune elapsed");
+        *ms = t / 3.f;
+        return r;
+    };
     static const int kWaves[] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64};
     int best_wave = im->cfg.max_images_per_wave, best_lanes = im->lanes;
+    int best_cpt = im->grid_cpt, best_fft = im->fft_mode;
     float best = 3.4e38f;
+    // 1. images per wave x lanes, with the gridding and FFT defaults
+    im->grid_cpt = 0;
+    im->fft_mode = BGI_FFT_SIMT;
     for (int wi = 0; !st && wi < (int)(sizeof(kWaves) / sizeof(kWaves[0])); ++wi) {
         if (kWaves[wi] > n_images) break;
         for (int lanes = 1; !st && lanes <= bgi_imager::kLanes; ++lanes) {
             im->cfg.max_images_per_wave = kWaves[wi];
             im->lanes = lanes;
-            st = image_impl(im, format, data, scales, n_intervals, flags, images, stream);  // sizes the scratch
-            if (!st) st = check_cuda(cudaEventRecord(e0, s), "autotune record");
-            for (int rep = 0; !st && rep < 3; ++rep) st = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
-            if (!st) st = check_cuda(cudaEventRecord(e1, s), "autotune record");
-            if (!st) st = check_cuda(cudaEventSynchronize(e1), "autotune sync");
             float ms = 0.f;
-            if (!st) st = check_cuda(cudaEventElapsedTime(&ms, e0, e1), "autotune elapsed");
-            if (!st && ms / 3.f < best) {
-                best = ms / 3.f;
+            st = time_current(&ms);
+            if (!st && ms < best) {
+                best = ms;
                 best_wave = kWaves[wi];
                 best_lanes = lanes;
+                best_cpt = 0;
+                best_fft = BGI_FFT_SIMT;
             }
+        }
+    }
+    // 2. at the best wave and lanes: gridding images per thread, then the last FFT pass's arithmetic
+    im->cfg.max_images_per_wave = best_wave;
+    im->lanes = best_lanes;
+    for (int cpt : {2, 4}) {
+        if (st) break;
+        im->grid_cpt = cpt;
+        float ms = 0.f;
+        st = time_current(&ms);
+        if (!st && ms < best) {
+            best = ms;
+            best_cpt = cpt;
+        }
+    }
+    im->grid_cpt = best_cpt;
+    if (!st && c2r_tensor_supported(im->cfg.n_pixels) && im->half_plane_path()) {
+        im->fft_mode = BGI_FFT_TENSOR_SPLIT16;
+        float ms = 0.f;
+        st = time_current(&ms);
+        if (!st && ms < best) {
+            best = ms;
+            best_fft = BGI_FFT_TENSOR_SPLIT16;
         }
     }
     cudaEventDestroy(e0);
@@ -1060,6 +1099,8 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     im->timing = timing;
     im->cfg.max_images_per_wave = best_wave;
     im->lanes = best_lanes;
+    im->grid_cpt = best_cpt;
+    im->fft_mode = best_fft;
     if (st) return st;
     // drop the candidates' scratch; the chosen schedule sizes its own on the next call
     BGI_TRY(check_cuda(cudaStreamSynchronize(s), "autotune sync"));
@@ -1070,6 +1111,19 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
         im->grid_dirty[l] = false;
     }
     if (best_ms) *best_ms = best;
+    return BGI_OK;
+}
+
+int bgi_set_gridding_images_per_thread(bgi_imager *im, int images_per_thread) {
+    if (!im || (images_per_thread != 0 && images_per_thread != 2 && images_per_thread != 4))
+        return set_error(BGI_ERR_INVALID, "set_gridding_images_per_thread: 0 (auto), 2 or 4");
+    im->grid_cpt = images_per_thread;
+    return BGI_OK;
+}
+
+int bgi_get_gridding_images_per_thread(const bgi_imager *im, int *images_per_thread) {
+    if (!im || !images_per_thread) return set_error(BGI_ERR_INVALID, "get_gridding_images_per_thread: bad arguments");
+    *images_per_thread = im->grid_cpt;
     return BGI_OK;
 }
 

@@ -409,7 +409,7 @@ int launch_gridding(const GridParams &p, cudaStream_t s) {
     }
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;
     const int max_groups = 65535;
-    const int cpt = images_per_thread(p.n_baselines);
+    const int cpt = p.cpt == 2 || p.cpt == 4 ? p.cpt : images_per_thread(p.n_baselines);
     for (int done = 0; done < p.img_count; done += max_groups * cpt) {
         GridParams q = p;
         q.img_begin = p.img_begin + done;

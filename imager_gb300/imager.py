@@ -360,6 +360,16 @@ class Imager:
         """0: nearest neighbour; 1..16: the reference's Kaiser-Bessel convolution kernel."""
         call("bgi_set_gridding_kernel", self._h, int(kernel_size), int(bool(with_sinc)))
 
+    def set_gridding_images_per_thread(self, k: int = 0):
+        """Images per gridding thread: 2 or 4 (0: by array size)."""
+        call("bgi_set_gridding_images_per_thread", self._h, int(k))
+
+    @property
+    def gridding_images_per_thread(self) -> int:
+        k = C.c_int()
+        call("bgi_get_gridding_images_per_thread", self._h, C.byref(k))
+        return k.value
+
     def set_fft_mode(self, mode: str = "simt"):
         """"simt" (FP32 passes) or "tensor_split16" (the complex-to-real pass's transforms as
         split-FP16 DFT products on the tensor cores; image side 512)."""

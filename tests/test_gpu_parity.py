@@ -523,8 +523,15 @@ def test_schedule_and_autotune(im):
     with pytest.raises(capi.BgiError):
         h.set_schedule(8, 9)
     h.set_deterministic(False)
+    for cpt in (2, 4, 0):  # images per gridding thread (0: by array size)
+        h.set_gridding_images_per_thread(cpt)
+        assert h.gridding_images_per_thread == cpt
+        assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6, cpt
+    with pytest.raises(capi.BgiError):
+        h.set_gridding_images_per_thread(3)
     wave, lanes, ms = h.autotune(vis)
     assert wave in (0, 4, 8, 12) and 1 <= lanes <= 8 and ms > 0
+    assert h.gridding_images_per_thread in (0, 2, 4) and h.fft_mode == "simt"  # no tensor pass at 128
     assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6
     h.close()
 

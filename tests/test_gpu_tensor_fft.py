@@ -101,6 +101,21 @@ def test_tensor_rows_dynamic_range(im):
         h.close()
 
 
+def test_autotune_chooses_among_fft_modes(im):
+    """bgi_autotune at 512 also times the tensor-core row pass; whatever it keeps images the
+    block within tolerance."""
+    obs = synth.small(seed=515, n_ant=48, n_intervals=2, n_channels=4, n_pixels=512)
+    vis = obs.vis_f32()
+    _, _, _, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, 512, n_uvw_sets=2)
+    h, _ = _pair(im, obs)
+    wave, lanes, ms = h.autotune(dev(vis))
+    assert ms > 0 and h.fft_mode in ("simt", "tensor_split16") and h.gridding_images_per_thread in (0, 2, 4)
+    out = h.image(dev(vis)).cpu().numpy()
+    for i in range(2):
+        for j in range(4):
+            assert rel_l2(out[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+
+
 def test_tensor_mode_rejected_off_512(im):
     from imager_gb300 import capi
     h = im.Imager(256)
