@@ -611,6 +611,8 @@ def run_ours(args, rank, world, local_rank):
             tuned = im.autotune(vis, None, "c64", flags=flags, out=out)
         else:
             tuned = im.autotune(stored[fmt][0], stored[fmt][1], fmt, flags=flags, out=out)
+    if args.fft_mode:
+        im.set_fft_mode(args.fft_mode)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -658,6 +660,7 @@ def run_ours(args, rank, world, local_rank):
             variants[f"storage_{f}"] = {"images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms,
                                         "steps": k, **({"errors_vs_fp64": image_errors(out, refs)} if rank == 0 else {})}
         # the complex-to-real pass on the tensor cores (split-FP16 DFT products), same step
+        step_mode = im.fft_mode
         im.set_fft_mode("tensor_split16")
         v_ms = time_steps(step, k, stream, flush)
         tc_errs = image_errors(out, refs) if rank == 0 else {}
@@ -665,7 +668,7 @@ def run_ours(args, rank, world, local_rank):
         timed_steps(step, stage_steps, stream, flush)
         tc_stages = im.stage_times()
         im.set_stage_timing(False)
-        im.set_fft_mode("simt")
+        im.set_fft_mode(step_mode)
         tc_pass2 = tc_stages.get("fft_pass2", (0.0, 0))
         variants["fft_tensor_split16"] = {
             "images_per_s": world * n_images / (v_ms / 1000.0), "ms_per_step": v_ms, "steps": k, "storage": fmt,
@@ -950,6 +953,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--storage", choices=["s16", "bf16", "fp16", "c64"], default="s16",
                     help="visibility storage of the timed step (s16: 16-bit block floating point)")
+    ap.add_argument("--fft-mode", choices=["simt", "tensor_split16"], default=None,
+                    help="force the FFT arithmetic of the timed step (default: the autotuner's choice)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default schedule (auto wave, two lanes) instead of bgi_autotune's")
     ap.add_argument("--no-serving", dest="serving", action="store_false", help="skip the serving measurement")
