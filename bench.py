@@ -549,7 +549,7 @@ def precision_measure(args, stream, flush):
             else "complex64",
             "sampled_images": [f"interval {t}, channel {c}" for t, c in samples],
             "oracle": "FP64 oracle of the original complex64 visibilities",
-            "fft": "FP32 Stockham passes of our own (no tensor-core DFT stages)",
+            "fft": "FP32 Stockham passes of our own (the tensor-core row pass is built for 512^2 only)",
             "formats": formats}
 
 
