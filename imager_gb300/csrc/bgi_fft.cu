@@ -183,7 +183,20 @@ __device__ __forceinline__ float2 tw_load(const float2 *tw, int i) {
     else return __ldg(tw + i);
 }
 
-template <int N, int R, bool WARP, bool ALIASED, bool TWS = false, class GLoad, class GStore, class GClear = NoClear>
+// w[m] = w1^m for m = 1..R-1, by squarings and single multiplications (at most log2(R) + 1
+// products deep, so a few float roundings from the exact power).
+template <int R>
+__device__ __forceinline__ void twiddle_powers(float2 w1, float2 *w) {
+    w[1] = w1;
+#pragma unroll
+    for (int m = 2; m < R; ++m) w[m] = (m & 1) ? cmul(w[m - 1], w1) : cmul(w[m / 2], w[m / 2]);
+}
+
+// TWPOW: each pass reads only its m = 1 twiddle, exp(+2*pi*i*k/(Ns*R)) (or exp(+2*pi*i*j/N) in the
+// final radix-R2 pass), and forms the others as its powers in registers: one table load per pass
+// instead of R - 1.
+template <int N, int R, bool WARP, bool ALIASED, bool TWS = false, bool TWPOW = false, class GLoad, class GStore,
+          class GClear = NoClear>
 __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *tw, GLoad gload,
                                               GStore gstore, GClear gclear = GClear()) {
     using C = FftCfg<N, R>;
@@ -202,8 +215,15 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
     for (int p = 0; p < C::NFULL; ++p) {
         const int k = t & (Ns - 1);
         if (p > 0) {
+            if constexpr (TWPOW) {
+                float2 w[R];
+                twiddle_powers<R>(tw_load<TWS>(tw, toff + k), w);
 #pragma unroll
-            for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw_load<TWS>(tw, toff + (m - 1) * Ns + k));
+                for (int m = 1; m < R; ++m) a[m] = cmul(a[m], w[m]);
+            } else {
+#pragma unroll
+                for (int m = 1; m < R; ++m) a[m] = cmul(a[m], tw_load<TWS>(tw, toff + (m - 1) * Ns + k));
+            }
             toff += (R - 1) * Ns;
         }
         dft<R>(a);
@@ -235,9 +255,16 @@ __device__ __forceinline__ void fft_transform(int t, float2 *sm, const float2 *t
         for (int q = 0; q < R / R2; ++q) {
             const int j = t + q * P;
             float2 b[R2];
+            if constexpr (TWPOW) {
+                float2 w[R2];
+                twiddle_powers<R2>(tw_load<TWS>(tw, TT::OFF_REM + j), w);
 #pragma unroll
-            for (int m = 0; m < R2; ++m)
-                b[m] = m ? cmul(a[q * R2 + m], tw_load<TWS>(tw, TT::OFF_REM + (m - 1) * (N / R2) + j)) : a[q * R2];
+                for (int m = 0; m < R2; ++m) b[m] = m ? cmul(a[q * R2 + m], w[m]) : a[q * R2];
+            } else {
+#pragma unroll
+                for (int m = 0; m < R2; ++m)
+                    b[m] = m ? cmul(a[q * R2 + m], tw_load<TWS>(tw, TT::OFF_REM + (m - 1) * (N / R2) + j)) : a[q * R2];
+            }
             dft<R2>(b);
 #pragma unroll
             for (int m = 0; m < R2; ++m) gstore(j + m * (N / R2), b[m]);
@@ -515,14 +542,51 @@ template <int N>
 constexpr unsigned c2r_wz_bytes() {
     return (unsigned)((N / 2) * sizeof(float2));
 }
+// Twiddles formed in registers instead of staged tables (radix 8 or 16 rows): the pass twiddles
+// as powers of one table entry per pass (fft_transform's TWPOW), and the z twiddles
+// 1 + i exp(+2*pi*i*k/N) for k = t + m*P as 1 + i e_t c_m with e_t = exp(+2*pi*i*t/N) loaded once
+// per thread and c_m = exp(+2*pi*i*m/(2R)) compile-time constants (P/N = 1/(2R)).  The block
+// then stages only its rows.
+#ifndef C2R_COMPUTED_TW
+#define C2R_COMPUTED_TW 1
+#endif
+template <int N>
+constexpr bool c2r_computed_tw() {
+    return C2R_COMPUTED_TW && C2RShape<N>::R <= 16;
+}
+template <int N>
+constexpr unsigned c2r_staged_tw_bytes() {
+    return c2r_computed_tw<N>() ? 0u : c2r_tw_bytes<N>();
+}
+template <int N>
+constexpr unsigned c2r_staged_wz_bytes() {
+    return c2r_computed_tw<N>() ? 0u : c2r_wz_bytes<N>();
+}
+// exp(+2*pi*i*t/N) for t < P, the per-thread root of the z twiddles (compile-time, as the tables)
+template <int N>
+struct alignas(16) C2RRootData {
+    TwEntry v[C2RShape<N>::P];
+};
+template <int N>
+constexpr C2RRootData<N> make_c2r_root() {
+    C2RRootData<N> d{};
+    for (int t = 0; t < C2RShape<N>::P; ++t) d.v[t] = twiddle_exact(t, N);
+    return d;
+}
+template <int N>
+__device__ const C2RRootData<N> g_c2r_root = make_c2r_root<N>();
+
 template <int N>
 constexpr size_t c2r_smem_bytes() {
-    return sizeof(float2) * (size_t)C2RShape<N>::ROWS * C2RShape<N>::BUF + c2r_row_bytes<N>() + c2r_tw_bytes<N>() +
-           c2r_wz_bytes<N>() + sizeof(uint64_t) + sizeof(float);
+    return sizeof(float2) * (size_t)C2RShape<N>::ROWS * C2RShape<N>::BUF + c2r_row_bytes<N>() +
+           c2r_staged_tw_bytes<N>() + c2r_staged_wz_bytes<N>() + sizeof(uint64_t) + sizeof(float);
 }
 
 template <int N, bool REAL>
-__global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
+#ifndef C2R_MIN_BLOCKS
+#define C2R_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P, C2R_MIN_BLOCKS) c2r_rows_kernel(float2 *grids, float2 *images,
                                                                                     const unsigned int *wsum,
                                                                                     unsigned copy_bytes) {
     using S = C2RShape<N>;
@@ -531,7 +595,8 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     static_assert(ROW_BYTES <= S::BUF * sizeof(float2), "staged row larger than its buffer");
     static_assert(ROW_BYTES <= W * sizeof(float2) && (W * sizeof(float2)) % 16 == 0, "rows copied whole");
     static_assert((S::BUF * sizeof(float2)) % 16 == 0, "row buffers 16-byte aligned");
-    constexpr unsigned TW_BYTES = c2r_tw_bytes<N>(), WZ_BYTES = c2r_wz_bytes<N>();
+    constexpr bool CMP = c2r_computed_tw<N>();
+    constexpr unsigned TW_BYTES = c2r_staged_tw_bytes<N>(), WZ_BYTES = c2r_staged_wz_bytes<N>();
     static_assert(TW_BYTES % 16 == 0 && WZ_BYTES % 16 == 0, "twiddle tables copied whole");
     extern __shared__ __align__(16) float2 smem[];
     float2 *zeros = smem + S::ROWS * S::BUF;
@@ -559,8 +624,10 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     __syncthreads();
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(bar, S::ROWS * copy_bytes + TW_BYTES + WZ_BYTES);
-        bulk_load(tw, twiddles<M, S::R>(), TW_BYTES, bar);
-        bulk_load(wz, g_z_twiddles<N>.v, WZ_BYTES, bar);
+        if constexpr (!CMP) {
+            bulk_load(tw, twiddles<M, S::R>(), TW_BYTES, bar);
+            bulk_load(wz, g_z_twiddles<N>.v, WZ_BYTES, bar);
+        }
         for (int r = 0; r < S::ROWS; ++r) bulk_load(smem + r * S::BUF, grids + (row0 + r) * W, copy_bytes, bar);
         // one FP64 reciprocal per block (all its rows are one image's), while the copies fly
         *s_scale = (float)(1.0 / (double)wsum[(row0 / N) * kWsumStride]);
@@ -575,10 +642,22 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_ke
     }
     const float scale = *s_scale;
     float2 *dst = images + row * N;
-    fft_transform<M, S::R, S::WARP, false, true>(
-        t, buf, tw,
+    float2 e_t = make_float2(1.f, 0.f);
+    if constexpr (CMP) e_t = __ldg(reinterpret_cast<const float2 *>(g_c2r_root<N>.v) + t);
+    fft_transform<M, S::R, S::WARP, false, !CMP, CMP>(
+        t, buf, CMP ? twiddles<M, S::R>() : tw,
         [&](int k) {
-            const float2 a = buf[k], b = buf[M - k], P = wz[k];
+            const float2 a = buf[k], b = buf[M - k];
+            float2 P;
+            if constexpr (CMP) {
+                // k = t + m*P with m fixed in the unrolled loading loop: exp(+2*pi*i*k/N) = e_t c_m
+                const int m = (k - t) / S::P;
+                constexpr int STEP = 32 / (2 * S::R);  // c_m = exp(+2*pi*i*(m*STEP)/32)
+                const float2 e = cmul(e_t, make_float2(cos32(m * STEP), sin32(m * STEP)));
+                P = make_float2(1.f - e.y, e.x);
+            } else {
+                P = wz[k];
+            }
             // 2 conj(b) + P (a - conj(b))
             const float dx = a.x - b.x, dy = a.y + b.y;
             return make_float2(fmaf(P.x, dx, fmaf(-P.y, dy, 2.f * b.x)), fmaf(P.x, dy, fmaf(P.y, dx, -2.f * b.y)));
