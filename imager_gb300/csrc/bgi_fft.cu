@@ -484,6 +484,10 @@ constexpr int half_width_of() {
 // launch covers the first `tiles` tiles of each image (the columns beyond are zero, and so are
 // their transforms), and rows ext_v < y < N - ext_v, which hold no gridded value, read as zero
 // without a load.
+// COLS_TWPOW: the pass twiddles as powers of one table entry per pass (fft_transform's TWPOW)
+#ifndef COLS_TWPOW
+#define COLS_TWPOW 0
+#endif
 template <int N>
 __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_half_kernel(float2 *grids, int tiles,
                                                                                         int ext_v) {
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ha
     const int x0 = (blockIdx.x % tiles) * COLS;
     const int c = threadIdx.x % COLS, t = threadIdx.x / COLS;
     float2 *g = grids + img * (size_t)N * W + x0 + c;
-    fft_transform<N, S::R, false, false>(
+    fft_transform<N, S::R, false, false, false, COLS_TWPOW != 0>(
         t, smem + c * S::STRIDE, tw,
         [&](int i) { return (i <= ext_v || i >= N - ext_v) ? g[(size_t)i * W] : make_float2(0.f, 0.f); },
         [&](int i, float2 v) { g[(size_t)((i + N / 2) & (N - 1)) * W] = v; });
@@ -504,6 +508,9 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ha
 // Complex-to-real row pass shape: transforms of length M = N/2.
 #ifndef C2R_THREADS
 #define C2R_THREADS 128
+#endif
+#ifndef C2R_MIN_BLOCKS_512
+#define C2R_MIN_BLOCKS_512 9
 #endif
 template <int N>
 struct C2RShape {
@@ -516,6 +523,9 @@ struct C2RShape {
     static constexpr int ROWS = WARP ? ((THREADS / P) < N ? (THREADS / P) : N) : (THREADS / P > 0 ? THREADS / P : 1);
     static constexpr int LEN = FftCfg<M, R>::LEN;
     static constexpr int BUF = ((LEN > M + 1 ? LEN : M + 1) + 1) & ~1;
+    // resident blocks per SM the registers must allow: at 512^2 nine 128-thread blocks (the
+    // shared-memory limit) measured faster than the eight that 60 registers leave
+    static constexpr int MIN_BLOCKS = N == 512 ? C2R_MIN_BLOCKS_512 : 1;
 };
 
 // Complex-to-real pass: half-plane row y (already at its fftshifted position) -> image row y.
@@ -583,12 +593,8 @@ constexpr size_t c2r_smem_bytes() {
 }
 
 template <int N, bool REAL>
-#ifndef C2R_MIN_BLOCKS
-#define C2R_MIN_BLOCKS 1
-#endif
-__global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P, C2R_MIN_BLOCKS) c2r_rows_kernel(float2 *grids, float2 *images,
-                                                                                    const unsigned int *wsum,
-                                                                                    unsigned copy_bytes) {
+__device__ __forceinline__ void c2r_rows_body(float2 *grids, float2 *images, const unsigned int *wsum,
+                                              unsigned copy_bytes) {
     using S = C2RShape<N>;
     constexpr int M = S::M, W = half_width_of<N>();
     constexpr unsigned ROW_BYTES = c2r_row_bytes<N>();
@@ -672,6 +678,21 @@ __global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P, C2R_MIN_BLO
                 __stcs(reinterpret_cast<float4 *>(dst + x), make_float4(z.x * scale, 0.f, z.y * scale, 0.f));
         });
     if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// The kernel, with the compiler's own register budget, and at 512^2 with the budget that keeps
+// nine blocks resident per SM (C2RShape::MIN_BLOCKS); a second launch-bounds argument of 1
+// would change the other sides' register allocation (80 -> 96 at 1024^2), so they keep none.
+template <int N, bool REAL>
+__global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P) c2r_rows_kernel(float2 *grids, float2 *images,
+                                                                                    const unsigned int *wsum,
+                                                                                    unsigned copy_bytes) {
+    c2r_rows_body<N, REAL>(grids, images, wsum, copy_bytes);
+}
+template <int N, bool REAL>
+__global__ void __launch_bounds__(C2RShape<N>::ROWS *C2RShape<N>::P, C2RShape<N>::MIN_BLOCKS)
+    c2r_rows_kernel_occ(float2 *grids, float2 *images, const unsigned int *wsum, unsigned copy_bytes) {
+    c2r_rows_body<N, REAL>(grids, images, wsum, copy_bytes);
 }
 
 // ---- complex-to-real rows on the tensor cores (N = 512) ------------------------------------
@@ -980,6 +1001,7 @@ int c2r_n(float2 *grids, float2 *images, int n_images, const unsigned int *wsum,
         }
     }
     auto k = real ? c2r_rows_kernel<N, true> : c2r_rows_kernel<N, false>;
+    if constexpr (S::MIN_BLOCKS > 1) k = real ? c2r_rows_kernel_occ<N, true> : c2r_rows_kernel_occ<N, false>;
     int st = prepare(k, smem);
     if (st) return st;
     k<<<blocks, S::ROWS * S::P, smem, s>>>(grids, images, wsum, copy_bytes);
