@@ -484,10 +484,6 @@ constexpr int half_width_of() {
 // launch covers the first `tiles` tiles of each image (the columns beyond are zero, and so are
 // their transforms), and rows ext_v < y < N - ext_v, which hold no gridded value, read as zero
 // without a load.
-// COLS_TWPOW: the pass twiddles as powers of one table entry per pass (fft_transform's TWPOW)
-#ifndef COLS_TWPOW
-#define COLS_TWPOW 0
-#endif
 template <int N>
 __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_half_kernel(float2 *grids, int tiles,
                                                                                         int ext_v) {
@@ -499,7 +495,7 @@ __global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_ha
     const int x0 = (blockIdx.x % tiles) * COLS;
     const int c = threadIdx.x % COLS, t = threadIdx.x / COLS;
     float2 *g = grids + img * (size_t)N * W + x0 + c;
-    fft_transform<N, S::R, false, false, false, COLS_TWPOW != 0>(
+    fft_transform<N, S::R, false, false>(
         t, smem + c * S::STRIDE, tw,
         [&](int i) { return (i <= ext_v || i >= N - ext_v) ? g[(size_t)i * W] : make_float2(0.f, 0.f); },
         [&](int i, float2 v) { g[(size_t)((i + N / 2) & (N - 1)) * W] = v; });
