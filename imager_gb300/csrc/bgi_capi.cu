@@ -1037,24 +1037,32 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     int st = check_cuda(cudaEventCreate(&e1), "autotune event");
     // milliseconds per call of the handle's current schedule: one call to size the scratch, then
     // three timed with CUDA events on the stream
-    auto time_current = [&](float *ms) {
+    auto time_current = [&](float *ms, int reps = 3) {
         int r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
         if (!r) r = check_cuda(cudaEventRecord(e0, s), "autotune record");
-        for (int rep = 0; !r && rep < 3; ++rep) r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+        for (int rep = 0; !r && rep < reps; ++rep)
+            r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
         if (!r) r = check_cuda(cudaEventRecord(e1, s), "autotune record");
         if (!r) r = check_cuda(cudaEventSynchronize(e1), "autotune sync");
         float t = 0.f;
         if (!r) r = check_cuda(cudaEventElapsedTime(&t, e0, e1), "autotune elapsed");
-        *ms = t / 3.f;
+        *ms = t / (float)reps;
         return r;
     };
     static const int kWaves[] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64};
     int best_wave = im->cfg.max_images_per_wave, best_lanes = im->lanes;
     int best_cpt = im->grid_cpt, best_fft = im->fft_mode;
     float best = 3.4e38f;
-    // 1. images per wave x lanes, with the gridding and FFT defaults
+    // 1. images per wave x lanes, with the gridding and FFT defaults: every candidate timed over
+    // three calls, then the three fastest again over ten calls each (a three-call time of a
+    // ~0.5 ms block varies by a few percent, enough to mis-rank neighbouring candidates)
     im->grid_cpt = 0;
     im->fft_mode = BGI_FFT_SIMT;
+    struct Cand {
+        float ms;
+        int wave, lanes;
+    };
+    std::vector<Cand> cands;
     for (int wi = 0; !st && wi < (int)(sizeof(kWaves) / sizeof(kWaves[0])); ++wi) {
         if (kWaves[wi] > n_images) break;
         for (int lanes = 1; !st && lanes <= bgi_imager::kLanes; ++lanes) {
@@ -1062,13 +1070,21 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
             im->lanes = lanes;
             float ms = 0.f;
             st = time_current(&ms);
-            if (!st && ms < best) {
-                best = ms;
-                best_wave = kWaves[wi];
-                best_lanes = lanes;
-                best_cpt = 0;
-                best_fft = BGI_FFT_SIMT;
-            }
+            if (!st) cands.push_back({ms, kWaves[wi], lanes});
+        }
+    }
+    std::sort(cands.begin(), cands.end(), [](const Cand &a, const Cand &b) { return a.ms < b.ms; });
+    for (size_t c = 0; !st && c < std::min<size_t>(3, cands.size()); ++c) {
+        im->cfg.max_images_per_wave = cands[c].wave;
+        im->lanes = cands[c].lanes;
+        float ms = 0.f;
+        st = time_current(&ms, 10);
+        if (!st && ms < best) {
+            best = ms;
+            best_wave = cands[c].wave;
+            best_lanes = cands[c].lanes;
+            best_cpt = 0;
+            best_fft = BGI_FFT_SIMT;
         }
     }
     // 2. at the best wave and lanes: gridding images per thread, then the last FFT pass's arithmetic
@@ -1078,7 +1094,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
         if (st) break;
         im->grid_cpt = cpt;
         float ms = 0.f;
-        st = time_current(&ms);
+        st = time_current(&ms, 10);
         if (!st && ms < best) {
             best = ms;
             best_cpt = cpt;
@@ -1088,7 +1104,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     if (!st && c2r_tensor_supported(im->cfg.n_pixels) && im->half_plane_path()) {
         im->fft_mode = BGI_FFT_TENSOR_SPLIT16;
         float ms = 0.f;
-        st = time_current(&ms);
+        st = time_current(&ms, 10);
         if (!st && ms < best) {
             best = ms;
             best_fft = BGI_FFT_TENSOR_SPLIT16;
