@@ -613,6 +613,8 @@ def run_ours(args, rank, world, local_rank):
             tuned = im.autotune(stored[fmt][0], stored[fmt][1], fmt, flags=flags, out=out)
     if args.fft_mode:
         im.set_fft_mode(args.fft_mode)
+    if args.gridding_images_per_thread:
+        im.set_gridding_images_per_thread(args.gridding_images_per_thread)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -953,6 +955,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--storage", choices=["s16", "bf16", "fp16", "c64"], default="s16",
                     help="visibility storage of the timed step (s16: 16-bit block floating point)")
+    ap.add_argument("--gridding-images-per-thread", type=int, choices=[2, 4, 8], default=None,
+                    help="force the gridding's images per thread of the timed step (default: the autotuner's)")
     ap.add_argument("--fft-mode", choices=["simt", "tensor_split16"], default=None,
                     help="force the FFT arithmetic of the timed step (default: the autotuner's choice)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

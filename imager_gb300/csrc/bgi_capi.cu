@@ -1090,7 +1090,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     // 2. at the best wave and lanes: gridding images per thread, then the last FFT pass's arithmetic
     im->cfg.max_images_per_wave = best_wave;
     im->lanes = best_lanes;
-    for (int cpt : {2, 4}) {
+    for (int cpt : {2, 4, 8}) {
         if (st) break;
         im->grid_cpt = cpt;
         float ms = 0.f;
@@ -1131,8 +1131,8 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
 }
 
 int bgi_set_gridding_images_per_thread(bgi_imager *im, int images_per_thread) {
-    if (!im || (images_per_thread != 0 && images_per_thread != 2 && images_per_thread != 4))
-        return set_error(BGI_ERR_INVALID, "set_gridding_images_per_thread: 0 (auto), 2 or 4");
+    if (!im || (images_per_thread != 0 && images_per_thread != 2 && images_per_thread != 4 && images_per_thread != 8))
+        return set_error(BGI_ERR_INVALID, "set_gridding_images_per_thread: 0 (auto), 2, 4 or 8");
     im->grid_cpt = images_per_thread;
     return BGI_OK;
 }

@@ -325,9 +325,130 @@ bool lean_applies(const GridParams &q, int cpt) {
     return one && nb < (1LL << 27) && (long long)cpt * 4 * nb < (1LL << 31) && cpt * per_image_grid < (1LL << 31);
 }
 
+// ---- the half-plane gridding with several images per thread, raw loads first ----------------
+// grid_half_lean_kernel holds its images' decoded values and channel constants in registers, which
+// limits it to a few images per thread.  This form keeps only the raw stored words of its IMG
+// images (one or two 4-byte words and block scales per image for the 16-bit formats), issues every
+// one of those loads before the first use, and per image decodes, reads the channel constants
+// (cached) and grids: the per-baseline work -- flags, cable delay, u/v/w and the delay phase --
+// is done once for all IMG images, and all of a thread's global loads are in flight together.
+// The images of a block may span two intervals with their own UVW sets (the block's images are
+// consecutive); u/v/w and the delay are then reloaded where the set changes.
+template <int POL, int FMT, int IMG>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) grid_half_loop_kernel(const GridParams p) {
+    __shared__ unsigned int s_count[IMG][kThreads / 32];
+    constexpr int P0 = POL == BGI_POL_XX ? 0 : POL == BGI_POL_YY ? 3 : POL == BGI_POL_I ? 0 : 1;  // planes
+    constexpr int P1 = POL == BGI_POL_I ? 3 : 2;
+    constexpr bool TWO = POL == BGI_POL_I || POL == BGI_POL_V;
+    constexpr bool C64 = FMT == BGI_VIS_C64;
+    const int img_first = p.img_begin + blockIdx.y * IMG;
+    const int n_here = min(IMG, p.img_begin + p.img_count - img_first);
+    const int nb = (int)p.n_baselines;
+    const int b = blockIdx.x * kThreads + threadIdx.x;
+    const bool in_range = b < nb;
+    const int n = p.n_pixels, w = p.half_width;
+    const int nblk = (int)p.vis_blocks;
+    // ---- every global load of the thread's images first ----------------------------------------
+    int flag = 1;
+    float2 dl = make_float2(0.f, 0.f);
+    float2 ra[IMG], rb[IMG];  // complex64: the pol values; 16-bit: (word bits, scale) pairs
+    if (in_range) {
+        flag = p.flags[b];
+        if (p.apply_cable) dl = p.dl[b];
+    }
+#pragma unroll
+    for (int j = 0; j < IMG; ++j) {
+        ra[j] = rb[j] = make_float2(0.f, 0.f);
+        if (in_range && j < n_here) {
+            const size_t img = (size_t)img_first + j;
+            if (C64) {
+                load_pols<POL>(reinterpret_cast<const float2 *>(p.vis) + (img * nb + b) * 4, ra[j], rb[j]);
+            } else {
+                const uint32_t *d = reinterpret_cast<const uint32_t *>(p.vis) + img * 4 * nb + b;
+                const float *sc = p.vis_scales + img * 4 * nblk + (b >> 7);
+                ra[j] = make_float2(__uint_as_float(__ldcs(d + P0 * nb)), __ldg(sc + P0 * nblk));
+                if (TWO) rb[j] = make_float2(__uint_as_float(__ldcs(d + P1 * nb)), __ldg(sc + P1 * nblk));
+            }
+        }
+    }
+    const bool corr = p.apply_geom || p.apply_cable;
+    float u = 0.f, v = 0.f, wv = 0.f, d_hi = 0.f, d_lo = 0.f;
+    int cur_set = -1;
+    int ch = img_first % p.n_channels;
+    float2 *gbase = p.grids + (size_t)(img_first - p.img_base) * n * w;
+#pragma unroll
+    for (int j = 0; j < IMG; ++j) {
+        if (j >= n_here) break;  // uniform across the block
+        const int set = p.n_uvw_sets > 1 ? (img_first + j) / p.n_channels : 0;
+        if (set != cur_set) {  // uniform across the block
+            cur_set = set;
+            if (in_range) {
+                const size_t off = (size_t)set * nb + b;
+                u = p.u[off];
+                v = p.v[off];
+                if (p.apply_geom) wv = p.w[off];
+            }
+            if (corr) delay_df(wv, dl.x, dl.y, d_hi, d_lo);
+        }
+        const float4 hot = __ldg(reinterpret_cast<const float4 *>(p.chan_consts + ch));
+        unsigned int counted = 0;
+        if (in_range && flag <= 0) {
+            float2 a = ra[j], bb = rb[j];
+            if (!C64) {
+                a = decode_vis<FMT>(__float_as_uint(ra[j].x), ra[j].y);
+                if (TWO) bb = decode_vis<FMT>(__float_as_uint(rb[j].x), rb[j].y);
+            }
+            float2 z = combine_pols<POL>(a, bb);
+            if (corr) z = rotate(z, phasor_df(d_hi, d_lo, hot.z, hot.w));
+            int ui, vi;
+            const bool cu = round_certain_lean(u * hot.x, &ui), cv = round_certain_lean(v * hot.y, &vi);
+            bool ok = !isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis;
+            if (ok && !(cu && cv)) {  // within the FP32 bound of a half-integer: the exact recipe
+                double up, vp;
+                const ChannelConst *ccp = p.chan_consts + ch;
+                ok = uv_pixels_exact(u, v, ccp->wavelength, p.du, p.dv, p.min_uv, &up, &vp) &&
+                     fabs(up) < 1073741824.0 && fabs(vp) < 1073741824.0;
+                ui = (int)up;
+                vi = (int)vp;
+            }
+            if (ok) {
+                const int u1 = ui + (n & (ui >> 31)), v1 = vi + (n & (vi >> 31));
+                const int u2 = -ui + (n & (-ui >> 31)), v2 = -vi + (n & (-vi >> 31));
+                float2 *g = gbase + (unsigned)(j * n * w);
+                if (u1 <= n / 2) atomicAdd(g + (unsigned)(v1 * w + u1), z);
+                if (u2 <= n / 2) atomicAdd(g + (unsigned)(v2 * w + u2), make_float2(z.x, -z.y));
+                counted = 2;
+            }
+        }
+        const unsigned int warp_total = __reduce_add_sync(0xffffffffu, counted);
+        if ((threadIdx.x & 31) == 0) s_count[j][threadIdx.x >> 5] = warp_total;
+        if (++ch == p.n_channels) ch = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < n_here) {
+        unsigned int total = 0;
+#pragma unroll
+        for (int k = 0; k < kThreads / 32; ++k) total += s_count[threadIdx.x][k];
+        if (total) atomicAdd(p.wsum + (size_t)(img_first + threadIdx.x - p.img_base) * kWsumStride, total);
+    }
+}
+
+// whether the looping kernel applies (the lean kernel's preconditions; the block's images may
+// span UVW sets)
+bool loop_applies(const GridParams &q, int img) {
+    if (q.half_width <= 0 || !q.chan_consts || q.min_uv >= 0.0 || q.counter_mode >= 0 || !q.wsum || q.kb_size > 0)
+        return false;
+    const long long per_image_grid = (long long)q.n_pixels * q.half_width;
+    return q.n_baselines < (1LL << 27) && img * per_image_grid < (1LL << 31);
+}
+
 template <int POL, int FMT, int CPT>
 void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
     const bool one = one_set(q, CPT);
+    if (CPT >= 4 && loop_applies(q, CPT)) {
+        grid_half_loop_kernel<POL, FMT, CPT><<<grid, kThreads, 0, s>>>(q);
+        return;
+    }
     if (lean_applies(q, CPT)) {
         grid_half_lean_kernel<POL, FMT, CPT><<<grid, kThreads, 0, s>>>(q);
         return;
@@ -357,6 +478,25 @@ void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
         case BGI_VIS_BF16: launch_fmt<POL, BGI_VIS_BF16, CPT>(grid, q, s); break;
         case BGI_VIS_FP16: launch_fmt<POL, BGI_VIS_FP16, CPT>(grid, q, s); break;
         default: launch_fmt<POL, BGI_VIS_C64, CPT>(grid, q, s);
+    }
+}
+
+template <int POL>
+void launch_loop8_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
+    switch (q.vis_format) {
+        case BGI_VIS_S16: grid_half_loop_kernel<POL, BGI_VIS_S16, 8><<<grid, kThreads, 0, s>>>(q); break;
+        case BGI_VIS_BF16: grid_half_loop_kernel<POL, BGI_VIS_BF16, 8><<<grid, kThreads, 0, s>>>(q); break;
+        case BGI_VIS_FP16: grid_half_loop_kernel<POL, BGI_VIS_FP16, 8><<<grid, kThreads, 0, s>>>(q); break;
+        default: grid_half_loop_kernel<POL, BGI_VIS_C64, 8><<<grid, kThreads, 0, s>>>(q);
+    }
+}
+
+void launch_loop8(const dim3 &grid, const GridParams &q, cudaStream_t s) {
+    switch (q.pol) {
+        case BGI_POL_XX: launch_loop8_pol<BGI_POL_XX>(grid, q, s); break;
+        case BGI_POL_YY: launch_loop8_pol<BGI_POL_YY>(grid, q, s); break;
+        case BGI_POL_I: launch_loop8_pol<BGI_POL_I>(grid, q, s); break;
+        default: launch_loop8_pol<BGI_POL_V>(grid, q, s); break;
     }
 }
 
@@ -409,13 +549,15 @@ int launch_gridding(const GridParams &p, cudaStream_t s) {
     }
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;
     const int max_groups = 65535;
-    const int cpt = p.cpt == 2 || p.cpt == 4 ? p.cpt : images_per_thread(p.n_baselines);
+    int cpt = p.cpt == 2 || p.cpt == 4 || p.cpt == 8 ? p.cpt : images_per_thread(p.n_baselines);
+    if (cpt == 8 && !loop_applies(p, 8)) cpt = 4;  // eight images per thread: the looping kernel only
     for (int done = 0; done < p.img_count; done += max_groups * cpt) {
         GridParams q = p;
         q.img_begin = p.img_begin + done;
         q.img_count = std::min(p.img_count - done, max_groups * cpt);
         const dim3 grid((unsigned)bx, (unsigned)((q.img_count + cpt - 1) / cpt));
-        if (cpt == 4) launch_cpt<4>(grid, q, s);
+        if (cpt == 8) launch_loop8(grid, q, s);
+        else if (cpt == 4) launch_cpt<4>(grid, q, s);
         else launch_cpt<2>(grid, q, s);
         int st = check_launch("gridding");
         if (st) return st;

@@ -361,7 +361,7 @@ class Imager:
         call("bgi_set_gridding_kernel", self._h, int(kernel_size), int(bool(with_sinc)))
 
     def set_gridding_images_per_thread(self, k: int = 0):
-        """Images per gridding thread: 2 or 4 (0: by array size)."""
+        """Images per gridding thread: 2, 4 or 8 (0: by array size)."""
         call("bgi_set_gridding_images_per_thread", self._h, int(k))
 
     @property

@@ -391,12 +391,13 @@ BGI_API int bgi_get_fft_mode(const bgi_imager *im, int *mode);
 
 /* Launch schedule of the bgi_image* calls: images per wave (0 = auto: about 26 MiB of grid
  * per lane, 24 half-plane images at 512^2), lanes (1..8 streams that image alternate waves,
- * each with its own grid scratch; 2 by default), images per gridding thread (2 or 4, 0 = by
- * array size: 2 below 65,536 baselines, 4 above) and the FFT arithmetic (bgi_set_fft_mode).
+ * each with its own grid scratch; 2 by default), images per gridding thread (2, 4 or 8, 0 = by
+ * array size: 2 below 65,536 baselines, 4 above; 4 and 8 issue all of a thread's visibility
+ * loads before gridding any) and the FFT arithmetic (bgi_set_fft_mode).
  * bgi_autotune times every wave size in {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to
  * the block's image count) with 1-8 lanes on the caller's own block (one call to size the
  * scratch, three timed with CUDA events on the stream), times the three fastest again over ten
- * calls each, then, at the best of those, 2 and 4 images per gridding thread and (image side
+ * calls each, then, at the best of those, 2, 4 and 8 images per gridding thread and (image side
  * 512, half plane) the tensor-core row pass (ten timed calls each);
  * it keeps the fastest on the handle, frees the candidates' scratch and writes the best
  * milliseconds per call to *best_ms (may be NULL).  Synchronous; `images` receives the block's

@@ -523,7 +523,7 @@ def test_schedule_and_autotune(im):
     with pytest.raises(capi.BgiError):
         h.set_schedule(8, 9)
     h.set_deterministic(False)
-    for cpt in (2, 4, 0):  # images per gridding thread (0: by array size)
+    for cpt in (2, 4, 8, 0):  # images per gridding thread (0: by array size)
         h.set_gridding_images_per_thread(cpt)
         assert h.gridding_images_per_thread == cpt
         assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6, cpt
@@ -531,7 +531,7 @@ def test_schedule_and_autotune(im):
         h.set_gridding_images_per_thread(3)
     wave, lanes, ms = h.autotune(vis)
     assert wave in (0, 4, 8, 12) and 1 <= lanes <= 8 and ms > 0
-    assert h.gridding_images_per_thread in (0, 2, 4) and h.fft_mode == "simt"  # no tensor pass at 128
+    assert h.gridding_images_per_thread in (0, 2, 4, 8) and h.fft_mode == "simt"  # no tensor pass at 128
     assert rel_l2(h.image(vis).cpu().numpy(), ref) < 1e-6
     h.close()
 
@@ -607,4 +607,28 @@ def test_image_buffers_off_16_byte_boundaries(im):
     with pytest.raises(capi.BgiError) as e:
         h.image(vis, flags=im.APPLY_GEOMETRIC | im.APPLY_CABLE | im.OUTPUT_REAL, out=real4)
     assert e.value.status == capi.ERR_INVALID
+    h.close()
+
+
+@pytest.mark.parametrize("pol", ["XX", "YY", "I", "V"])
+@pytest.mark.parametrize("cpt", [4, 8])
+def test_gridding_images_per_thread_against_oracle(im, pol, cpt):
+    """Four and eight images per gridding thread (all of a thread's visibility loads issued
+    first): every pol, complex64 and s16 storage, per-interval UVW sets, so a block's images
+    cross an interval boundary (3 channels per interval) and reload u/v/w mid-block."""
+    n = 128
+    obs = synth.small(seed=70 + cpt, n_ant=40, n_intervals=4, n_channels=3, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, counters, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n,
+                                             pol=pol, n_uvw_sets=4)
+    h = _imager_for(im, obs, n, pol)
+    h.set_gridding_images_per_thread(cpt)
+    out = h.image(dev(vis)).cpu().numpy()
+    data, scales = im.compress_visibilities(dev(vis), "s16")
+    s16 = h.image_compressed(data, scales, "s16").cpu().numpy()
+    for i in range(4):
+        for j in range(3):
+            assert rel_l2(out[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+            assert rel_l2(s16[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+    assert np.array_equal(h.weight_sums(12), counters.reshape(12, -1).sum(1).astype(np.uint32))
     h.close()

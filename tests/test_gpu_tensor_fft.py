@@ -109,7 +109,7 @@ def test_autotune_chooses_among_fft_modes(im):
     _, _, _, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, 512, n_uvw_sets=2)
     h, _ = _pair(im, obs)
     wave, lanes, ms = h.autotune(dev(vis))
-    assert ms > 0 and h.fft_mode in ("simt", "tensor_split16") and h.gridding_images_per_thread in (0, 2, 4)
+    assert ms > 0 and h.fft_mode in ("simt", "tensor_split16") and h.gridding_images_per_thread in (0, 2, 4, 8)
     out = h.image(dev(vis)).cpu().numpy()
     for i in range(2):
         for j in range(4):
