@@ -549,7 +549,12 @@ int launch_gridding(const GridParams &p, cudaStream_t s) {
     }
     const long long bx = (p.n_baselines + kThreads - 1) / kThreads;
     const int max_groups = 65535;
-    int cpt = p.cpt == 2 || p.cpt == 4 || p.cpt == 8 ? p.cpt : images_per_thread(p.n_baselines);
+    // by default 4 on the half-plane path (the looping kernel: 0.518-0.521 against 0.530 ms per
+    // step with 2 at 256 antennas, and the uneven 512-antenna batch 7.41 against 7.87 ms), else by
+    // array size
+    int cpt = p.cpt == 2 || p.cpt == 4 || p.cpt == 8 ? p.cpt
+              : loop_applies(p, 4)                  ? 4
+                                                    : images_per_thread(p.n_baselines);
     if (cpt == 8 && !loop_applies(p, 8)) cpt = 4;  // eight images per thread: the looping kernel only
     for (int done = 0; done < p.img_count; done += max_groups * cpt) {
         GridParams q = p;

@@ -391,9 +391,10 @@ BGI_API int bgi_get_fft_mode(const bgi_imager *im, int *mode);
 
 /* Launch schedule of the bgi_image* calls: images per wave (0 = auto: about 26 MiB of grid
  * per lane, 24 half-plane images at 512^2), lanes (1..8 streams that image alternate waves,
- * each with its own grid scratch; 2 by default), images per gridding thread (2, 4 or 8, 0 = by
- * array size: 2 below 65,536 baselines, 4 above; 4 and 8 issue all of a thread's visibility
- * loads before gridding any) and the FFT arithmetic (bgi_set_fft_mode).
+ * each with its own grid scratch; 2 by default), images per gridding thread (2, 4 or 8; 0 =
+ * default: 4 on the half-plane path, else 2 below 65,536 baselines and 4 above; on the half
+ * plane 4 and 8 issue all of a thread's visibility loads before gridding any) and the FFT
+ * arithmetic (bgi_set_fft_mode).
  * bgi_autotune times every wave size in {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to
  * the block's image count) with 1-8 lanes on the caller's own block (one call to size the
  * scratch, three timed with CUDA events on the stream), times the three fastest again over ten
