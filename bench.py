@@ -861,6 +861,14 @@ def run_ours(args, rank, world, local_rank):
             stage_info[k] = {"ms_per_launch": per_launch_ms, "launches": launches,
                              "images_per_launch": imgs_per_launch, "achieved_gbs": gbs,
                              "share": tot_ms / max(sum(v[0] for v in stages.values()), 1e-12)}
+    if "gridding" in stage_info:
+        # the fixed per-image count for gridding (stored visibilities read, the whole N x N grid
+        # written, the counters per channel) beside the pruned one above
+        g = stage_info["gridding"]
+        fixed = vis_bytes + 8 * N * N + 4 * N * N / T
+        g["fixed_count_bytes_per_image"] = fixed
+        g["fixed_count_gbs"] = fixed * g["images_per_launch"] / (g["ms_per_launch"] / 1000.0) / 1e9
+        g["fixed_count_frac"] = g["fixed_count_gbs"] / hbm_peak
     dom = max(stage_info, key=lambda k: stage_info[k]["share"])
     traffic = None
     try:
