@@ -917,7 +917,7 @@ def run_ours(args, rank, world, local_rank):
                    "images_per_step": n_images, "n_pixels": N, "baselines": B,
                    "schedule": {"images_per_wave": im.schedule[0] or "auto", "lanes": im.schedule[1],
                                 "gridding_images_per_thread": im.gridding_images_per_thread or "auto",
-                                "fft_mode": im.fft_mode,
+                                "fft_mode": im.fft_mode, "column_radix": im.column_radix,
                                 "chosen_by": "bgi_autotune on this block" if tuned else "default"},
                    "l2": "flushed before every timed step (512 MB written outside the step's events)",
                    "storage": fmt,

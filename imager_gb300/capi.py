@@ -87,6 +87,8 @@ _SIGNATURES = {
     "bgi_uniform_weighting_gpu": (_i, [_vp, _vp, _i, _i, _vp]),
     "bgi_set_fft_mode": (_i, [_vp, _i]),
     "bgi_set_gridding_images_per_thread": (_i, [_vp, _i]),
+    "bgi_set_column_radix": (_i, [_vp, _i]),
+    "bgi_get_column_radix": (_i, [_vp, _vp]),
     "bgi_get_gridding_images_per_thread": (_i, [_vp, _vp]),
     "bgi_get_fft_mode": (_i, [_vp, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),

@@ -153,6 +153,7 @@ struct bgi_imager {
     int kb_size = 0;           // Kaiser-Bessel kernel size (0: nearest neighbour)
     int fft_mode = BGI_FFT_SIMT;  // enum bgi_fft_mode
     int grid_cpt = 0;             // gridding images per thread (0: by array size)
+    int col_radix = 0;            // column-pass radix of the half plane (0: the side's default)
     DevBuf<float> kb_table;    // its rows [1023][kb_size]
     bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
@@ -820,7 +821,7 @@ int run_waves(bgi_imager *im, GridParams p, float2 *out, int img_first, int coun
         if (p.half_width > 0) {
             int eu, ev;
             im->half_plane_extent(&eu, &ev);
-            BGI_TRY(launch_fft_cols_half(grid, n, cnt, eu, ev, ls));           // in place, rows shifted
+            BGI_TRY(launch_fft_cols_half(grid, n, cnt, eu, ev, ls, im->col_radix));  // in place, rows shifted
             BGI_TRY(im->mark(ls));
             BGI_TRY(launch_c2r_rows(grid, image_ptr(out, img0, npix, real), n, cnt, ws, eu, ls, real,
                                     im->fft_mode == BGI_FFT_TENSOR_SPLIT16));  // clears the scratch
@@ -1051,13 +1052,14 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     };
     static const int kWaves[] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64};
     int best_wave = im->cfg.max_images_per_wave, best_lanes = im->lanes;
-    int best_cpt = im->grid_cpt, best_fft = im->fft_mode;
+    int best_cpt = im->grid_cpt, best_fft = im->fft_mode, best_radix = im->col_radix;
     float best = 3.4e38f;
     // 1. images per wave x lanes, with the gridding and FFT defaults: every candidate timed over
     // three calls, then the three fastest again over ten calls each (a three-call time of a
     // ~0.5 ms block varies by a few percent, enough to mis-rank neighbouring candidates)
     im->grid_cpt = 0;
     im->fft_mode = BGI_FFT_SIMT;
+    im->col_radix = 0;
     struct Cand {
         float ms;
         int wave, lanes;
@@ -1085,6 +1087,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
             best_lanes = cands[c].lanes;
             best_cpt = 0;
             best_fft = BGI_FFT_SIMT;
+            best_radix = 0;
         }
     }
     // 2. at the best wave and lanes: gridding images per thread, then the last FFT pass's arithmetic
@@ -1101,6 +1104,18 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
         }
     }
     im->grid_cpt = best_cpt;
+    // 3. the column pass's other compiled radix (half plane)
+    const int alt = col_alt_radix(im->cfg.n_pixels);
+    if (!st && alt && im->half_plane_path()) {
+        im->col_radix = alt;
+        float ms = 0.f;
+        st = time_current(&ms, 10);
+        if (!st && ms < best) {
+            best = ms;
+            best_radix = alt;
+        }
+    }
+    im->col_radix = best_radix;
     if (!st && c2r_tensor_supported(im->cfg.n_pixels) && im->half_plane_path()) {
         im->fft_mode = BGI_FFT_TENSOR_SPLIT16;
         float ms = 0.f;
@@ -1117,6 +1132,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     im->lanes = best_lanes;
     im->grid_cpt = best_cpt;
     im->fft_mode = best_fft;
+    im->col_radix = best_radix;
     if (st) return st;
     // drop the candidates' scratch; the chosen schedule sizes its own on the next call
     BGI_TRY(check_cuda(cudaStreamSynchronize(s), "autotune sync"));
@@ -1127,6 +1143,22 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
         im->grid_dirty[l] = false;
     }
     if (best_ms) *best_ms = best;
+    return BGI_OK;
+}
+
+int bgi_set_column_radix(bgi_imager *im, int radix) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_column_radix: null handle");
+    const int n = im->cfg.n_pixels;
+    if (radix != 0 && radix != col_default_radix(n) && radix != col_alt_radix(n))
+        return set_error(BGI_ERR_UNSUPPORTED, "set_column_radix: radix %d not compiled for image side %d (%d%s%d)", radix,
+                         n, col_default_radix(n), col_alt_radix(n) ? " or " : "", col_alt_radix(n));
+    im->col_radix = radix == col_default_radix(n) ? 0 : radix;
+    return BGI_OK;
+}
+
+int bgi_get_column_radix(const bgi_imager *im, int *radix) {
+    if (!im || !radix) return set_error(BGI_ERR_INVALID, "get_column_radix: bad arguments");
+    *radix = im->col_radix ? im->col_radix : col_default_radix(im->cfg.n_pixels);
     return BGI_OK;
 }
 

@@ -368,9 +368,9 @@ struct Shape {
 #ifndef COL_THREADS
 #define COL_THREADS 256
 #endif
-template <int N>
+template <int N, int RADIX = Shape<N>::R>
 struct ColShape {
-    static constexpr int R = Shape<N>::R;
+    static constexpr int R = RADIX;
     static constexpr int P = N / R;
     static constexpr int COLS = (COL_THREADS / P) < 4 ? 4 : ((COL_THREADS / P) > N ? N : (COL_THREADS / P));
     static constexpr int MOD = COLS >= 16 ? 1 : 16 / COLS;  // column stride modulo 16 (banks)
@@ -484,11 +484,15 @@ constexpr int half_width_of() {
 // launch covers the first `tiles` tiles of each image (the columns beyond are zero, and so are
 // their transforms), and rows ext_v < y < N - ext_v, which hold no gridded value, read as zero
 // without a load.
-template <int N>
-__global__ void __launch_bounds__(ColShape<N>::COLS *ColShape<N>::P) fft_cols_half_kernel(float2 *grids, int tiles,
-                                                                                        int ext_v) {
-    using S = ColShape<N>;
+// RADIX: the column transforms' radix (Shape<N>::R by default; the other compiled radix is
+// col_alt_radix(N), picked per handle).  The grid's width W is the default shape's either way.
+template <int N, int RADIX = Shape<N>::R>
+__global__ void __launch_bounds__(ColShape<N, RADIX>::COLS *ColShape<N, RADIX>::P) fft_cols_half_kernel(float2 *grids,
+                                                                                                      int tiles,
+                                                                                                      int ext_v) {
+    using S = ColShape<N, RADIX>;
     constexpr int COLS = S::COLS, W = half_width_of<N>();
+    static_assert(W % COLS == 0, "column tiles cover the half-plane width");
     extern __shared__ float2 smem[];
     const float2 *tw = twiddles<N, S::R>();
     const size_t img = blockIdx.x / tiles;
@@ -963,16 +967,16 @@ int cols_n(float2 *src, float2 *dst, int n_images, const unsigned int *wsum, boo
     return check_launch("fft cols");
 }
 
-template <int N>
+template <int N, int RADIX = Shape<N>::R>
 int cols_half_n(float2 *grids, int n_images, int ext_u, int ext_v, cudaStream_t s) {
-    using S = ColShape<N>;
+    using S = ColShape<N, RADIX>;
     constexpr int TILES = half_width_of<N>() / S::COLS;
     const int eu = ext_u < 0 ? 0 : (ext_u > N / 2 ? N / 2 : ext_u);
     const int ev = ext_v < 0 ? 0 : (ext_v > N / 2 ? N / 2 : ext_v);
     const int tiles = std::min(TILES, eu / S::COLS + 1);  // tiles holding columns 0..eu
     const size_t smem = sizeof(float2) * ((size_t)S::COLS * S::STRIDE);
     const unsigned blocks = (unsigned)((size_t)n_images * tiles);
-    auto k = fft_cols_half_kernel<N>;
+    auto k = fft_cols_half_kernel<N, RADIX>;
     int st = prepare(k, smem);
     if (st) return st;
     k<<<blocks, S::COLS * S::P, smem, s>>>(grids, tiles, ev);
@@ -1120,8 +1124,42 @@ int half_plane_width(int n) {
     }
 }
 
-int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s) {
+int col_default_radix(int n) {
+    switch (n) {
+        case 64: return Shape<64>::R;
+        case 128: return Shape<128>::R;
+        case 256: return Shape<256>::R;
+        case 512: return Shape<512>::R;
+        case 1024: return Shape<1024>::R;
+        case 2048: return Shape<2048>::R;
+        case 4096: return Shape<4096>::R;
+        default: return 0;
+    }
+}
+
+int col_alt_radix(int n) {
+    switch (n) {
+        case 256: return 8;
+        case 512: return 16;
+        case 1024: return 16;
+        case 2048: return 32;
+        case 4096: return 32;
+        default: return 0;  // one compiled radix
+    }
+}
+
+int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s, int radix) {
     if (n_images <= 0) return BGI_OK;
+    if (radix != 0 && radix == col_alt_radix(n)) {
+        switch (n) {
+            case 256: return cols_half_n<256, 8>(grids, n_images, ext_u, ext_v, s);
+            case 512: return cols_half_n<512, 16>(grids, n_images, ext_u, ext_v, s);
+            case 1024: return cols_half_n<1024, 16>(grids, n_images, ext_u, ext_v, s);
+            case 2048: return cols_half_n<2048, 32>(grids, n_images, ext_u, ext_v, s);
+            case 4096: return cols_half_n<4096, 32>(grids, n_images, ext_u, ext_v, s);
+            default: break;
+        }
+    }
     switch (n) {
         case 64: return cols_half_n<64>(grids, n_images, ext_u, ext_v, s);
         case 128: return cols_half_n<128>(grids, n_images, ext_u, ext_v, s);

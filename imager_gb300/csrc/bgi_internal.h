@@ -122,7 +122,10 @@ int half_plane_width(int n);
 // 0..ext_u and rows 0..ext_v, N-ext_v..N-1 may hold gridded values (the caller's bound on the
 // pixel coordinates; N/2 for no bound): the columns beyond are left as they are (zero, so their
 // transforms are zero) and the rows between read as zero.
-int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s);
+// radix: the column transforms' radix, col_default_radix(n) or col_alt_radix(n) (0 = default).
+int launch_fft_cols_half(float2 *grids, int n, int n_images, int ext_u, int ext_v, cudaStream_t s, int radix = 0);
+int col_default_radix(int n);
+int col_alt_radix(int n);  // 0 when the side has one compiled radix
 // Complex-to-real row pass: half-plane rows -> image rows (fftshift of columns and
 // (float)(1/wsum) applied), clearing the grid rows it read.  Images are complex with zero
 // imaginary parts and must be 16-byte aligned.  Columns beyond ext_u are zero in the grid (the

@@ -370,6 +370,17 @@ class Imager:
         call("bgi_get_gridding_images_per_thread", self._h, C.byref(k))
         return k.value
 
+    def set_column_radix(self, radix: int = 0):
+        """Radix of the half-plane column pass (0: the side's default; sides 256..4096 have a
+        second compiled radix)."""
+        call("bgi_set_column_radix", self._h, int(radix))
+
+    @property
+    def column_radix(self) -> int:
+        r = C.c_int()
+        call("bgi_get_column_radix", self._h, C.byref(r))
+        return r.value
+
     def set_fft_mode(self, mode: str = "simt"):
         """"simt" (FP32 passes) or "tensor_split16" (the complex-to-real pass's transforms as
         split-FP16 DFT products on the tensor cores; image side 512)."""

@@ -398,12 +398,19 @@ BGI_API int bgi_get_fft_mode(const bgi_imager *im, int *mode);
  * bgi_autotune times every wave size in {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to
  * the block's image count) with 1-8 lanes on the caller's own block (one call to size the
  * scratch, three timed with CUDA events on the stream), times the three fastest again over ten
- * calls each, then, at the best of those, 2, 4 and 8 images per gridding thread and (image side
- * 512, half plane) the tensor-core row pass (ten timed calls each);
+ * calls each, then, at the best of those, 2, 4 and 8 images per gridding thread, the column
+ * pass's second radix (bgi_set_column_radix) and (image side 512, half plane) the tensor-core
+ * row pass (ten timed calls each);
  * it keeps the fastest on the handle, frees the candidates' scratch and writes the best
  * milliseconds per call to *best_ms (may be NULL).  Synchronous; `images` receives the block's
  * images.  No reference counterpart. */
 BGI_API int bgi_set_gridding_images_per_thread(bgi_imager *im, int images_per_thread);
+/* Radix of the half-plane column pass: every power-of-two side has its default radix (8 up to
+ * 128, 16 at 256, 32 at 512 and 1024, 16 above), and sides 256..4096 a second compiled one (8,
+ * 16, 16, 32, 32); 0 = the default, another value BGI_ERR_UNSUPPORTED.  bgi_autotune times the
+ * second one too.  bgi_get_column_radix reports the radix in use. */
+BGI_API int bgi_set_column_radix(bgi_imager *im, int radix);
+BGI_API int bgi_get_column_radix(const bgi_imager *im, int *radix);
 BGI_API int bgi_get_gridding_images_per_thread(const bgi_imager *im, int *images_per_thread);
 BGI_API int bgi_set_schedule(bgi_imager *im, int images_per_wave, int lanes);
 BGI_API int bgi_get_schedule(const bgi_imager *im, int *images_per_wave, int *lanes);

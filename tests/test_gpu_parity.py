@@ -632,3 +632,28 @@ def test_gridding_images_per_thread_against_oracle(im, pol, cpt):
             assert rel_l2(s16[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
     assert np.array_equal(h.weight_sums(12), counters.reshape(12, -1).sum(1).astype(np.uint32))
     h.close()
+
+
+@pytest.mark.parametrize("n", [256, 512, 1024])
+def test_column_radix_alternatives(im, n):
+    """The column pass's second compiled radix images the same block as the default one (the
+    oracle within 1e-4, the default radix within FP32 rounding); other radices are refused."""
+    obs = synth.small(seed=80 + n // 256, n_ant=40, n_intervals=1, n_channels=3, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, _, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n, n_uvw_sets=1)
+    h = _imager_for(im, obs, n, "XX")
+    default = h.column_radix
+    a = h.image(dev(vis)).cpu().numpy()
+    alt = {256: 8, 512: 16, 1024: 16}[n]
+    h.set_column_radix(alt)
+    assert h.column_radix == alt
+    b = h.image(dev(vis)).cpu().numpy()
+    for j in range(3):
+        assert rel_l2(b[0, j], ref[0, j]) < IMAGE_TOL, j
+        assert rel_l2(b[0, j], a[0, j]) < 2e-6, j
+    with pytest.raises(capi.BgiError) as e:
+        h.set_column_radix(4)
+    assert e.value.status == capi.ERR_UNSUPPORTED
+    h.set_column_radix(0)
+    assert h.column_radix == default
+    h.close()
