@@ -20,7 +20,12 @@
  *                 set 0 serves every interval when n_uvw_sets == 1 (the reference's case)
  *
  * Every function returns BGI_OK (0) or a negative status; bgi_last_error() gives the message
- * of the calling thread's last failure.  Nothing throws across this interface.  Streams are
+ * of the calling thread's last failure.  Nothing throws across this interface.
+ *
+ * Device memory the library keeps (a handle's buffers, the twiddle table of each image side
+ * that is not a power of two, the address of bgi_image_noalloc's static scratch) belongs to the
+ * device's primary context: after a cudaDeviceReset the library must not be used again in that
+ * process.  Streams are
  * cudaStream_t passed as void* (NULL = legacy default stream).  Launches are asynchronous
  * unless stated otherwise.
  */
