@@ -324,6 +324,27 @@ constexpr TwEntry twiddle_exact(int idx, int n) {
     return TwEntry{(float)e.x, (float)e.y};
 }
 
+// cos(2*pi*j/64) for j = 0..16 as float constants evaluated by the compiler (scalar constexpr
+// variables, so device code folds them), and cos64 / sin64 of any j by symmetry: the constants
+// c_m = exp(+2*pi*i*m/(2R)) of the complex-to-real pass's z twiddles for radix R <= 32.
+#define BGI_COS64(J) constexpr float kCos64_##J = (float)taylor_cos(kPi * (J) / 32.0);
+BGI_COS64(1) BGI_COS64(2) BGI_COS64(3) BGI_COS64(4) BGI_COS64(5) BGI_COS64(6) BGI_COS64(7) BGI_COS64(8)
+BGI_COS64(9) BGI_COS64(10) BGI_COS64(11) BGI_COS64(12) BGI_COS64(13) BGI_COS64(14) BGI_COS64(15)
+#undef BGI_COS64
+__host__ __device__ constexpr float cos64_base(int j) {
+    return j == 0 ? 1.0f : j == 1 ? kCos64_1 : j == 2 ? kCos64_2 : j == 3 ? kCos64_3 : j == 4 ? kCos64_4
+         : j == 5 ? kCos64_5 : j == 6 ? kCos64_6 : j == 7 ? kCos64_7 : j == 8 ? kCos64_8 : j == 9 ? kCos64_9
+         : j == 10 ? kCos64_10 : j == 11 ? kCos64_11 : j == 12 ? kCos64_12 : j == 13 ? kCos64_13
+         : j == 14 ? kCos64_14 : j == 15 ? kCos64_15 : 0.0f;
+}
+__host__ __device__ constexpr float cos64(int j) {
+    return (j & 63) <= 16 ? cos64_base(j & 63)
+         : (j & 63) <= 32 ? -cos64_base(32 - (j & 63))
+         : (j & 63) <= 48 ? -cos64_base((j & 63) - 32)
+                          : cos64_base(64 - (j & 63));
+}
+__host__ __device__ constexpr float sin64(int j) { return cos64(j - 16); }
+
 template <int N, int R>
 struct alignas(16) TwData {  // 16-byte aligned: bulk copies stage it in shared memory
     TwEntry v[TwTables<N, R>::SIZE];
@@ -552,17 +573,17 @@ template <int N>
 constexpr unsigned c2r_wz_bytes() {
     return (unsigned)((N / 2) * sizeof(float2));
 }
-// Twiddles formed in registers instead of staged tables (radix 8 or 16 rows): the pass twiddles
+// Twiddles formed in registers instead of staged tables: the pass twiddles
 // as powers of one table entry per pass (fft_transform's TWPOW), and the z twiddles
 // 1 + i exp(+2*pi*i*k/N) for k = t + m*P as 1 + i e_t c_m with e_t = exp(+2*pi*i*t/N) loaded once
 // per thread and c_m = exp(+2*pi*i*m/(2R)) compile-time constants (P/N = 1/(2R)).  The block
 // then stages only its rows.
-#ifndef C2R_COMPUTED_TW
-#define C2R_COMPUTED_TW 1
+#ifndef C2R_COMPUTED_TW_MAX_R
+#define C2R_COMPUTED_TW_MAX_R 32  // the largest row radix whose twiddles are formed in registers
 #endif
 template <int N>
 constexpr bool c2r_computed_tw() {
-    return C2R_COMPUTED_TW && C2RShape<N>::R <= 16;
+    return C2RShape<N>::R <= C2R_COMPUTED_TW_MAX_R;
 }
 template <int N>
 constexpr unsigned c2r_staged_tw_bytes() {
@@ -658,8 +679,8 @@ __device__ __forceinline__ void c2r_rows_body(float2 *grids, float2 *images, con
             if constexpr (CMP) {
                 // k = t + m*P with m fixed in the unrolled loading loop: exp(+2*pi*i*k/N) = e_t c_m
                 const int m = (k - t) / S::P;
-                constexpr int STEP = 32 / (2 * S::R);  // c_m = exp(+2*pi*i*(m*STEP)/32)
-                const float2 e = cmul(e_t, make_float2(cos32(m * STEP), sin32(m * STEP)));
+                constexpr int STEP = 64 / (2 * S::R);  // c_m = exp(+2*pi*i*(m*STEP)/64)
+                const float2 e = cmul(e_t, make_float2(cos64(m * STEP), sin64(m * STEP)));
                 P = make_float2(1.f - e.y, e.x);
             } else {
                 P = wz[k];
