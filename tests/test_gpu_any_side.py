@@ -189,3 +189,18 @@ def test_deterministic_gridder_any_side_and_uniform(im):
     for j in range(2):
         assert rel_l2(a[0, j], ref[0, j]) < IMAGE_TOL, j
     h.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 8, 15])
+def test_image_tiny_sides(im, n):
+    """The smallest sides through the handle (full plane, mixed-radix passes below 16): the
+    oracle's images, and the weight sums exact."""
+    obs = synth.small(seed=90 + n, n_ant=12, n_intervals=1, n_channels=2, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, counters, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n)
+    h = _imager(im, obs, n)
+    out = h.image(dev(vis)).cpu().numpy()
+    for j in range(2):
+        assert rel_l2(out[0, j], ref[0, j]) < IMAGE_TOL, j
+    assert np.array_equal(h.weight_sums(2), counters.reshape(2, -1).sum(1).astype(np.uint32))
+    h.close()
