@@ -585,6 +585,11 @@ template <int N>
 constexpr bool c2r_computed_tw() {
     return C2RShape<N>::R <= C2R_COMPUTED_TW_MAX_R;
 }
+// with the z twiddles computed: 1 = the pass twiddles as powers of one load per pass, 0 = each
+// read from the global table through the L1 cache (no shared-memory traffic either way)
+#ifndef C2R_TW_POWERS
+#define C2R_TW_POWERS 1
+#endif
 template <int N>
 constexpr unsigned c2r_staged_tw_bytes() {
     return c2r_computed_tw<N>() ? 0u : c2r_tw_bytes<N>();
@@ -671,7 +676,7 @@ __device__ __forceinline__ void c2r_rows_body(float2 *grids, float2 *images, con
     float2 *dst = images + row * N;
     float2 e_t = make_float2(1.f, 0.f);
     if constexpr (CMP) e_t = __ldg(reinterpret_cast<const float2 *>(g_c2r_root<N>.v) + t);
-    fft_transform<M, S::R, S::WARP, false, !CMP, CMP>(
+    fft_transform<M, S::R, S::WARP, false, !CMP, CMP && C2R_TW_POWERS != 0>(
         t, buf, CMP ? twiddles<M, S::R>() : tw,
         [&](int k) {
             const float2 a = buf[k], b = buf[M - k];
