@@ -573,8 +573,8 @@ template <int N>
 constexpr unsigned c2r_wz_bytes() {
     return (unsigned)((N / 2) * sizeof(float2));
 }
-// Twiddles formed in registers instead of staged tables: the pass twiddles
-// as powers of one table entry per pass (fft_transform's TWPOW), and the z twiddles
+// Twiddles without staged tables: the pass twiddles read from the global table through the L1
+// cache (or formed as powers of one table entry per pass, fft_transform's TWPOW), and the z twiddles
 // 1 + i exp(+2*pi*i*k/N) for k = t + m*P as 1 + i e_t c_m with e_t = exp(+2*pi*i*t/N) loaded once
 // per thread and c_m = exp(+2*pi*i*m/(2R)) compile-time constants (P/N = 1/(2R)).  The block
 // then stages only its rows.
@@ -585,10 +585,12 @@ template <int N>
 constexpr bool c2r_computed_tw() {
     return C2RShape<N>::R <= C2R_COMPUTED_TW_MAX_R;
 }
-// with the z twiddles computed: 1 = the pass twiddles as powers of one load per pass, 0 = each
-// read from the global table through the L1 cache (no shared-memory traffic either way)
+// with the z twiddles computed: 0 = each pass twiddle read from the global table through the L1
+// cache, 1 = the pass twiddles as powers of one load per pass (no shared-memory traffic either
+// way).  The same speed at 512^2 and 1024^2; the table is exact to half an ulp and needs fewer
+// registers (84 against 96 at 1024^2), so it is the default.
 #ifndef C2R_TW_POWERS
-#define C2R_TW_POWERS 1
+#define C2R_TW_POWERS 0
 #endif
 template <int N>
 constexpr unsigned c2r_staged_tw_bytes() {
