@@ -806,6 +806,22 @@ def run_ours(args, rank, world, local_rank):
                 "images_per_s": world * n_images / e2e_time(lambda: im.image_host(vis_h, flags=flags, out=out_h)),
                 "h2d_bytes_per_step": h2d_c64, "d2h_bytes_per_step": d2h_complex,
                 "what": "the reference caller's input and output types end to end"}
+        # correlator output: the XX correlation matrices (element (i, j), j <= i, is baseline
+        # i(i+1)/2 + j) uploaded, converted to s16 visibilities on the device and imaged
+        n_ant = obs.n_ant
+        ii, jj = np.tril_indices(n_ant)
+        xx = np.zeros((T, Cn, n_ant, n_ant), np.complex64)
+        xx[:, :, ii, jj] = np.asarray(obs.vis)[:, :, :, 0]
+        re_h = torch.from_numpy(np.ascontiguousarray(xx.real)).pin_memory()
+        im_h = torch.from_numpy(np.ascontiguousarray(xx.imag)).pin_memory()
+        del xx
+        e2e_variants["correlation_matrices_input_real_output"] = {
+            "images_per_s": world * n_images / e2e_time(lambda: im.image_matrices_host(
+                re_h, im_h, fmt="s16", flags=flags | IM.OUTPUT_REAL, out=out_hr)),
+            "h2d_bytes_per_step": 2 * n_images * n_ant * n_ant * 4, "d2h_bytes_per_step": d2h_real,
+            "what": "bgi_image_correlation_matrices_host: XX correlation matrices (float32 re, im) in, "
+                    "ingested to s16 on the device, real images back"}
+        del re_h, im_h
         del out_h
     t3 = time.monotonic()
     clocks.stop()

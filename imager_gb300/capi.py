@@ -88,6 +88,7 @@ _SIGNATURES = {
     "bgi_set_fft_mode": (_i, [_vp, _i]),
     "bgi_set_gridding_images_per_thread": (_i, [_vp, _i]),
     "bgi_set_column_radix": (_i, [_vp, _i]),
+    "bgi_image_correlation_matrices_host": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i, _u, _vp, _vp]),
     "bgi_get_column_radix": (_i, [_vp, _vp]),
     "bgi_get_gridding_images_per_thread": (_i, [_vp, _vp]),
     "bgi_get_fft_mode": (_i, [_vp, _vp]),

@@ -178,6 +178,7 @@ struct bgi_imager {
     DevBuf<unsigned int> wsum;    // per-image weight counts of the last call
     DevBuf<float> io_vis, io_img; // device staging of bgi_image_host
     DevBuf<float> io_scales;      // block scales staged by bgi_image_compressed_host
+    DevBuf<float> io_mat;         // correlation matrices staged by bgi_image_correlation_matrices_host
     int last_images = 0;
 
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
@@ -455,6 +456,7 @@ int bgi_destroy(bgi_imager *im) {
     im->wsum.release();
     im->io_vis.release();
     im->io_scales.release();
+    im->io_mat.release();
     im->io_img.release();
     delete im;
     return BGI_OK;
@@ -1232,11 +1234,15 @@ int planes_for(int pol, int out[2]) {
 // scales), its waves run on the lanes as soon as they have landed, and its images come back on
 // a second copy stream as soon as they are done, so uploads, imaging and downloads of
 // different chunks overlap.
+// mats (optional): host correlation matrices re_xx, im_xx, re_yy, im_yy [T][C][A][A] in place of
+// stored visibilities: each chunk's matrices are uploaded and converted on the device
+// (launch_ingest, on the upload stream) into the staged visibilities in `format`.
 int image_host_impl(bgi_imager *im, int format, const void *vis_host, const float *scales_host, int n_intervals,
-                    unsigned flags, float *images_host, void *stream) {
+                    unsigned flags, float *images_host, void *stream, const float *const *mats = nullptr) {
     TraceRange trace("bgi_image_host");
     BGI_TRY(image_checks(im, n_intervals, flags));
-    if (!vis_host || !images_host || (format != BGI_VIS_C64 && !scales_host))
+    if (!images_host || (!mats && (!vis_host || (format != BGI_VIS_C64 && !scales_host))) ||
+        (mats && (!mats[0] || !mats[1])))
         return set_error(BGI_ERR_INVALID, "image_host: null buffer");
     BGI_TRY(im->activate());
     cudaStream_t s = as_stream(stream);
@@ -1250,6 +1256,11 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     BGI_TRY(im->io_vis.ensure(rec_floats * n_images, "image_host vis staging"));
     if (planar) BGI_TRY(im->io_scales.ensure(sc_floats * n_images, "image_host scale staging"));
     BGI_TRY(im->io_img.ensure(img_floats * n_images, "image_host image staging"));
+    // correlation matrices: XX always, YY when given and the pol reads it
+    const size_t mat_floats = (size_t)im->n_ant * im->n_ant;  // one image's matrix
+    const bool with_yy = mats && mats[2] && mats[3] && (im->cfg.pol == BGI_POL_YY || im->cfg.pol == BGI_POL_I);
+    const int n_mats = mats ? (with_yy ? 4 : 2) : 0;
+    if (mats) BGI_TRY(im->io_mat.ensure(mat_floats * n_images * n_mats, "image_host matrix staging"));
     int wave = 0, n_lanes = 0;
     GridParams p = block_params(im, im->io_vis.ptr, n_intervals, flags, im->io_img.ptr, format,
                                       planar ? im->io_scales.ptr : nullptr);
@@ -1275,7 +1286,17 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     for (int c = 0; c < n_chunks; ++c) {
         const int img0 = c * chunk;
         const int cnt = std::min(chunk, n_images - img0);
-        if (!planar) {
+        if (mats) {
+            float *dm[4] = {nullptr, nullptr, nullptr, nullptr};
+            for (int q = 0; q < n_mats; ++q) {
+                dm[q] = im->io_mat.ptr + mat_floats * ((size_t)q * n_images + img0);
+                BGI_TRY(check_cuda(cudaMemcpyAsync(dm[q], mats[q] + mat_floats * img0, sizeof(float) * mat_floats * cnt,
+                                                   cudaMemcpyHostToDevice, im->copy_in),
+                                   "image_host H2D matrices"));
+            }
+            BGI_TRY(launch_ingest(dm[0], dm[1], dm[2], dm[3], im->n_ant, cnt, format, im->io_vis.ptr + rec_floats * img0,
+                                  planar ? im->io_scales.ptr + sc_floats * img0 : nullptr, im->copy_in));
+        } else if (!planar) {
             BGI_TRY(check_cuda(cudaMemcpyAsync(im->io_vis.ptr + rec_floats * img0, src + rec_floats * img0,
                                                sizeof(float) * rec_floats * cnt, cudaMemcpyHostToDevice, im->copy_in),
                                "image_host H2D"));
@@ -1331,6 +1352,15 @@ int bgi_image_compressed_host(bgi_imager *im, int format, const void *data_host,
     if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
         return set_error(BGI_ERR_INVALID, "image_compressed_host: bad format %d", format);
     return image_host_impl(im, format, data_host, scales_host, n_intervals, flags, images_host, stream);
+}
+
+int bgi_image_correlation_matrices_host(bgi_imager *im, int format, const float *re_xx, const float *im_xx,
+                                        const float *re_yy, const float *im_yy, int n_intervals, unsigned flags,
+                                        float *images_host, void *stream) {
+    if (format < BGI_VIS_C64 || format > BGI_VIS_FP16)
+        return set_error(BGI_ERR_INVALID, "image_correlation_matrices_host: bad format %d", format);
+    const float *mats[4] = {re_xx, im_xx, re_yy, im_yy};
+    return image_host_impl(im, format, nullptr, nullptr, n_intervals, flags, images_host, stream, mats);
 }
 
 int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream) {

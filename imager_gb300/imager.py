@@ -333,6 +333,18 @@ class Imager:
              _ptr(out), _stream(stream))
         return out
 
+    def image_matrices_host(self, re_xx, im_xx, re_yy=None, im_yy=None, fmt="s16",
+                            flags: int = APPLY_GEOMETRIC | APPLY_CABLE, out=None, stream=None):
+        """Host correlation matrices float32 [T][C][A][A] (XX; YY optional) to host images: uploaded,
+        converted to stored visibilities of `fmt` and imaged on the device, chunk by chunk."""
+        T, Cn = int(re_xx.shape[0]), int(re_xx.shape[1])
+        n = self.n_pixels
+        if out is None:
+            out = np.empty((T, Cn, n, n), np.float32 if flags & OUTPUT_REAL else np.complex64)
+        call("bgi_image_correlation_matrices_host", self._h, VIS_FORMAT[fmt], _ptr(re_xx), _ptr(im_xx),
+             _ptr(re_yy), _ptr(im_yy), T, int(flags), _ptr(out), _stream(stream))
+        return out
+
     @property
     def schedule(self):
         """(images per wave, lanes) of the bgi_image* calls; 0 images per wave = auto."""

@@ -320,6 +320,18 @@ BGI_API int bgi_image_compressed_host(bgi_imager *im, int format, const void *da
                                       const float *scales_host, int n_intervals, unsigned flags,
                                       float *images_host, void *stream);
 
+/* From correlator output to images, on host buffers: the block's correlation matrices
+ * float[T][C][n_ant][n_ant] (XX; YY or both NULL, as bgi_ingest_correlation_matrices) are
+ * uploaded chunk by chunk, converted on the device into stored visibilities of `format` (complex64
+ * records or a 16-bit format, encoded as bgi_compress_visibilities encodes), imaged as
+ * bgi_image_compressed / bgi_image do with `flags`, and the images copied back; uploads, ingest,
+ * imaging and downloads of different chunks overlap.  Replaces the reference's host-side
+ * ConvertFits2XCorr (apps/pacer_imager_main.cpp:720-804) followed by run(); the YY matrices are
+ * uploaded only for pols YY and I.  Synchronises the stream before returning. */
+BGI_API int bgi_image_correlation_matrices_host(bgi_imager *im, int format, const float *re_xx, const float *im_xx,
+                                                const float *re_yy, const float *im_yy, int n_intervals,
+                                                unsigned flags, float *images_host, void *stream);
+
 /* Per-image weight sums (number of gridded points) of the last bgi_image call on this
  * handle, as uint32[n_images]; copies to host and synchronises the stream. */
 BGI_API int bgi_last_weight_sums(bgi_imager *im, uint32_t *sums_host, int n_images, void *stream);
