@@ -90,6 +90,8 @@ int64_t bgo_gridding(const float *vis, int n_intervals, int n_channels, int n_an
 void bgo_fft2_inverse_f64(const double *in, double *out, int n_pixels, int n_images);
 /* The same transform in FP32 arithmetic (used for the timed CPU baseline). */
 void bgo_fft2_inverse_f32(const float *in, float *out, int n_pixels, int n_images);
+/* the same transform one line at a time (the check of bgo_fft2_inverse_f32's blocked form) */
+void bgo_fft2_inverse_f32_scalar(const float *in, float *out, int n_pixels, int n_images);
 
 /* fftshift by swapping halves along x then y (src/pacer_imager.cpp:110-128), complex data. */
 void bgo_fft_shift_f32(float *image, int x_side, int y_side);

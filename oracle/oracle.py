@@ -71,6 +71,7 @@ def library():
                                    dbl, i32, dbl, i32, i32, _f32p, _f32p]),
             "bgo_fft2_inverse_f64": (None, [_f64p, _f64p, i32, i32]),
             "bgo_fft2_inverse_f32": (None, [_f32p, _f32p, i32, i32]),
+            "bgo_fft2_inverse_f32_scalar": (None, [_f32p, _f32p, i32, i32]),
             "bgo_fft_shift_f32": (None, [_f32p, i32, i32]),
             "bgo_fft_shift_f64": (None, [_f64p, i32, i32]),
             "bgo_image_f64": (None, [_f32p, _f32p, i32, i32, _f64p]),
