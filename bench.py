@@ -405,6 +405,37 @@ def serving_measure(args):
     return res
 
 
+def host_link_rates(host_out, h2d_bytes, reps=3):
+    """Plain copies over the host link with the step's byte counts: the pinned image buffer
+    from a device buffer of its size (device to host) and h2d_bytes from pinned memory (host to
+    device), each timed with CUDA events on the current stream, best of `reps`.  The end-to-end
+    step cannot beat max(d2h / d2h_gbs, h2d / h2d_gbs), the two directions running at once."""
+    s = torch.cuda.current_stream()
+    dev = torch.empty(host_out.numel(), dtype=host_out.dtype, device="cuda")
+    src_h = torch.empty(max(h2d_bytes // 4, 1), dtype=torch.float32).pin_memory()
+    dst_d = torch.empty_like(src_h, device="cuda")
+    host_flat = host_out.view(-1)
+
+    def rate(fn, nbytes):
+        best = float("inf")
+        for _ in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(s)
+            fn()
+            e1.record(s)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return nbytes / (best / 1000.0) / 1e9
+
+    d2h = rate(lambda: host_flat.copy_(dev, non_blocking=True), host_out.numel() * host_out.element_size())
+    h2d = rate(lambda: dst_d.copy_(src_h, non_blocking=True), src_h.numel() * 4)
+    del dev, dst_d, src_h
+    return {"d2h_gbs": d2h, "h2d_gbs": h2d,
+            "what": "plain pinned copies of the step's bytes over the host link (cudaMemcpyAsync through "
+                    "torch), each direction alone, best of 3"}
+
+
 def batched_measure(args, stream, flush):
     """The uneven batch workload: 512 antennas in 16 sub-stations, 256 channels in four bands of 64
     imaged at 256/512/1024/2048 pixels, 5 intervals, s16 stored, complex images on the device.
@@ -788,6 +819,7 @@ def run_ours(args, rank, world, local_rank):
         h2d = n_images * n_planes * (B * 4 + int(s_h.shape[-1]) * 4)
     e2e_s = e2e_time(e2e_step)
     d2h_real, d2h_complex = n_images * N * N * 4, n_images * N * N * 8
+    link = host_link_rates(out_hr, h2d)
     e2e_variants = {}
     if args.variants:
         out_h = torch.empty((T, Cn, N, N), dtype=torch.complex64).pin_memory()
@@ -944,6 +976,10 @@ def run_ours(args, rank, world, local_rank):
         "vis_per_s": world * gridded_vis * args.steps / (ms / 1000.0),
         "e2e": {"value": world * n_images / e2e_s, "unit": "images/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h_real,
+                "link": dict(link, bound_images_per_s=world * n_images / max(d2h_real / link["d2h_gbs"] / 1e9,
+                                                                             h2d / link["h2d_gbs"] / 1e9),
+                             frac=(n_images / e2e_s) / (n_images / max(d2h_real / link["d2h_gbs"] / 1e9,
+                                                                       h2d / link["h2d_gbs"] / 1e9))),
                 "api": ("bgi_image_host" if fmt == "c64" else "bgi_image_compressed_host") +
                        " with BGI_OUTPUT_REAL (pinned host buffers; XX images are real)",
                 "variants": e2e_variants},

@@ -91,6 +91,8 @@ _SIGNATURES = {
     "bgi_image_correlation_matrices_host": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i, _u, _vp, _vp]),
     "bgi_get_column_radix": (_i, [_vp, _vp]),
     "bgi_get_gridding_images_per_thread": (_i, [_vp, _vp]),
+    "bgi_set_gridding_aggregation": (_i, [_vp, _i]),
+    "bgi_get_gridding_aggregation": (_i, [_vp, _vp]),
     "bgi_get_fft_mode": (_i, [_vp, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),
     "bgi_create": (_i, [C.POINTER(Config), C.POINTER(_vp)]),

@@ -154,6 +154,7 @@ struct bgi_imager {
     int fft_mode = BGI_FFT_SIMT;  // enum bgi_fft_mode
     int grid_cpt = 0;             // gridding images per thread (0: by array size)
     int col_radix = 0;            // column-pass radix of the half plane (0: the side's default)
+    int grid_agg = 0;             // 1: warp-aggregated gridding atomics (4 or 8 images per thread)
     DevBuf<float> kb_table;    // its rows [1023][kb_size]
     bool cc_valid = false;     // d_cc matches the frequencies and delta_u/v
     int *d_flags = nullptr;
@@ -766,6 +767,7 @@ GridParams block_params(const bgi_imager *im, const float *vis, int n_intervals,
     p.kb_size = im->kb_size;
     p.kb_table = im->kb_table.ptr;
     p.cpt = im->grid_cpt;
+    p.aggregate = im->grid_agg;
     // the complex-to-real pass stores pixel pairs: 16 bytes of complex or 8 bytes of real pixels
     if ((reinterpret_cast<uintptr_t>(images) & ((flags & BGI_OUTPUT_REAL) ? 7u : 15u)) != 0) p.half_width = 0;
     // uniform weighting divides cells by their counters: full-plane grids with counter grids
@@ -1052,9 +1054,10 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
         *ms = t / (float)reps;
         return r;
     };
-    static const int kWaves[] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64};
+    // 0: the automatic wave; 1-3 suit the large sides, whose single images fill the GPU
+    static const int kWaves[] = {0, 1, 2, 3, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64};
     int best_wave = im->cfg.max_images_per_wave, best_lanes = im->lanes;
-    int best_cpt = im->grid_cpt, best_fft = im->fft_mode, best_radix = im->col_radix;
+    int best_cpt = im->grid_cpt, best_fft = im->fft_mode, best_radix = im->col_radix, best_agg = im->grid_agg;
     float best = 3.4e38f;
     // 1. images per wave x lanes, with the gridding and FFT defaults: every candidate timed over
     // three calls, then the three fastest again over ten calls each (a three-call time of a
@@ -1062,6 +1065,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     im->grid_cpt = 0;
     im->fft_mode = BGI_FFT_SIMT;
     im->col_radix = 0;
+    im->grid_agg = 0;
     struct Cand {
         float ms;
         int wave, lanes;
@@ -1090,6 +1094,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
             best_cpt = 0;
             best_fft = BGI_FFT_SIMT;
             best_radix = 0;
+            best_agg = 0;
         }
     }
     // 2. at the best wave and lanes: gridding images per thread, then the last FFT pass's arithmetic
@@ -1104,6 +1109,23 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
             best = ms;
             best_cpt = cpt;
         }
+    }
+    // warp-aggregated atomics (the looping kernel: half plane, 4 or 8 images per thread); they
+    // pay where the array's points crowd few cells
+    if (im->half_plane_path()) {
+        im->grid_agg = 1;
+        for (int cpt : {4, 8}) {
+            if (st) break;
+            im->grid_cpt = cpt;
+            float ms = 0.f;
+            st = time_current(&ms, 10);
+            if (!st && ms < best) {
+                best = ms;
+                best_cpt = cpt;
+                best_agg = 1;
+            }
+        }
+        im->grid_agg = best_agg;
     }
     im->grid_cpt = best_cpt;
     // 3. the column pass's other compiled radix (half plane)
@@ -1135,6 +1157,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     im->grid_cpt = best_cpt;
     im->fft_mode = best_fft;
     im->col_radix = best_radix;
+    im->grid_agg = best_agg;
     if (st) return st;
     // drop the candidates' scratch; the chosen schedule sizes its own on the next call
     BGI_TRY(check_cuda(cudaStreamSynchronize(s), "autotune sync"));
@@ -1174,6 +1197,18 @@ int bgi_set_gridding_images_per_thread(bgi_imager *im, int images_per_thread) {
 int bgi_get_gridding_images_per_thread(const bgi_imager *im, int *images_per_thread) {
     if (!im || !images_per_thread) return set_error(BGI_ERR_INVALID, "get_gridding_images_per_thread: bad arguments");
     *images_per_thread = im->grid_cpt;
+    return BGI_OK;
+}
+
+int bgi_set_gridding_aggregation(bgi_imager *im, int on) {
+    if (!im || (on != 0 && on != 1)) return set_error(BGI_ERR_INVALID, "set_gridding_aggregation: 0 or 1");
+    im->grid_agg = on;
+    return BGI_OK;
+}
+
+int bgi_get_gridding_aggregation(const bgi_imager *im, int *on) {
+    if (!im || !on) return set_error(BGI_ERR_INVALID, "get_gridding_aggregation: bad arguments");
+    *on = im->grid_agg;
     return BGI_OK;
 }
 

@@ -334,12 +334,11 @@ bool lean_applies(const GridParams &q, int cpt) {
 // is done once for all IMG images, and all of a thread's global loads are in flight together.
 // The images of a block may span two intervals with their own UVW sets (the block's images are
 // consecutive); u/v/w and the delay are then reloaded where the set changes.
-// GRID_WARP_AGG: equal cells within a warp summed before one atomic per cell (an experiment; the
-// points of a warp fall on distinct cells 99.8 % of the time at the workload)
-#ifndef GRID_WARP_AGG
-#define GRID_WARP_AGG 0
-#endif
-#if GRID_WARP_AGG
+// Warp aggregation (AGG): the points of a warp that fall on the same cell are summed at one lane
+// before a single atomic per distinct cell.  It pays where many points share few cells (an array
+// whose short baselines crowd the centre of a small grid: the uneven batch's 256^2 band puts its
+// 130,816 points of an image on about 300 cells, 9.5 % of a warp's points on distinct cells) and
+// costs where they are spread (99.8 % distinct at the 512^2 workload); bgi_autotune times it.
 __device__ __forceinline__ void warp_aggregated_add(float2 *base, int key, float2 v) {
     const int lane = (int)(threadIdx.x & 31);
     const unsigned grp = __match_any_sync(0xffffffffu, key >= 0 ? key : -1 - lane);  // idle lanes alone
@@ -356,9 +355,8 @@ __device__ __forceinline__ void warp_aggregated_add(float2 *base, int key, float
     }
     if (key >= 0 && lane == __ffs(grp) - 1) atomicAdd(base + (unsigned)key, v);
 }
-#endif
 
-template <int POL, int FMT, int IMG>
+template <int POL, int FMT, int IMG, bool AGG = false>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_half_loop_kernel(const GridParams p) {
     __shared__ unsigned int s_count[IMG][kThreads / 32];
     constexpr int P0 = POL == BGI_POL_XX ? 0 : POL == BGI_POL_YY ? 3 : POL == BGI_POL_I ? 0 : 1;  // planes
@@ -416,10 +414,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_half_loop_kernel(co
         }
         const float4 hot = __ldg(reinterpret_cast<const float4 *>(p.chan_consts + ch));
         unsigned int counted = 0;
-#if GRID_WARP_AGG
-        int key1 = -1, key2 = -1;
+        int key1 = -1, key2 = -1;  // AGG: the point's cell offsets from gbase (-1: none)
         float2 z1 = make_float2(0.f, 0.f), z2 = z1;
-#endif
         if (in_range && flag <= 0) {
             float2 a = ra[j], bb = rb[j];
             if (!C64) {
@@ -442,27 +438,27 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) grid_half_loop_kernel(co
             if (ok) {
                 const int u1 = ui + (n & (ui >> 31)), v1 = vi + (n & (vi >> 31));
                 const int u2 = -ui + (n & (-ui >> 31)), v2 = -vi + (n & (-vi >> 31));
-#if GRID_WARP_AGG
-                if (u1 <= n / 2) {
-                    key1 = j * n * w + v1 * w + u1;
-                    z1 = z;
+                if constexpr (AGG) {
+                    if (u1 <= n / 2) {
+                        key1 = j * n * w + v1 * w + u1;
+                        z1 = z;
+                    }
+                    if (u2 <= n / 2) {
+                        key2 = j * n * w + v2 * w + u2;
+                        z2 = make_float2(z.x, -z.y);
+                    }
+                } else {
+                    float2 *g = gbase + (unsigned)(j * n * w);
+                    if (u1 <= n / 2) atomicAdd(g + (unsigned)(v1 * w + u1), z);
+                    if (u2 <= n / 2) atomicAdd(g + (unsigned)(v2 * w + u2), make_float2(z.x, -z.y));
                 }
-                if (u2 <= n / 2) {
-                    key2 = j * n * w + v2 * w + u2;
-                    z2 = make_float2(z.x, -z.y);
-                }
-#else
-                float2 *g = gbase + (unsigned)(j * n * w);
-                if (u1 <= n / 2) atomicAdd(g + (unsigned)(v1 * w + u1), z);
-                if (u2 <= n / 2) atomicAdd(g + (unsigned)(v2 * w + u2), make_float2(z.x, -z.y));
-#endif
                 counted = 2;
             }
         }
-#if GRID_WARP_AGG
-        warp_aggregated_add(gbase, key1, z1);
-        warp_aggregated_add(gbase, key2, z2);
-#endif
+        if constexpr (AGG) {  // every lane of the warp takes part
+            warp_aggregated_add(gbase, key1, z1);
+            warp_aggregated_add(gbase, key2, z2);
+        }
         const unsigned int warp_total = __reduce_add_sync(0xffffffffu, counted);
         if ((threadIdx.x & 31) == 0) s_count[j][threadIdx.x >> 5] = warp_total;
         if (++ch == p.n_channels) ch = 0;
@@ -488,9 +484,12 @@ bool loop_applies(const GridParams &q, int img) {
 template <int POL, int FMT, int CPT>
 void launch_fmt(const dim3 &grid, const GridParams &q, cudaStream_t s) {
     const bool one = one_set(q, CPT);
-    if (CPT >= 4 && loop_applies(q, CPT)) {
-        grid_half_loop_kernel<POL, FMT, CPT><<<grid, kThreads, 0, s>>>(q);
-        return;
+    if constexpr (CPT >= 4) {
+        if (loop_applies(q, CPT)) {
+            if (q.aggregate) grid_half_loop_kernel<POL, FMT, CPT, true><<<grid, kThreads, 0, s>>>(q);
+            else grid_half_loop_kernel<POL, FMT, CPT><<<grid, kThreads, 0, s>>>(q);
+            return;
+        }
     }
     if (lean_applies(q, CPT)) {
         grid_half_lean_kernel<POL, FMT, CPT><<<grid, kThreads, 0, s>>>(q);
@@ -527,10 +526,21 @@ void launch_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
 template <int POL>
 void launch_loop8_pol(const dim3 &grid, const GridParams &q, cudaStream_t s) {
     switch (q.vis_format) {
-        case BGI_VIS_S16: grid_half_loop_kernel<POL, BGI_VIS_S16, 8><<<grid, kThreads, 0, s>>>(q); break;
-        case BGI_VIS_BF16: grid_half_loop_kernel<POL, BGI_VIS_BF16, 8><<<grid, kThreads, 0, s>>>(q); break;
-        case BGI_VIS_FP16: grid_half_loop_kernel<POL, BGI_VIS_FP16, 8><<<grid, kThreads, 0, s>>>(q); break;
-        default: grid_half_loop_kernel<POL, BGI_VIS_C64, 8><<<grid, kThreads, 0, s>>>(q);
+        case BGI_VIS_S16:
+            if (q.aggregate) grid_half_loop_kernel<POL, BGI_VIS_S16, 8, true><<<grid, kThreads, 0, s>>>(q);
+            else grid_half_loop_kernel<POL, BGI_VIS_S16, 8><<<grid, kThreads, 0, s>>>(q);
+            break;
+        case BGI_VIS_BF16:
+            if (q.aggregate) grid_half_loop_kernel<POL, BGI_VIS_BF16, 8, true><<<grid, kThreads, 0, s>>>(q);
+            else grid_half_loop_kernel<POL, BGI_VIS_BF16, 8><<<grid, kThreads, 0, s>>>(q);
+            break;
+        case BGI_VIS_FP16:
+            if (q.aggregate) grid_half_loop_kernel<POL, BGI_VIS_FP16, 8, true><<<grid, kThreads, 0, s>>>(q);
+            else grid_half_loop_kernel<POL, BGI_VIS_FP16, 8><<<grid, kThreads, 0, s>>>(q);
+            break;
+        default:
+            if (q.aggregate) grid_half_loop_kernel<POL, BGI_VIS_C64, 8, true><<<grid, kThreads, 0, s>>>(q);
+            else grid_half_loop_kernel<POL, BGI_VIS_C64, 8><<<grid, kThreads, 0, s>>>(q);
     }
 }
 

@@ -50,6 +50,7 @@ struct GridParams {
     const float *kb_table;     // Kaiser-Bessel kernel rows [1023][kb_size] (kb_size > 0), else null
     int kb_size;               // 0: nearest neighbour; K: K x K convolution kernel (full plane)
     int cpt;                   // images per gridding thread: 2, 4 or 8, 0 = by array size
+    int aggregate;             // 1: warp-aggregated atomics (half plane, 4 or 8 images per thread)
 };
 int launch_gridding(const GridParams &p, cudaStream_t s);
 // table[c] = make_channel_const(freqs[c], du, dv) for c < n_channels

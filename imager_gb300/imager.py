@@ -382,6 +382,17 @@ class Imager:
         call("bgi_get_gridding_images_per_thread", self._h, C.byref(k))
         return k.value
 
+    def set_gridding_aggregation(self, on: bool = False):
+        """Warp-aggregated gridding atomics (half plane, 4 or 8 images per thread): points of a
+        warp on the same cell summed before one atomic per cell."""
+        call("bgi_set_gridding_aggregation", self._h, int(on))
+
+    @property
+    def gridding_aggregation(self) -> bool:
+        k = C.c_int()
+        call("bgi_get_gridding_aggregation", self._h, C.byref(k))
+        return bool(k.value)
+
     def set_column_radix(self, radix: int = 0):
         """Radix of the half-plane column pass (0: the side's default; sides 256..4096 have a
         second compiled radix)."""

@@ -410,14 +410,14 @@ BGI_API int bgi_get_fft_mode(const bgi_imager *im, int *mode);
  * per lane, 24 half-plane images at 512^2), lanes (1..8 streams that image alternate waves,
  * each with its own grid scratch; 2 by default), images per gridding thread (2, 4 or 8; 0 =
  * default: 4 on the half-plane path, else 2 below 65,536 baselines and 4 above; on the half
- * plane 4 and 8 issue all of a thread's visibility loads before gridding any) and the FFT
- * arithmetic (bgi_set_fft_mode).
- * bgi_autotune times every wave size in {auto, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64} (up to
- * the block's image count) with 1-8 lanes on the caller's own block (one call to size the
- * scratch, three timed with CUDA events on the stream), times the three fastest again over ten
- * calls each, then, at the best of those, 2, 4 and 8 images per gridding thread, the column
- * pass's second radix (bgi_set_column_radix) and (image side 512, half plane) the tensor-core
- * row pass (ten timed calls each);
+ * plane 4 and 8 issue all of a thread's visibility loads before gridding any), warp-aggregated
+ * gridding atomics (bgi_set_gridding_aggregation) and the FFT arithmetic (bgi_set_fft_mode).
+ * bgi_autotune times every wave size in {auto, 1, 2, 3, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48,
+ * 64} (up to the block's image count) with 1-8 lanes on the caller's own block (one call to size
+ * the scratch, three timed with CUDA events on the stream), times the three fastest again over
+ * ten calls each, then, at the best of those, 2, 4 and 8 images per gridding thread, 4 and 8
+ * with aggregated atomics (half plane), the column pass's second radix (bgi_set_column_radix)
+ * and (image side 512, half plane) the tensor-core row pass (ten timed calls each);
  * it keeps the fastest on the handle, frees the candidates' scratch and writes the best
  * milliseconds per call to *best_ms (may be NULL).  Synchronous; `images` receives the block's
  * images.  No reference counterpart. */
@@ -429,6 +429,14 @@ BGI_API int bgi_set_gridding_images_per_thread(bgi_imager *im, int images_per_th
 BGI_API int bgi_set_column_radix(bgi_imager *im, int radix);
 BGI_API int bgi_get_column_radix(const bgi_imager *im, int *radix);
 BGI_API int bgi_get_gridding_images_per_thread(const bgi_imager *im, int *images_per_thread);
+/* Warp-aggregated gridding atomics (0 = off, the default; 1 = on): the visibilities of a warp
+ * that land on the same cell are summed across its lanes before one atomic per distinct cell.
+ * Applies on the half-plane path with 4 or 8 images per gridding thread (the default 4 there);
+ * elsewhere the setting is kept and has no effect.  It pays where many points share few cells
+ * (short baselines on a small grid) and costs a few percent where they are spread.  Sums are
+ * regrouped, so cells agree with the plain atomics to FP32 rounding. */
+BGI_API int bgi_set_gridding_aggregation(bgi_imager *im, int on);
+BGI_API int bgi_get_gridding_aggregation(const bgi_imager *im, int *on);
 BGI_API int bgi_set_schedule(bgi_imager *im, int images_per_wave, int lanes);
 BGI_API int bgi_get_schedule(const bgi_imager *im, int *images_per_wave, int *lanes);
 BGI_API int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scales,

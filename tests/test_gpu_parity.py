@@ -634,6 +634,38 @@ def test_gridding_images_per_thread_against_oracle(im, pol, cpt):
     h.close()
 
 
+@pytest.mark.parametrize("pol", ["XX", "I"])
+@pytest.mark.parametrize("cpt", [4, 8])
+def test_gridding_aggregation_against_oracle(im, pol, cpt):
+    """Warp-aggregated gridding atomics on a crowded grid (100 antennas in a 35 m disk imaged at
+    64^2: about 15,000 points per image on at most 2,080 half-plane cells, so most warps hold
+    repeated cells): the oracle within 1e-4, the plain atomics within FP32 rounding, weight sums
+    exact; complex64 and s16 storage, per-interval UVW sets."""
+    n = 64
+    obs = synth.small(seed=90 + cpt, n_ant=100, n_intervals=3, n_channels=3, n_pixels=n)
+    vis = obs.vis_f32()
+    _, _, counters, ref, _ = O.full_pipeline(vis, obs.u, obs.v, obs.w, obs.cable, obs.flags, obs.freqs, n,
+                                             pol=pol, n_uvw_sets=3)
+    h = _imager_for(im, obs, n, pol)
+    assert h.half_plane and not h.gridding_aggregation
+    h.set_gridding_images_per_thread(cpt)
+    plain = h.image(dev(vis)).cpu().numpy()
+    h.set_gridding_aggregation(True)
+    assert h.gridding_aggregation
+    agg = h.image(dev(vis)).cpu().numpy()
+    data, scales = im.compress_visibilities(dev(vis), "s16")
+    s16 = h.image_compressed(data, scales, "s16").cpu().numpy()
+    for i in range(3):
+        for j in range(3):
+            assert rel_l2(agg[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+            assert rel_l2(s16[i, j], ref[i, j]) < IMAGE_TOL, (i, j)
+            assert rel_l2(agg[i, j], plain[i, j]) < 2e-6, (i, j)
+    assert np.array_equal(h.weight_sums(9), counters.reshape(9, -1).sum(1).astype(np.uint32))
+    with pytest.raises(capi.BgiError):
+        h.set_gridding_aggregation(2)
+    h.close()
+
+
 @pytest.mark.parametrize("n", [256, 512, 1024])
 def test_column_radix_alternatives(im, n):
     """The column pass's second compiled radix images the same block as the default one (the
