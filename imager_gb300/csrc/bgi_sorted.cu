@@ -33,16 +33,24 @@ struct SortedWs {
     unsigned *start;    // [chunk][N*N] first segment slot of each cell within its tile
     unsigned *tile_off; // [chunk][tiles(N)] first segment slot of each tile of kScanTile cells
     unsigned *cursor;   // [chunk][N*N] slots used so far
-    unsigned *n_long;   // [chunk] cells whose segment is longer than kShortSeg
-    unsigned *longs;    // [chunk][long_cap(B)] those cells
+    unsigned *n_long;   // [chunk] cells whose segment is longer than kShortSeg, up to kLongSort
+    unsigned *n_huge;   // [chunk] cells whose segment is longer than kLongSort
+    unsigned *longs;    // [chunk][long_cap(B)] the first from the front, the second from the back
 };
 
-// Segments up to this length are ordered by the thread of their cell; longer ones (rare: many
-// short baselines in one cell) are handed to one block each.
+// Segments up to this length are ordered by the thread of their cell; longer ones (many short
+// baselines in one cell) are handed to one block each.
 constexpr unsigned kShortSeg = 32;
 constexpr int kLongThreads = 512;
-constexpr int kLongBlocks = 8;  // blocks per image sharing its long cells
+constexpr int kLongBlocks = 32;  // blocks per image sharing its long cells, at least (four per SM
+                                 // across the chunk's images when that is more)
+constexpr int kHugeBlocks = 8;   // blocks per image sharing its huge cells
 constexpr int kTile = 1024;
+// Long segments up to kLongSort points are ordered by a bitonic sort in shared memory (32 KB,
+// several blocks per SM), huge ones up to kHugeSort in a block of 128 KB of shared memory, and
+// longer ones still (over 32,768 points in one cell) by counting ranks against tiles.
+constexpr unsigned kLongSort = 8192;
+constexpr unsigned kHugeSort = 32768;
 // The per-image prefix sum runs over tiles of 4096 cells (256 threads x 16 cells), then over
 // the tiles' totals.
 constexpr int kScanTile = 4096;
@@ -58,7 +66,7 @@ __host__ __device__ inline size_t long_cap(long long nb) { return (size_t)(2 * n
 size_t per_image_bytes(long long nb, int n) {
     const size_t pts = 2 * (size_t)nb, cells = (size_t)n * n;
     return pts * (sizeof(unsigned) + sizeof(float2) + sizeof(unsigned)) + 3 * cells * sizeof(unsigned) +
-           (1 + long_cap(nb) + scan_tiles(n)) * sizeof(unsigned) + 9 * 256;  // 9 arrays, each start rounded up to 256 B
+           (2 + long_cap(nb) + scan_tiles(n)) * sizeof(unsigned) + 10 * 256;  // 10 arrays, each start rounded up to 256 B
 }
 
 SortedWs carve(void *ws, int chunk, long long nb, int n) {
@@ -78,6 +86,7 @@ SortedWs carve(void *ws, int chunk, long long nb, int n) {
     w.cursor = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
     w.tile_off = reinterpret_cast<unsigned *>(take(chunk * scan_tiles(n) * sizeof(unsigned)));
     w.n_long = reinterpret_cast<unsigned *>(take(chunk * sizeof(unsigned)));
+    w.n_huge = reinterpret_cast<unsigned *>(take(chunk * sizeof(unsigned)));
     w.longs = reinterpret_cast<unsigned *>(take(chunk * long_cap(nb) * sizeof(unsigned)));
     return w;
 }
@@ -305,9 +314,12 @@ __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, in
     const size_t cbase = (size_t)local * cells;
     const unsigned len = w.cnt[cbase + c];
     if (len == 0) return;
-    if (len > kShortSeg) {
-        const unsigned slot = atomicAdd(w.n_long + local, 1u);
-        w.longs[(size_t)local * long_cap(n_points / 2) + slot] = (unsigned)c;
+    if (len > kShortSeg) {  // every listed cell holds more than kShortSeg points: both lists fit
+        const size_t cap = long_cap(n_points / 2);
+        if (len <= kLongSort)
+            w.longs[(size_t)local * cap + atomicAdd(w.n_long + local, 1u)] = (unsigned)c;
+        else
+            w.longs[(size_t)local * cap + cap - 1 - atomicAdd(w.n_huge + local, 1u)] = (unsigned)c;
         return;
     }
     const int img = chunk_first + local;
@@ -348,27 +360,64 @@ __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, in
     }
 }
 
-// long segments: one block per cell.  Each point index is placed at its rank (the number of
+// Ascending bitonic sort of s[0..len) in shared memory, padded with 0xffffffff to the next power
+// of two P (the padding sorts last; s holds P entries).  Every thread of the block takes part.
+__device__ void bitonic_sort_shared(unsigned *s, unsigned len) {
+    unsigned P = 2;
+    while (P < len) P <<= 1;
+    for (unsigned i = len + threadIdx.x; i < P; i += blockDim.x) s[i] = 0xffffffffu;
+    __syncthreads();
+    for (unsigned k = 2; k <= P; k <<= 1) {
+        for (unsigned j = k >> 1; j > 0; j >>= 1) {
+            for (unsigned i = threadIdx.x; i < P; i += blockDim.x) {
+                const unsigned ixj = i ^ j;  // < P: j < P and P is a power of two
+                if (ixj > i) {
+                    const unsigned a = s[i], b = s[ixj];
+                    if ((a > b) == ((i & k) == 0)) {
+                        s[i] = b;
+                        s[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// long segments: one block per cell.  A segment of up to kLongSort points is loaded into shared
+// memory and sorted there; a longer one has each point index placed at its rank (the number of
 // smaller indices in the segment, counted against shared-memory tiles) in the cell's range of
-// the key array, which is free after placement; then the values are staged in tiles and thread
-// 0 adds them in that order.
+// the key array, which is free after placement.  Then the values are staged in tiles in index
+// order and thread 0 adds them in that order.
+// HUGE: the cells listed from the back (more than kLongSort points), sorted in shared memory up
+// to kHugeSort.  Shared memory (dynamic): CAP point indices, then kTile staged values.
+template <bool HUGE>
 __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, int chunk_first, SortedWs w,
                                                             long long n_points) {
-    __shared__ unsigned s_idx[kTile];
-    __shared__ float2 s_val[kTile];
+    constexpr unsigned CAP = HUGE ? kHugeSort : kLongSort;
+    extern __shared__ __align__(16) unsigned s_dyn[];
+    unsigned *s_idx = s_dyn;
+    float2 *s_val = reinterpret_cast<float2 *>(s_dyn + CAP);
     const int n = p.n_pixels;
     const size_t cells = (size_t)n * n;
     const int local = blockIdx.y;
     const int img = chunk_first + local;
-    const unsigned n_long = w.n_long[local];
-    for (unsigned li = blockIdx.x; li < n_long; li += gridDim.x) {
-        const unsigned c = w.longs[(size_t)local * long_cap(n_points / 2) + li];
+    const size_t cap = long_cap(n_points / 2);
+    const unsigned n_list = HUGE ? w.n_huge[local] : w.n_long[local];
+    for (unsigned li = blockIdx.x; li < n_list; li += gridDim.x) {
+        const unsigned c = w.longs[(size_t)local * cap + (HUGE ? cap - 1 - li : li)];
         const size_t cbase = (size_t)local * cells;
         const unsigned len = w.cnt[cbase + c];
         const unsigned st = seg_start(w, local, n, c);
         const unsigned *seg = w.seg + (size_t)local * n_points + st;
         unsigned *ordered = w.key + (size_t)local * n_points + st;
-        for (unsigned i0 = 0; i0 < len; i0 += kLongThreads) {
+        const bool in_shared = len <= CAP;
+        if (in_shared) {
+            for (unsigned i = threadIdx.x; i < len; i += kLongThreads) s_idx[i] = seg[i];
+            bitonic_sort_shared(s_idx, len);  // ends with a block barrier
+            ordered = s_idx;
+        }
+        for (unsigned i0 = 0; !in_shared && i0 < len; i0 += kLongThreads) {
             const bool mine_valid = i0 + threadIdx.x < len;
             const unsigned mine = mine_valid ? seg[i0 + threadIdx.x] : 0u;
             unsigned rank = 0;
@@ -412,6 +461,8 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, 
     }
 }
 
+constexpr size_t long_smem_bytes(unsigned cap) { return cap * sizeof(unsigned) + kTile * sizeof(float2); }
+
 }  // namespace
 
 size_t sorted_workspace_bytes(long long n_baselines, int n_pixels, int n_images) {
@@ -420,6 +471,18 @@ size_t sorted_workspace_bytes(long long n_baselines, int n_pixels, int n_images)
 
 int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaStream_t s) {
     if (p.img_count <= 0 || p.n_baselines <= 0) return BGI_OK;
+    {  // the huge-segment kernel's shared memory is above the default 48 KB
+        const int st = check_cuda(cudaFuncSetAttribute(long_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)long_smem_bytes(kHugeSort)),
+                                  "gridding_sorted: shared memory of the huge-segment kernel");
+        if (st) return st;
+    }
+    int dev = 0, n_sm = 0;
+    {
+        int st = check_cuda(cudaGetDevice(&dev), "gridding_sorted: device");
+        if (!st) st = check_cuda(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "gridding_sorted: SMs");
+        if (st) return st;
+    }
     const int n = p.n_pixels;
     const size_t per = per_image_bytes(p.n_baselines, n);
     const int chunk = (int)std::min<size_t>((size_t)p.img_count, ws_bytes / per);
@@ -437,6 +500,8 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
         st = check_cuda(cudaMemsetAsync(w.cursor, 0, cell_bytes, s), "gridding_sorted: clear cursors");
         if (st) return st;
         st = check_cuda(cudaMemsetAsync(w.n_long, 0, sizeof(unsigned) * cnt, s), "gridding_sorted: clear long list");
+        if (st) return st;
+        st = check_cuda(cudaMemsetAsync(w.n_huge, 0, sizeof(unsigned) * cnt, s), "gridding_sorted: clear huge list");
         if (st) return st;
         for (int done = 0; done < cnt; done += 65535) {
             const int k = std::min(65535, cnt - done);
@@ -474,11 +539,17 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
             place_kernel<<<dim3(bx_p, k), kThreads, 0, s>>>(wd, n_points, n);
             if ((st = check_launch("gridding_sorted place"))) return st;
             wd.n_long += done;
+            wd.n_huge += done;
             wd.longs += (size_t)done * long_cap(p.n_baselines);
             reduce_kernel<<<dim3(bx_c, k), kThreads, 0, s>>>(p, img0 + done, wd, n_points);
             if ((st = check_launch("gridding_sorted reduce"))) return st;
-            long_kernel<<<dim3(kLongBlocks, k), kLongThreads, 0, s>>>(p, img0 + done, wd, n_points);
+            const unsigned long_blocks = (unsigned)std::max(kLongBlocks, (4 * n_sm + k - 1) / k);
+            long_kernel<false><<<dim3(long_blocks, k), kLongThreads, long_smem_bytes(kLongSort), s>>>(p, img0 + done, wd,
+                                                                                                   n_points);
             if ((st = check_launch("gridding_sorted long segments"))) return st;
+            long_kernel<true><<<dim3(kHugeBlocks, k), kLongThreads, long_smem_bytes(kHugeSort), s>>>(p, img0 + done, wd,
+                                                                                                  n_points);
+            if ((st = check_launch("gridding_sorted huge segments"))) return st;
         }
     }
     return BGI_OK;

@@ -101,6 +101,32 @@ def test_sorted_crowded_cells(im):
     _assert_bit_identical(g, g_ref)
 
 
+def test_sorted_long_segments_both_paths(im):
+    """Segments longer than the shared-memory sort holds (8,192 points: about 19,500 points on
+    the centre cell, ordered by counting ranks) beside segments of about 1,400 points (sorted in
+    shared memory) and short ones: the same bits as the loop, counters exact."""
+    n_ant, n = 180, 64
+    nb = n_ant * (n_ant + 1) // 2
+    rng = np.random.default_rng(11)
+    u = rng.uniform(-1.4, 1.4, nb).astype(np.float32)
+    v = rng.uniform(-1.4, 1.4, nb).astype(np.float32)
+    centre = rng.random(nb) < 0.6
+    u[centre] = 0.0
+    v[centre] = 0.0
+    far = rng.choice(nb, 40, replace=False)
+    u[far] = rng.uniform(-25, 25, 40).astype(np.float32)
+    v[far] = rng.uniform(-25, 25, 40).astype(np.float32)
+    flags = np.zeros(nb, np.int32)
+    flags[::131] = 1
+    freqs = np.array([299792458.0, 150e6])
+    vis = (rng.standard_normal((1, 2, nb, 4, 2)) * 10).astype(np.float32)
+    g_ref, c_ref, _ = O.gridding(vis, u, v, flags, freqs, 1.0, 1.0, n, -1000.0, "XX")
+    assert c_ref.max() > 8192 and np.sort(c_ref.reshape(-1))[-2] > 1000
+    g, c = _grid_sorted(im, vis, u, v, flags, freqs, 1.0, 1.0, n, -1000.0, "XX", 1)
+    assert np.array_equal(c, c_ref)
+    _assert_bit_identical(g, g_ref)
+
+
 def test_sorted_reference_golden_bits(im):
     """The reference's own CPU grids (golden vectors from its gridding loop) come out bit for
     bit from the reference's corrected visibilities."""
