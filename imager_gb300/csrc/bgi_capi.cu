@@ -136,8 +136,9 @@ struct bgi_imager {
         return up < cfg.n_pixels - 1 && vp < cfg.n_pixels - 1;
     }
     // Whether bgi_image grids the half plane (images 16-byte aligned): the exactness condition
-    // above, and neither the ordered gridder nor a convolution kernel (both full plane).
-    bool half_plane_path() const { return half_plane() && !deterministic && kb_size == 0; }
+    // above, and no convolution kernel (full plane).  The ordered gridder sums the half plane's
+    // cells as it sums the full plane's.
+    bool half_plane_path() const { return half_plane() && kb_size == 0; }
     // Bound on the pixel coordinates |u|, |v| of every gridded point (bgi_uv_extent), for
     // pruning the half-plane FFT passes.
     void half_plane_extent(int *eu, int *ev) const {

@@ -56,21 +56,26 @@ constexpr unsigned kHugeSort = 32768;
 constexpr int kScanTile = 4096;
 constexpr int kScanPer = kScanTile / kThreads;
 
-__host__ __device__ inline size_t scan_tiles(int n) { return ((size_t)n * n + kScanTile - 1) / kScanTile; }
-__device__ __forceinline__ unsigned seg_start(const SortedWs &w, int local, int n, size_t c) {
-    return w.tile_off[(size_t)local * scan_tiles(n) + c / kScanTile] + w.start[(size_t)local * n * n + c];
+// Cells of one image's grid: N x N, or N x W on the half plane (half_width W > 0).
+__host__ __device__ inline size_t grid_cells(const GridParams &p) {
+    return (size_t)p.n_pixels * (p.half_width > 0 ? (size_t)p.half_width : (size_t)p.n_pixels);
+}
+__host__ __device__ inline size_t scan_tiles(size_t cells) { return (cells + kScanTile - 1) / kScanTile; }
+__device__ __forceinline__ unsigned seg_start(const SortedWs &w, int local, size_t cells, size_t c) {
+    return w.tile_off[(size_t)local * scan_tiles(cells) + c / kScanTile] + w.start[(size_t)local * cells + c];
 }
 
 __host__ __device__ inline size_t long_cap(long long nb) { return (size_t)(2 * nb) / (kShortSeg + 1) + 1; }
 
-size_t per_image_bytes(long long nb, int n) {
-    const size_t pts = 2 * (size_t)nb, cells = (size_t)n * n;
+// Workspace per image for grids of `cells` cells (the full plane's N * N bounds either plane).
+size_t per_image_bytes(long long nb, size_t cells) {
+    const size_t pts = 2 * (size_t)nb;
     return pts * (sizeof(unsigned) + sizeof(float2) + sizeof(unsigned)) + 3 * cells * sizeof(unsigned) +
-           (2 + long_cap(nb) + scan_tiles(n)) * sizeof(unsigned) + 10 * 256;  // 10 arrays, each start rounded up to 256 B
+           (2 + long_cap(nb) + scan_tiles(cells)) * sizeof(unsigned) + 10 * 256;  // 10 arrays, each start rounded up to 256 B
 }
 
-SortedWs carve(void *ws, int chunk, long long nb, int n) {
-    const size_t pts = 2 * (size_t)nb * chunk, cells = (size_t)n * n * chunk;
+SortedWs carve(void *ws, int chunk, long long nb, size_t image_cells) {
+    const size_t pts = 2 * (size_t)nb * chunk, cells = image_cells * chunk;
     char *p = static_cast<char *>(ws);
     auto take = [&](size_t bytes) {
         char *q = p;
@@ -84,7 +89,7 @@ SortedWs carve(void *ws, int chunk, long long nb, int n) {
     w.cnt = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
     w.start = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
     w.cursor = reinterpret_cast<unsigned *>(take(cells * sizeof(unsigned)));
-    w.tile_off = reinterpret_cast<unsigned *>(take(chunk * scan_tiles(n) * sizeof(unsigned)));
+    w.tile_off = reinterpret_cast<unsigned *>(take(chunk * scan_tiles(image_cells) * sizeof(unsigned)));
     w.n_long = reinterpret_cast<unsigned *>(take(chunk * sizeof(unsigned)));
     w.n_huge = reinterpret_cast<unsigned *>(take(chunk * sizeof(unsigned)));
     w.longs = reinterpret_cast<unsigned *>(take(chunk * long_cap(nb) * sizeof(unsigned)));
@@ -105,7 +110,10 @@ __device__ __forceinline__ float2 load_selected(const GridParams &p, size_t img,
     return combine_pols<POL>(a, bb);
 }
 
-// keys: grid x = baselines, y = images of the chunk
+// keys: grid x = baselines, y = images of the chunk.  On the half plane (half_width > 0; every
+// point's mirror cell exists, |u|, |v| pixels < N) a visibility's two points keep the cells whose
+// u index is at most N/2, numbered v * W + u: the same points, in the same order, as those
+// cells of the full plane, so their ordered sums are the same bits.
 __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int chunk_first, SortedWs w) {
     __shared__ ChannelConst s_cc;
     const int img = chunk_first + blockIdx.y;
@@ -118,7 +126,7 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
     const bool in_range = b < nb;
     const size_t set = p.n_uvw_sets > 1 ? (size_t)t * nb : 0;
     const int n = p.n_pixels;
-    unsigned k1 = kNoCell, k2 = kNoCell;
+    unsigned k1 = kNoCell, k2 = kNoCell, counted = 0;
     float2 z = make_float2(0.f, 0.f);
     if (in_range && p.flags[b] <= 0) {
         switch (p.pol) {
@@ -138,8 +146,19 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
         if (!isnan(z.x) && !isnan(z.y) && fabsf(z.x) < kMaxVis && fabsf(z.y) < kMaxVis &&
             uv_pixels(p.u[set + b], p.v[set + b], s_cc.su, s_cc.sv, &s_cc, p.du, p.dv, p.min_uv, p.min_uv >= 0.0, &ui,
                       &vi)) {
-            const long long pos = cell_pos(ui, vi, +1, n), pos2 = cell_pos(ui, vi, -1, n);
-            unsigned *cnt = w.cnt + (size_t)local * n * n;
+            long long pos, pos2;
+            if (p.half_width > 0) {
+                const int u1 = ui + (n & (ui >> 31)), v1 = vi + (n & (vi >> 31));
+                const int u2 = -ui + (n & (-ui >> 31)), v2 = -vi + (n & (-vi >> 31));
+                pos = u1 <= n / 2 ? (long long)v1 * p.half_width + u1 : -1;
+                pos2 = u2 <= n / 2 ? (long long)v2 * p.half_width + u2 : -1;
+                counted = 2;  // both points of the full plane
+            } else {
+                pos = cell_pos(ui, vi, +1, n);
+                pos2 = cell_pos(ui, vi, -1, n);
+                counted = (pos >= 0) + (pos2 >= 0);
+            }
+            unsigned *cnt = w.cnt + (size_t)local * grid_cells(p);
             if (pos >= 0) {
                 k1 = (unsigned)pos;
                 atomicAdd(cnt + pos, 1u);
@@ -151,7 +170,6 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
         }
     }
     if (p.wsum) {
-        const unsigned counted = (k1 != kNoCell) + (k2 != kNoCell);
         const unsigned total = __reduce_add_sync(0xffffffffu, counted);
         if ((threadIdx.x & 31) == 0 && total)
             atomicAdd(p.wsum + (size_t)(img - p.img_base) * kWsumStride, total);
@@ -168,9 +186,8 @@ __global__ void __launch_bounds__(kThreads) keys_kernel(const GridParams p, int 
 // written as 16-byte vectors when the image's cell count is a multiple of 4).  Writes each
 // cell's exclusive prefix within its tile and the tile's total.
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads) scan_tiles_kernel(SortedWs w, int n) {
+__global__ void __launch_bounds__(kThreads) scan_tiles_kernel(SortedWs w, size_t cells) {
     __shared__ unsigned s_warp[kThreads / 32];
-    const size_t cells = (size_t)n * n;
     const int local = blockIdx.y;
     const size_t c0 = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPer;
     const unsigned *cnt = w.cnt + (size_t)local * cells;
@@ -229,14 +246,14 @@ __global__ void __launch_bounds__(kThreads) scan_tiles_kernel(SortedWs w, int n)
         for (int j = 0; j < kScanPer; ++j)
             if (c0 + j < cells) start[c0 + j] = out[j];
     }
-    if (threadIdx.x == kThreads - 1) w.tile_off[(size_t)local * scan_tiles(n) + blockIdx.x] = run;
+    if (threadIdx.x == kThreads - 1) w.tile_off[(size_t)local * scan_tiles(cells) + blockIdx.x] = run;
 }
 
 // scan, second level: one block per image turns its tile totals into exclusive offsets (each
 // thread owns a contiguous run of tiles).
-__global__ void __launch_bounds__(1024) scan_offsets_kernel(SortedWs w, int n) {
+__global__ void __launch_bounds__(1024) scan_offsets_kernel(SortedWs w, size_t cells) {
     __shared__ unsigned s_part[1024];
-    const size_t tiles = scan_tiles(n);
+    const size_t tiles = scan_tiles(cells);
     unsigned *off = w.tile_off + (size_t)blockIdx.x * tiles;
     const size_t per = (tiles + blockDim.x - 1) / blockDim.x;
     const size_t t0 = threadIdx.x * per, t1 = t0 + per < tiles ? t0 + per : tiles;
@@ -259,16 +276,16 @@ __global__ void __launch_bounds__(1024) scan_offsets_kernel(SortedWs w, int n) {
 }
 
 // place: one thread per point
-__global__ void __launch_bounds__(kThreads) place_kernel(SortedWs w, long long n_points, int n) {
+__global__ void __launch_bounds__(kThreads) place_kernel(SortedWs w, long long n_points, size_t cells) {
     const long long q = (long long)blockIdx.x * kThreads + threadIdx.x;
     const int local = blockIdx.y;
     if (q >= n_points) return;
     const size_t base = (size_t)local * n_points;
     const unsigned key = w.key[base + q];
     if (key == kNoCell) return;
-    const size_t cbase = (size_t)local * n * n;
+    const size_t cbase = (size_t)local * cells;
     const unsigned slot = atomicAdd(w.cursor + cbase + key, 1u);
-    w.seg[base + seg_start(w, local, n, key) + slot] = (unsigned)q;
+    w.seg[base + seg_start(w, local, cells, key) + slot] = (unsigned)q;
 }
 
 // Orders a segment of at most K point indices in registers (adjacent compare-exchanges of an
@@ -306,8 +323,7 @@ __device__ __forceinline__ void sum_segment_in_registers(const unsigned *seg, un
 // current value.
 __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, int chunk_first, SortedWs w,
                                                           long long n_points) {
-    const int n = p.n_pixels;
-    const long long cells = (long long)n * n;
+    const long long cells = (long long)grid_cells(p);
     const long long c = (long long)blockIdx.x * kThreads + threadIdx.x;
     const int local = blockIdx.y;
     if (c >= cells) return;
@@ -325,7 +341,7 @@ __global__ void __launch_bounds__(kThreads) reduce_kernel(const GridParams p, in
     const int img = chunk_first + local;
     float2 *cell = p.grids + (size_t)(img - p.img_base) * cells + c;
     float2 acc = p.grids_zero ? make_float2(0.f, 0.f) : *cell;
-    unsigned *seg = w.seg + (size_t)local * n_points + seg_start(w, local, n, c);
+    unsigned *seg = w.seg + (size_t)local * n_points + seg_start(w, local, (size_t)cells, c);
     const float2 *val = w.val + (size_t)local * n_points;
     if (len == 1) {
         const float2 v = val[seg[0]];
@@ -398,8 +414,7 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, 
     extern __shared__ __align__(16) unsigned s_dyn[];
     unsigned *s_idx = s_dyn;
     float2 *s_val = reinterpret_cast<float2 *>(s_dyn + CAP);
-    const int n = p.n_pixels;
-    const size_t cells = (size_t)n * n;
+    const size_t cells = grid_cells(p);
     const int local = blockIdx.y;
     const int img = chunk_first + local;
     const size_t cap = long_cap(n_points / 2);
@@ -408,7 +423,7 @@ __global__ void __launch_bounds__(kLongThreads) long_kernel(const GridParams p, 
         const unsigned c = w.longs[(size_t)local * cap + (HUGE ? cap - 1 - li : li)];
         const size_t cbase = (size_t)local * cells;
         const unsigned len = w.cnt[cbase + c];
-        const unsigned st = seg_start(w, local, n, c);
+        const unsigned st = seg_start(w, local, cells, c);
         const unsigned *seg = w.seg + (size_t)local * n_points + st;
         unsigned *ordered = w.key + (size_t)local * n_points + st;
         const bool in_shared = len <= CAP;
@@ -466,7 +481,7 @@ constexpr size_t long_smem_bytes(unsigned cap) { return cap * sizeof(unsigned) +
 }  // namespace
 
 size_t sorted_workspace_bytes(long long n_baselines, int n_pixels, int n_images) {
-    return per_image_bytes(n_baselines, n_pixels) * (size_t)std::max(1, n_images);
+    return per_image_bytes(n_baselines, (size_t)n_pixels * n_pixels) * (size_t)std::max(1, n_images);
 }
 
 int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaStream_t s) {
@@ -483,18 +498,18 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
         if (!st) st = check_cuda(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "gridding_sorted: SMs");
         if (st) return st;
     }
-    const int n = p.n_pixels;
-    const size_t per = per_image_bytes(p.n_baselines, n);
+    const size_t cells = grid_cells(p);
+    const size_t per = per_image_bytes(p.n_baselines, cells);
     const int chunk = (int)std::min<size_t>((size_t)p.img_count, ws_bytes / per);
     if (chunk < 1 || !ws) return set_error(BGI_ERR_INVALID, "gridding_sorted: workspace of %zu bytes is below %zu", ws_bytes, per);
     const long long n_points = 2 * p.n_baselines;
     const unsigned bx_b = (unsigned)((p.n_baselines + kThreads - 1) / kThreads);
     const unsigned bx_p = (unsigned)((n_points + kThreads - 1) / kThreads);
-    const unsigned bx_c = (unsigned)(((long long)n * n + kThreads - 1) / kThreads);
+    const unsigned bx_c = (unsigned)((cells + kThreads - 1) / kThreads);
     for (int img0 = p.img_begin; img0 < p.img_begin + p.img_count; img0 += chunk) {
         const int cnt = std::min(chunk, p.img_begin + p.img_count - img0);
-        SortedWs w = carve(ws, cnt, p.n_baselines, n);
-        const size_t cell_bytes = sizeof(unsigned) * (size_t)n * n * cnt;
+        SortedWs w = carve(ws, cnt, p.n_baselines, cells);
+        const size_t cell_bytes = sizeof(unsigned) * cells * cnt;
         int st = check_cuda(cudaMemsetAsync(w.cnt, 0, cell_bytes, s), "gridding_sorted: clear counts");
         if (st) return st;
         st = check_cuda(cudaMemsetAsync(w.cursor, 0, cell_bytes, s), "gridding_sorted: clear cursors");
@@ -508,23 +523,23 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
             SortedWs wd = w;
             wd.key += (size_t)done * n_points;
             wd.val += (size_t)done * n_points;
-            wd.cnt += (size_t)done * n * n;
+            wd.cnt += (size_t)done * cells;
             keys_kernel<<<dim3(bx_b, k), kThreads, 0, s>>>(p, img0 + done, wd);
             if ((st = check_launch("gridding_sorted keys"))) return st;
         }
         for (int done = 0; done < cnt; done += 65535) {
             const int k = std::min(65535, cnt - done);
             SortedWs wd = w;
-            wd.cnt += (size_t)done * n * n;
-            wd.start += (size_t)done * n * n;
-            wd.tile_off += (size_t)done * scan_tiles(n);
-            if ((size_t)n * n % 4 == 0)
-                scan_tiles_kernel<true><<<dim3((unsigned)scan_tiles(n), k), kThreads, 0, s>>>(wd, n);
+            wd.cnt += (size_t)done * cells;
+            wd.start += (size_t)done * cells;
+            wd.tile_off += (size_t)done * scan_tiles(cells);
+            if (cells % 4 == 0)
+                scan_tiles_kernel<true><<<dim3((unsigned)scan_tiles(cells), k), kThreads, 0, s>>>(wd, cells);
             else
-                scan_tiles_kernel<false><<<dim3((unsigned)scan_tiles(n), k), kThreads, 0, s>>>(wd, n);
+                scan_tiles_kernel<false><<<dim3((unsigned)scan_tiles(cells), k), kThreads, 0, s>>>(wd, cells);
             if ((st = check_launch("gridding_sorted scan tiles"))) return st;
         }
-        scan_offsets_kernel<<<cnt, 1024, 0, s>>>(w, n);
+        scan_offsets_kernel<<<cnt, 1024, 0, s>>>(w, cells);
         if ((st = check_launch("gridding_sorted scan offsets"))) return st;
         for (int done = 0; done < cnt; done += 65535) {
             const int k = std::min(65535, cnt - done);
@@ -532,11 +547,11 @@ int launch_gridding_sorted(const GridParams &p, void *ws, size_t ws_bytes, cudaS
             wd.key += (size_t)done * n_points;
             wd.val += (size_t)done * n_points;
             wd.seg += (size_t)done * n_points;
-            wd.cnt += (size_t)done * n * n;
-            wd.start += (size_t)done * n * n;
-            wd.cursor += (size_t)done * n * n;
-            wd.tile_off += (size_t)done * scan_tiles(n);
-            place_kernel<<<dim3(bx_p, k), kThreads, 0, s>>>(wd, n_points, n);
+            wd.cnt += (size_t)done * cells;
+            wd.start += (size_t)done * cells;
+            wd.cursor += (size_t)done * cells;
+            wd.tile_off += (size_t)done * scan_tiles(cells);
+            place_kernel<<<dim3(bx_p, k), kThreads, 0, s>>>(wd, n_points, cells);
             if ((st = check_launch("gridding_sorted place"))) return st;
             wd.n_long += done;
             wd.n_huge += done;

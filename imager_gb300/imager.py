@@ -416,7 +416,8 @@ class Imager:
         return {v: k for k, v in capi.FFT_MODE.items()}[m.value]
 
     def set_deterministic(self, enable: bool = True):
-        """Grid by sort and ordered per-cell sums (full plane): the same image bits on every run."""
+        """Grid by sort and ordered per-cell sums (the half plane when the handle takes it): the
+        same image bits on every run."""
         call("bgi_set_deterministic", self._h, int(bool(enable)))
 
     def image_wcs(self, ra_deg: float = 0.0, dec_deg: float = -26.703319) -> dict:

@@ -230,8 +230,8 @@ BGI_API int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float
 BGI_API int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz);
 
 /* 1 when bgi_image would take the half-plane path for the current array, frequencies and
- * configuration (16-byte aligned complex images; not with bgi_set_deterministic, a convolution
- * kernel or BGI_WEIGHT_UNIFORM, which grid the full plane), 0 when it would transform the full plane;
+ * configuration (16-byte aligned complex images; not with a convolution kernel or
+ * BGI_WEIGHT_UNIFORM, which grid the full plane), 0 when it would transform the full plane;
  * negative status on error. */
 BGI_API int bgi_half_plane(const bgi_imager *im);
 
@@ -473,7 +473,8 @@ BGI_API int bgi_batch_destroy(bgi_batch *batch);
 BGI_API int bgi_set_gridding_kernel(bgi_imager *im, int kernel_size, int with_sinc);
 
 /* Deterministic mode (default off): bgi_image and bgi_image_host grid with the ordered
- * per-cell sums of bgi_gridding_sorted_gpu on the full plane, so every image is the same bits
+ * per-cell sums of bgi_gridding_sorted_gpu (on the half plane when the handle takes it: its
+ * cells hold the same sums as those cells of the full plane), so every image is the same bits
  * on every run and whatever else shares the call.  No reference counterpart. */
 BGI_API int bgi_set_deterministic(bgi_imager *im, int enable);
 
