@@ -410,6 +410,7 @@ def host_link_rates(host_out, h2d_bytes, reps=3):
     from a device buffer of its size (device to host) and h2d_bytes from pinned memory (host to
     device), each timed with CUDA events on the current stream, best of `reps`.  The end-to-end
     step cannot beat max(d2h / d2h_gbs, h2d / h2d_gbs), the two directions running at once."""
+    import torch
     s = torch.cuda.current_stream()
     dev = torch.empty(host_out.numel(), dtype=host_out.dtype, device="cuda")
     src_h = torch.empty(max(h2d_bytes // 4, 1), dtype=torch.float32).pin_memory()
@@ -460,6 +461,7 @@ def batched_measure(args, stream, flush):
         schedules.append(h.autotune(d, sc, "s16", flags=flags, out=out)[:2])
         items.append(dict(imager=h, data=d, scales=sc, fmt="s16", flags=flags, out=out))
     n_images = sum(o.n_intervals * o.n_channels for o in bands)
+    aggs = {f"{o.n_pixels}": it["imager"].gridding_aggregation for o, it in zip(bands, items)}  # autotuned
     k = max(3, min(args.steps, 10))
 
     def direct():
@@ -467,6 +469,11 @@ def batched_measure(args, stream, flush):
             it["imager"].image_compressed(it["data"], it["scales"], "s16", flags=flags, out=it["out"])
 
     ms_direct = time_steps(direct, k, stream, flush)
+    ms_band = {}
+    for o, it in zip(bands, items):
+        ms_band[f"{o.n_pixels}"] = time_steps(
+            lambda it=it: it["imager"].image_compressed(it["data"], it["scales"], "s16", flags=flags, out=it["out"]),
+            k, stream, flush)
     batch = IM.Batch(items)
     ms_graph = time_steps(batch.launch, k, stream, flush)
     torch.cuda.synchronize()
@@ -494,7 +501,9 @@ def batched_measure(args, stream, flush):
             "images_per_step": n_images, "steps": k,
             "schedules": {f"{o.n_pixels}": {"images_per_wave": w or "auto", "lanes": l}
                           for o, (w, l) in zip(bands, schedules)},
-            "direct_calls": {"ms_per_step": ms_direct, "images_per_s": n_images / (ms_direct / 1000.0)},
+            "direct_calls": {"ms_per_step": ms_direct, "images_per_s": n_images / (ms_direct / 1000.0),
+                             "ms_per_band": ms_band},
+            "gridding_aggregation": aggs,
             "cuda_graph": {"ms_per_step": ms_graph, "images_per_s": n_images / (ms_graph / 1000.0)},
             "cuda_graph_deterministic": {"ms_per_step": ms_det, "images_per_s": n_images / (ms_det / 1000.0)},
             "errors_vs_fp64_rel_l2": {f"{o.n_pixels}": e for o, e in zip(bands, errs)}}
