@@ -30,6 +30,7 @@ public:
     size_t n_baselines() const { return size_t(obsInfo.nAntennas) * (obsInfo.nAntennas + 1) / 2; }
     unsigned int integration_intervals() const { return nIntervals; }
     std::complex<float> *data() { return buf.data(); }
+    const std::complex<float> *data() const { return buf.data(); }
     std::complex<float> *at(size_t t, size_t ch, size_t baseline) {
         return buf.data() + ((t * nFrequencies + ch) * n_baselines() + baseline) * 4;
     }
