@@ -173,8 +173,8 @@ struct bgi_imager {
     bool cnt_dirty[kLanes] = {};
     cudaStream_t lane[kLanes] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[kLanes] = {};
-    // Deterministic mode: gridding by sort and ordered per-cell sums (full plane), with a
-    // workspace per lane for one wave.
+    // Deterministic mode: gridding by sort and ordered per-cell sums (the half plane when the
+    // handle takes it), with a workspace per lane for one wave.
     bool deterministic = false;
     DevBuf<unsigned char> sorted_ws[kLanes];
     DevBuf<unsigned int> wsum;    // per-image weight counts of the last call
@@ -185,6 +185,35 @@ struct bgi_imager {
 
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     std::vector<cudaEvent_t> ev_in, ev_done;  // per chunk of bgi_image_host
+
+    // Replay of repeated calls.  The second of two consecutive calls with the same arguments
+    // on an unchanged handle is also captured into a CUDA graph (on cap_stream: recorded, not
+    // run); while the calls keep repeating, each one is that graph launched on the caller's
+    // stream, one launch in place of the ~100-200 stream operations of the waves and copies.
+    // Any other call, and every call that changes the handle's state, drops the graph.
+    struct CallKey {
+        int kind = -1, format = 0, n_intervals = 0;
+        unsigned flags = 0;
+        const void *in[5] = {};
+        const void *out = nullptr;
+        bool operator==(const CallKey &o) const {
+            if (kind != o.kind || format != o.format || n_intervals != o.n_intervals || flags != o.flags || out != o.out)
+                return false;
+            for (int i = 0; i < 5; ++i)
+                if (in[i] != o.in[i]) return false;
+            return true;
+        }
+    };
+    CallKey last_key, graph_key;
+    bool have_last = false, replay_refused = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+        have_last = false;
+        replay_refused = false;
+    }
 
     int ensure_copy_streams() {
         if (copy_in) return BGI_OK;
@@ -438,6 +467,8 @@ int bgi_create(const bgi_config *cfg, bgi_imager **out) {
 int bgi_destroy(bgi_imager *im) {
     if (!im) return BGI_OK;
     im->activate();
+    im->drop_graph();
+    if (im->cap_stream) cudaStreamDestroy(im->cap_stream);
     im->release_array();
     dev_free(im->d_freqs);
     for (cudaEvent_t e : im->ev_pool) cudaEventDestroy(e);
@@ -466,6 +497,7 @@ int bgi_destroy(bgi_imager *im) {
 
 int bgi_set_array(bgi_imager *im, int n_ant, int n_uvw_sets, const float *u, const float *v,
                   const float *w, const int *baseline_flags, const double *cable_lengths) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im || !u || !v || !baseline_flags || n_ant < 1 || n_uvw_sets < 1)
         return set_error(BGI_ERR_INVALID, "set_array: bad arguments");
     BGI_TRY(im->activate());
@@ -541,6 +573,7 @@ int bgi_pointed_uvw_gpu(const double *xyz, int n_ant, const bgi_uvw_step *steps,
 
 int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_host, int n_steps,
                           const bgi_uvw_step *steps_host, const int *baseline_flags, const double *cable_lengths) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im || !xyz_host || !steps_host || !baseline_flags || n_ant < 1 || n_ant > 46340 || n_steps < 1)
         return set_error(BGI_ERR_INVALID, "set_array_pointed: bad arguments");
     BGI_TRY(im->activate());
@@ -590,6 +623,7 @@ int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_host, int
 }
 
 int bgi_set_frequencies(bgi_imager *im, int n_channels, const double *freqs_hz) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im || !freqs_hz || n_channels < 1) return set_error(BGI_ERR_INVALID, "set_frequencies: bad arguments");
     for (int c = 0; c < n_channels; ++c)
         if (!(freqs_hz[c] > 0.0) || !std::isfinite(freqs_hz[c]))
@@ -613,6 +647,7 @@ int bgi_half_plane(const bgi_imager *im) {
 }
 
 int bgi_set_uv_cell(bgi_imager *im, double delta_u, double delta_v) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im) return set_error(BGI_ERR_INVALID, "set_uv_cell: null handle");
     if (im->n_ant == 0) return set_error(BGI_ERR_STATE, "set_uv_cell: array not set");
     if (!(delta_u > 0) || !(delta_v > 0) || !std::isfinite(delta_u) || !std::isfinite(delta_v))
@@ -896,17 +931,54 @@ int image_impl(bgi_imager *im, int format, const void *data, const float *scales
 
 }  // namespace
 
+namespace {
+int image_replayed(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals, unsigned flags,
+                   float *images, void *stream);
+
+// Records enqueue(stream) -- the stream work of one call, whose scratch an earlier run of the
+// same call has sized -- into an executable graph on the handle's capture stream (nothing
+// runs).  On failure *exec is null, the handle's scratch is marked for clearing and the CUDA
+// error state is reset.
+template <class F>
+int record_call(bgi_imager *im, F &&enqueue, cudaGraphExec_t *exec) {
+    *exec = nullptr;
+    int st = BGI_OK;
+    if (!im->cap_stream) st = check_cuda(cudaStreamCreateWithFlags(&im->cap_stream, cudaStreamNonBlocking), "capture stream");
+    cudaGraph_t g = nullptr;
+    if (!st) st = check_cuda(cudaStreamBeginCapture(im->cap_stream, cudaStreamCaptureModeThreadLocal), "image capture");
+    if (!st) {
+        const int issued = enqueue(im->cap_stream);
+        const int ended = check_cuda(cudaStreamEndCapture(im->cap_stream, &g), "image end capture");
+        st = issued ? issued : ended;
+    }
+    if (!st) st = check_cuda(cudaGraphInstantiate(exec, g, 0), "image graph instantiate");
+    if (g) cudaGraphDestroy(g);
+    if (st) {
+        if (*exec) cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+        cudaGetLastError();
+        for (int l = 0; l < bgi_imager::kLanes; ++l) im->grid_dirty[l] = im->cnt_dirty[l] = true;
+    }
+    return st;
+}
+}  // namespace
+
 extern "C" {
 
+int bgi_replay_ready(const bgi_imager *im) {
+    if (!im) return set_error(BGI_ERR_INVALID, "replay_ready: null handle");
+    return im->graph_exec != nullptr ? 1 : 0;
+}
+
 int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images, void *stream) {
-    return image_impl(im, BGI_VIS_C64, vis, nullptr, n_intervals, flags, images, stream);
+    return image_replayed(im, BGI_VIS_C64, vis, nullptr, n_intervals, flags, images, stream);
 }
 
 int bgi_image_compressed(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals,
                          unsigned flags, float *images, void *stream) {
     if (format != BGI_VIS_S16 && format != BGI_VIS_BF16 && format != BGI_VIS_FP16)
         return set_error(BGI_ERR_INVALID, "image_compressed: bad format %d", format);
-    return image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+    return image_replayed(im, format, data, scales, n_intervals, flags, images, stream);
 }
 
 }  // extern "C"
@@ -945,6 +1017,8 @@ int bgi_batch_create(const bgi_batch_item *items, int n_items, void *stream, bgi
             return set_error(BGI_ERR_INVALID, "batch_create: items on different devices");
         if (items[i].imager->timing) return set_error(BGI_ERR_STATE, "batch_create: stage timing is on (item %d)", i);
     }
+    // the items' warm-up run may grow an imager's scratch: no replay of its earlier calls
+    for (int i = 0; i < n_items; ++i) items[i].imager->drop_graph();
     BGI_TRY(items[0].imager->activate());
     // the items run and are captured on a stream of our own (the legacy default stream cannot
     // be captured), ordered after the caller's stream
@@ -998,6 +1072,7 @@ int bgi_batch_destroy(bgi_batch *b) {
 }
 
 int bgi_set_fft_mode(bgi_imager *im, int mode) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im) return set_error(BGI_ERR_INVALID, "set_fft_mode: null handle");
     if (mode != BGI_FFT_SIMT && mode != BGI_FFT_TENSOR_SPLIT16)
         return set_error(BGI_ERR_INVALID, "set_fft_mode: bad mode %d", mode);
@@ -1015,6 +1090,7 @@ int bgi_get_fft_mode(const bgi_imager *im, int *mode) {
 }
 
 int bgi_set_schedule(bgi_imager *im, int images_per_wave, int lanes) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im || images_per_wave < 0 || lanes < 1 || lanes > bgi_imager::kLanes)
         return set_error(BGI_ERR_INVALID, "set_schedule: wave >= 0 (0 = auto) and 1 <= lanes <= %d", bgi_imager::kLanes);
     im->cfg.max_images_per_wave = images_per_wave;
@@ -1031,6 +1107,7 @@ int bgi_get_schedule(const bgi_imager *im, int *images_per_wave, int *lanes) {
 
 int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals, unsigned flags,
                  float *images, void *stream, double *best_ms) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     BGI_TRY(image_checks(im, n_intervals, flags));
     if (format < BGI_VIS_C64 || format > BGI_VIS_FP16) return set_error(BGI_ERR_INVALID, "autotune: bad format %d", format);
     BGI_TRY(im->activate());
@@ -1042,14 +1119,24 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
     BGI_TRY(check_cuda(cudaEventCreate(&e0), "autotune event"));
     int st = check_cuda(cudaEventCreate(&e1), "autotune event");
     // milliseconds per call of the handle's current schedule: one call to size the scratch, then
-    // three timed with CUDA events on the stream
+    // three timed with CUDA events on the stream -- as launches of the call's recorded graph, the
+    // form repeated calls take (issued directly where recording fails)
     auto time_current = [&](float *ms, int reps = 3) {
-        int r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+        auto enqueue = [&](cudaStream_t st) {
+            return image_impl(im, format, data, scales, n_intervals, flags, images, st);
+        };
+        int r = enqueue(s);
+        cudaGraphExec_t ex = nullptr;
+        if (!r) record_call(im, enqueue, &ex);
         if (!r) r = check_cuda(cudaEventRecord(e0, s), "autotune record");
         for (int rep = 0; !r && rep < reps; ++rep)
-            r = image_impl(im, format, data, scales, n_intervals, flags, images, stream);
+            r = ex ? check_cuda(cudaGraphLaunch(ex, s), "autotune graph launch") : enqueue(s);
         if (!r) r = check_cuda(cudaEventRecord(e1, s), "autotune record");
         if (!r) r = check_cuda(cudaEventSynchronize(e1), "autotune sync");
+        if (ex) {
+            if (r) cudaStreamSynchronize(s);  // no launch of it still in flight
+            cudaGraphExecDestroy(ex);
+        }
         float t = 0.f;
         if (!r) r = check_cuda(cudaEventElapsedTime(&t, e0, e1), "autotune elapsed");
         *ms = t / (float)reps;
@@ -1173,6 +1260,7 @@ int bgi_autotune(bgi_imager *im, int format, const void *data, const float *scal
 }
 
 int bgi_set_column_radix(bgi_imager *im, int radix) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im) return set_error(BGI_ERR_INVALID, "set_column_radix: null handle");
     const int n = im->cfg.n_pixels;
     if (radix != 0 && radix != col_default_radix(n) && radix != col_alt_radix(n))
@@ -1189,6 +1277,7 @@ int bgi_get_column_radix(const bgi_imager *im, int *radix) {
 }
 
 int bgi_set_gridding_images_per_thread(bgi_imager *im, int images_per_thread) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im || (images_per_thread != 0 && images_per_thread != 2 && images_per_thread != 4 && images_per_thread != 8))
         return set_error(BGI_ERR_INVALID, "set_gridding_images_per_thread: 0 (auto), 2, 4 or 8");
     im->grid_cpt = images_per_thread;
@@ -1202,6 +1291,7 @@ int bgi_get_gridding_images_per_thread(const bgi_imager *im, int *images_per_thr
 }
 
 int bgi_set_gridding_aggregation(bgi_imager *im, int on) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im || (on != 0 && on != 1)) return set_error(BGI_ERR_INVALID, "set_gridding_aggregation: 0 or 1");
     im->grid_agg = on;
     return BGI_OK;
@@ -1273,15 +1363,8 @@ int planes_for(int pol, int out[2]) {
 // mats (optional): host correlation matrices re_xx, im_xx, re_yy, im_yy [T][C][A][A] in place of
 // stored visibilities: each chunk's matrices are uploaded and converted on the device
 // (launch_ingest, on the upload stream) into the staged visibilities in `format`.
-int image_host_impl(bgi_imager *im, int format, const void *vis_host, const float *scales_host, int n_intervals,
-                    unsigned flags, float *images_host, void *stream, const float *const *mats = nullptr) {
-    TraceRange trace("bgi_image_host");
-    BGI_TRY(image_checks(im, n_intervals, flags));
-    if (!images_host || (!mats && (!vis_host || (format != BGI_VIS_C64 && !scales_host))) ||
-        (mats && (!mats[0] || !mats[1])))
-        return set_error(BGI_ERR_INVALID, "image_host: null buffer");
-    BGI_TRY(im->activate());
-    cudaStream_t s = as_stream(stream);
+int image_host_enqueue(bgi_imager *im, int format, const void *vis_host, const float *scales_host, int n_intervals,
+                       unsigned flags, float *images_host, cudaStream_t s, const float *const *mats) {
     const int n_images = n_intervals * im->n_channels;
     const long long nb = im->n_baselines, nblk = vis_blocks(nb);
     const bool planar = format != BGI_VIS_C64;
@@ -1366,7 +1449,104 @@ int image_host_impl(bgi_imager *im, int format, const void *vis_host, const floa
     }
     BGI_TRY(check_cuda(cudaEventRecord(im->ev_join[0], im->copy_out), "join record"));
     BGI_TRY(check_cuda(cudaStreamWaitEvent(s, im->ev_join[0], 0), "join wait"));
-    im->last_images = n_images;
+    return BGI_OK;
+}
+
+// Whether a host pointer is page-locked (registered with CUDA): copies from pageable memory
+// cannot be captured into a graph.
+bool pinned(const void *p) {
+    if (!p) return true;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Runs enqueue(s) -- the stream work of one imaging call -- or, when the same call on the same
+// handle state was the last one and has been captured, launches its graph on s.  The second of
+// two identical calls in a row is run and then also captured (on the handle's capture stream,
+// recorded and not run) for the calls that repeat it.  No replay under stage timing, inside a
+// caller's stream capture, or where a capture failed for this call.
+template <class F>
+int run_replayed(bgi_imager *im, const bgi_imager::CallKey &key, bool capturable, cudaStream_t s, F &&enqueue) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    BGI_TRY(check_cuda(cudaStreamIsCapturing(s, &cs), "capture status"));
+    const bool replay = capturable && !im->timing && cs == cudaStreamCaptureStatusNone;
+    const bool same = im->have_last && im->last_key == key;
+    if (replay && same && im->graph_exec && im->graph_key == key) {
+        const int st = check_cuda(cudaGraphLaunch(im->graph_exec, s), "image graph launch");
+        if (st) {
+            im->drop_graph();
+            for (int l = 0; l < bgi_imager::kLanes; ++l) im->grid_dirty[l] = im->cnt_dirty[l] = true;
+        }
+        return st;
+    }
+    if (im->graph_exec) {
+        cudaGraphExecDestroy(im->graph_exec);
+        im->graph_exec = nullptr;
+    }
+    if (!same) im->replay_refused = false;
+    im->last_key = key;
+    im->have_last = false;  // set again once this call's work is issued
+    BGI_TRY(enqueue(s));
+    im->have_last = true;
+    if (!replay || !same || im->replay_refused) return BGI_OK;
+    // the same call twice in a row: record it for the calls that repeat it
+    if (record_call(im, enqueue, &im->graph_exec) != BGI_OK) {
+        im->replay_refused = true;  // the call itself has run: keep its result, replay nothing for it
+        return BGI_OK;
+    }
+    im->graph_key = key;
+    return BGI_OK;
+}
+
+// bgi_image / bgi_image_compressed: image_impl, replayed as a graph while the call repeats.
+int image_replayed(bgi_imager *im, int format, const void *data, const float *scales, int n_intervals, unsigned flags,
+                   float *images, void *stream) {
+    if (!im) return set_error(BGI_ERR_INVALID, "image: null handle");
+    BGI_TRY(im->activate());
+    bgi_imager::CallKey key;
+    key.kind = 0;
+    key.format = format;
+    key.n_intervals = n_intervals;
+    key.flags = flags;
+    key.out = images;
+    key.in[0] = data;
+    key.in[1] = scales;
+    return run_replayed(im, key, true, as_stream(stream), [&](cudaStream_t st) {
+        return image_impl(im, format, data, scales, n_intervals, flags, images, st);
+    });
+}
+
+int image_host_impl(bgi_imager *im, int format, const void *vis_host, const float *scales_host, int n_intervals,
+                    unsigned flags, float *images_host, void *stream, const float *const *mats = nullptr) {
+    TraceRange trace("bgi_image_host");
+    BGI_TRY(image_checks(im, n_intervals, flags));
+    if (!images_host || (!mats && (!vis_host || (format != BGI_VIS_C64 && !scales_host))) ||
+        (mats && (!mats[0] || !mats[1])))
+        return set_error(BGI_ERR_INVALID, "image_host: null buffer");
+    BGI_TRY(im->activate());
+    cudaStream_t s = as_stream(stream);
+    bgi_imager::CallKey key;
+    key.kind = mats ? 2 : 1;
+    key.format = format;
+    key.n_intervals = n_intervals;
+    key.flags = flags;
+    key.out = images_host;
+    key.in[0] = vis_host;
+    key.in[1] = scales_host;
+    bool capturable = pinned(images_host) && pinned(vis_host) && pinned(scales_host);
+    for (int q = 0; mats && q < 4; ++q) {
+        key.in[1 + q] = mats[q];
+        capturable = capturable && pinned(mats[q]);
+    }
+    if (mats) key.in[0] = nullptr;
+    BGI_TRY(run_replayed(im, key, capturable, s, [&](cudaStream_t st) {
+        return image_host_enqueue(im, format, vis_host, scales_host, n_intervals, flags, images_host, st, mats);
+    }));
+    im->last_images = n_intervals * im->n_channels;
     BGI_TRY(check_cuda(cudaStreamSynchronize(s), "image_host sync"));
     unsigned int fault = 0;
     BGI_TRY(read_device_fault(&fault, false));
@@ -1430,6 +1610,7 @@ int bgi_selftest_wait_timeout(int device, void *stream) {
 }
 
 int bgi_set_gridding_kernel(bgi_imager *im, int kernel_size, int with_sinc) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im) return set_error(BGI_ERR_INVALID, "set_gridding_kernel: null handle");
     if (kernel_size < 0 || kernel_size > kMaxKernel)
         return set_error(BGI_ERR_INVALID, "set_gridding_kernel: kernel size 0..%d", kMaxKernel);
@@ -1462,12 +1643,14 @@ int bgi_gridding_kb_gpu(const float *vis, int n_ant, int n_channels, int n_inter
 }
 
 int bgi_set_deterministic(bgi_imager *im, int enable) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im) return set_error(BGI_ERR_INVALID, "set_deterministic: null handle");
     im->deterministic = enable != 0;
     return BGI_OK;
 }
 
 int bgi_set_stage_timing(bgi_imager *im, int enable) {
+    if (im) im->drop_graph();  // the handle changes: no replay of an earlier call
     if (!im) return set_error(BGI_ERR_INVALID, "set_stage_timing: null handle");
     im->timing = enable != 0;
     im->ev_used = 0;

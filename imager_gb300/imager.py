@@ -382,6 +382,14 @@ class Imager:
         call("bgi_get_gridding_images_per_thread", self._h, C.byref(k))
         return k.value
 
+    @property
+    def replay_ready(self) -> bool:
+        """Whether the next call identical to the last one launches its recorded CUDA graph."""
+        st = capi.lib().bgi_replay_ready(self._h)
+        if st < 0:
+            capi.check(st)
+        return st == 1
+
     def set_gridding_aggregation(self, on: bool = False):
         """Warp-aggregated gridding atomics (half plane, 4 or 8 images per thread): points of a
         warp on the same cell summed before one atomic per cell."""

@@ -283,7 +283,16 @@ BGI_API int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_h
 /* Whole path on device buffers: vis float[T][C][B][4][2] (read only: corrections are applied
  * in registers and not written back), images float[T][C][N][N][2] out.  Each image is
  * normalised by its own weight sum (the CPU path, src/pacer_imager.cpp:171-178) and
- * fftshifted.  Stream-ordered; no host synchronisation. */
+ * fftshifted.  Stream-ordered; no host synchronisation.
+ * Repeated calls: when a call repeats the previous call on the handle exactly (same buffers,
+ * interval count, flags and format, no setter in between), the second such call is also
+ * recorded into a CUDA graph, and the calls after it launch that graph on `stream` instead of
+ * issuing each wave's kernels: the same work and results, one host launch per call.  Not under
+ * stage timing or inside a stream capture of the caller's; the same holds for the host-buffer
+ * calls below when their host buffers are page-locked. */
+/* 1 when the handle holds the recorded graph of its last call (the next identical call
+ * launches it), 0 otherwise; negative status on error. */
+BGI_API int bgi_replay_ready(const bgi_imager *im);
 BGI_API int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
               void *stream);
 
@@ -414,8 +423,8 @@ BGI_API int bgi_get_fft_mode(const bgi_imager *im, int *mode);
  * gridding atomics (bgi_set_gridding_aggregation) and the FFT arithmetic (bgi_set_fft_mode).
  * bgi_autotune times every wave size in {auto, 1, 2, 3, 4, 8, 12, 16, 20, 24, 28, 32, 40, 48,
  * 64} (up to the block's image count) with 1-8 lanes on the caller's own block (one call to size
- * the scratch, three timed with CUDA events on the stream), times the three fastest again over
- * ten calls each, then, at the best of those, 2, 4 and 8 images per gridding thread, 4 and 8
+ * the scratch, then three timed with CUDA events on the stream as launches of the call's
+ * recorded graph, the form repeated calls take), times the three fastest again over ten calls each, then, at the best of those, 2, 4 and 8 images per gridding thread, 4 and 8
  * with aggregated atomics (half plane), the column pass's second radix (bgi_set_column_radix)
  * and (image side 512, half plane) the tensor-core row pass (ten timed calls each);
  * it keeps the fastest on the handle, frees the candidates' scratch and writes the best
