@@ -1,10 +1,10 @@
-"""The reference-side binding that INTEGRATION.md gives (section 1: the C++ a maintainer puts in
-the reference's src/gpu/ in place of gridding_gpu.cpp, corrections_gpu.cpp and gpu_utils.cpp)
-compiles against the reference's own src/gpu headers and include/blink_imager_gb300.h: the
-signatures it defines are the reference's (src/gpu/gridding_gpu.h:12-18,
-src/gpu/corrections_gpu.h:7-9, src/gpu/gpu_utils.h:8-19) and the calls it makes are the ABI's.
-g++ -fsyntax-only, with the host-only stand-ins of oracle/ref_shim for the astroio types.
-Skipped where the reference checkout or g++ is absent."""
+"""The reference-side binding (tests/cpp/reference_binding.cpp: the C++ a maintainer puts in the
+reference's src/gpu/ in place of gridding_gpu.cpp, corrections_gpu.cpp and gpu_utils.cpp; the
+integration guide prints the same code) compiles against the reference's own src/gpu headers
+and include/blink_imager_gb300.h: the signatures it defines are the reference's
+(src/gpu/gridding_gpu.h:12-18, src/gpu/corrections_gpu.h:7-9, src/gpu/gpu_utils.h:8-19) and the
+calls it makes are the ABI's.  g++ -fsyntax-only, with the host-only stand-ins of
+oracle/ref_shim for the astroio types.  Skipped where the reference checkout or g++ is absent."""
 import os
 import re
 import shutil
@@ -16,29 +16,21 @@ from oracle import oracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "cpp", "reference_binding.cpp")
 
 
-def _binding_source() -> str:
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = [b for b in re.findall(r"```cpp\n(.*?)```", text, re.S) if "gb300_bindings.cpp" in b]
-    assert len(blocks) == 1, "INTEGRATION.md has one gb300_bindings.cpp block"
-    return blocks[0]
-
-
-def test_reference_binding_compiles(tmp_path):
-    src = _binding_source()
+def test_reference_binding_compiles():
     gpu_dir = os.path.join(O.REF_SRC, "gpu") if O.REF_SRC else ""
     if not gpu_dir or not os.path.isfile(os.path.join(gpu_dir, "gridding_gpu.h")):
         pytest.skip("no reference checkout (BGI_REFERENCE_SRC)")
     if not shutil.which("g++"):
         pytest.skip("no g++")
-    f = tmp_path / "gb300_bindings.cpp"
-    f.write_text(src)
     cmd = ["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-I", os.path.join(ROOT, "oracle", "ref_shim"), "-I",
-           gpu_dir, "-I", os.path.join(ROOT, "include"), str(f)]
+           gpu_dir, "-I", os.path.join(ROOT, "include"), SRC]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     # every function of the reference's three src/gpu headers that carries GPU work is defined
+    src = open(SRC).read()
     for name in ("apply_geometric_corrections_gpu", "apply_cable_lengths_corrections_gpu", "gridding_gpu",
                  "vector_sum_gpu", "fft_shift_and_norm_gpu", "image_averaging_gpu"):
         assert re.search(rf"\b{name}\s*\(", src), name
