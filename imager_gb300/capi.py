@@ -93,6 +93,7 @@ _SIGNATURES = {
     "bgi_get_gridding_images_per_thread": (_i, [_vp, _vp]),
     "bgi_set_gridding_aggregation": (_i, [_vp, _i]),
     "bgi_replay_ready": (_i, [_vp]),
+    "bgi_set_replay": (_i, [_vp, _i]),
     "bgi_get_gridding_aggregation": (_i, [_vp, _vp]),
     "bgi_get_fft_mode": (_i, [_vp, _vp]),
     "bgi_image_averaging_gpu": (_i, [_vp, _i64, _i, _vp, _vp]),

@@ -205,6 +205,7 @@ struct bgi_imager {
         }
     };
     CallKey last_key, graph_key;
+    bool replay_enabled = true;  // bgi_set_replay
     bool have_last = false, replay_refused = false;
     cudaGraphExec_t graph_exec = nullptr;
     cudaStream_t cap_stream = nullptr;
@@ -965,6 +966,13 @@ int record_call(bgi_imager *im, F &&enqueue, cudaGraphExec_t *exec) {
 
 extern "C" {
 
+int bgi_set_replay(bgi_imager *im, int enable) {
+    if (!im) return set_error(BGI_ERR_INVALID, "set_replay: null handle");
+    im->drop_graph();
+    im->replay_enabled = enable != 0;
+    return BGI_OK;
+}
+
 int bgi_replay_ready(const bgi_imager *im) {
     if (!im) return set_error(BGI_ERR_INVALID, "replay_ready: null handle");
     return im->graph_exec != nullptr ? 1 : 0;
@@ -1473,7 +1481,7 @@ template <class F>
 int run_replayed(bgi_imager *im, const bgi_imager::CallKey &key, bool capturable, cudaStream_t s, F &&enqueue) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     BGI_TRY(check_cuda(cudaStreamIsCapturing(s, &cs), "capture status"));
-    const bool replay = capturable && !im->timing && cs == cudaStreamCaptureStatusNone;
+    const bool replay = capturable && im->replay_enabled && !im->timing && cs == cudaStreamCaptureStatusNone;
     const bool same = im->have_last && im->last_key == key;
     if (replay && same && im->graph_exec && im->graph_key == key) {
         const int st = check_cuda(cudaGraphLaunch(im->graph_exec, s), "image graph launch");

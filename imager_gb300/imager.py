@@ -382,6 +382,10 @@ class Imager:
         call("bgi_get_gridding_images_per_thread", self._h, C.byref(k))
         return k.value
 
+    def set_replay(self, enable: bool = True):
+        """Record repeated calls as a CUDA graph and launch it for later repeats (default on)."""
+        call("bgi_set_replay", self._h, int(bool(enable)))
+
     @property
     def replay_ready(self) -> bool:
         """Whether the next call identical to the last one launches its recorded CUDA graph."""

@@ -291,8 +291,11 @@ BGI_API int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_h
  * stage timing or inside a stream capture of the caller's; the same holds for the host-buffer
  * calls below when their host buffers are page-locked. */
 /* 1 when the handle holds the recorded graph of its last call (the next identical call
- * launches it), 0 otherwise; negative status on error. */
+ * launches it), 0 otherwise; negative status on error.  bgi_set_replay(im, 0) turns the
+ * recording off for the handle (every call issues its stream work; for one-off calls, whose
+ * recording would not be used), 1 (the default) on. */
 BGI_API int bgi_replay_ready(const bgi_imager *im);
+BGI_API int bgi_set_replay(bgi_imager *im, int enable);
 BGI_API int bgi_image(bgi_imager *im, const float *vis, int n_intervals, unsigned flags, float *images,
               void *stream);
 

@@ -201,3 +201,26 @@ def test_replay_host_buffers(im):
             for j in range(3):
                 assert rel_l2(got[i, j], ref2[i, j]) < 2e-6
     h.close()
+
+
+def test_replay_off(im):
+    """bgi_set_replay(0): repeated calls issue their work every time, with the same images."""
+    n = 128
+    obs = synth.small(seed=107, n_ant=32, n_intervals=1, n_channels=3, n_pixels=n)
+    vis = torch.from_numpy(obs.vis_f32()).cuda()
+    h = _imager(im, obs, n)
+    h.set_deterministic(True)
+    out = torch.empty((1, 3, n, n), dtype=torch.complex64, device="cuda")
+    h.image(vis, out=out)
+    ref = _bits(out)
+    h.set_replay(False)
+    for _ in range(3):
+        out.zero_()
+        h.image(vis, out=out)
+        assert not h.replay_ready
+        assert np.array_equal(_bits(out), ref)
+    h.set_replay(True)
+    for _ in range(3):
+        h.image(vis, out=out)
+    assert h.replay_ready and np.array_equal(_bits(out), ref)
+    h.close()
