@@ -145,8 +145,6 @@ struct bgi_server {
                                 a.flags.data(), a.cable.empty() ? nullptr : a.cable.data());
         if (*st == BGI_OK) *st = bgi_set_frequencies(h, a.n_channels, a.freqs.data());
         if (*st == BGI_OK) *st = bgi_set_deterministic(h, cfg.deterministic);
-        // each request images its own buffers once: recording calls for replay would only cost
-        if (*st == BGI_OK) *st = bgi_set_replay(h, 0);
         if (*st != BGI_OK) {
             bgi_destroy(h);
             return nullptr;
