@@ -63,6 +63,12 @@ def test_create_rejects_bad_config(lib):
     assert lib.bgi_create(None, C.byref(h)) == capi.ERR_INVALID
     # null handle calls
     assert lib.bgi_image(None, C.c_void_p(16), 1, 0, C.c_void_p(16), None) == capi.ERR_INVALID
+    assert lib.bgi_image_compressed(None, 1, C.c_void_p(16), C.c_void_p(16), 1, 0, C.c_void_p(16),
+                                    None) == capi.ERR_INVALID
+    assert lib.bgi_replay_ready(None) == capi.ERR_INVALID
+    assert lib.bgi_set_replay(None, 1) == capi.ERR_INVALID
+    assert lib.bgi_set_gridding_aggregation(None, 1) == capi.ERR_INVALID
+    assert lib.bgi_get_gridding_aggregation(None, None) == capi.ERR_INVALID
     assert lib.bgi_destroy(None) == capi.OK
 
 
