@@ -251,13 +251,14 @@ def test_cpu_runnable_plain_case_against_reference_build(oracle_lib):
 
 
 def test_fp32_fft_blocked_equals_scalar(oracle_lib):
-    """The CPU baseline's FP32 2D transform, blocked over 16 lines with a vectorisable inner loop,
-    gives the same bits as the one-line-at-a-time form (same butterflies, order and twiddles), for
-    batches below and above the thread count, and matches numpy to FP32 rounding."""
+    """The CPU baseline's FP32 2D transform, blocked over 16 lines with a vectorisable inner loop
+    and its radix-2 stages taken two at a time, gives the same bits as the one-line-at-a-time form
+    (same butterflies, order and twiddles), for even and odd stage counts, for batches below and
+    above the thread count, and matches numpy to FP32 rounding."""
     O = oracle_lib
     lib = O.library()
     rng = np.random.default_rng(5)
-    for n, batch in ((16, 1), (64, 3), (512, 1), (256, 40)):
+    for n, batch in ((2, 1), (8, 2), (16, 1), (32, 5), (64, 3), (512, 1), (256, 40)):
         x = rng.standard_normal((batch, n, n, 2)).astype(np.float32)
         a = np.empty_like(x)
         b = np.empty_like(x)
