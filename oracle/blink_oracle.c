@@ -364,46 +364,7 @@ static void fft_lines_f32(float *re, float *im, int n, const float *tw) {
             }
         }
     }
-    /* Two radix-2 stages (lengths 2m and 4m) at a time: each group of four elements s+k,
-     * s+k+m, s+k+2m, s+k+3m goes through both stages' butterflies in registers, with the
-     * radix-2 stages' own twiddle entries and operation order, so the results are the same
-     * bits with half the passes over the block. */
-    int len = 2;
-    for (; 2 * len <= n; len *= 4) {
-        const int m = len >> 1, step2 = n / len, step4 = n / (2 * len);
-        for (int s = 0; s < n; s += 2 * len) {
-            for (int k = 0; k < m; ++k) {
-                const float w2r = tw[2 * k * step2], w2i = tw[2 * k * step2 + 1];
-                const float wAr = tw[2 * k * step4], wAi = tw[2 * k * step4 + 1];
-                const float wBr = tw[2 * (k + m) * step4], wBi = tw[2 * (k + m) * step4 + 1];
-                float *restrict r0 = re + (s + k) * BGO_LINES, *restrict i0 = im + (s + k) * BGO_LINES;
-                float *restrict r1 = re + (s + k + m) * BGO_LINES, *restrict i1 = im + (s + k + m) * BGO_LINES;
-                float *restrict r2 = re + (s + k + 2 * m) * BGO_LINES, *restrict i2 = im + (s + k + 2 * m) * BGO_LINES;
-                float *restrict r3 = re + (s + k + 3 * m) * BGO_LINES, *restrict i3 = im + (s + k + 3 * m) * BGO_LINES;
-                for (int v = 0; v < BGO_LINES; ++v) {
-                    /* stage 2m: (0, 1) and (2, 3) */
-                    const float t1r = r1[v] * w2r - i1[v] * w2i, t1i = r1[v] * w2i + i1[v] * w2r;
-                    const float a1r = r0[v] - t1r, a1i = i0[v] - t1i;
-                    const float a0r = r0[v] + t1r, a0i = i0[v] + t1i;
-                    const float t3r = r3[v] * w2r - i3[v] * w2i, t3i = r3[v] * w2i + i3[v] * w2r;
-                    const float a3r = r2[v] - t3r, a3i = i2[v] - t3i;
-                    const float a2r = r2[v] + t3r, a2i = i2[v] + t3i;
-                    /* stage 4m: (0, 2) with twiddle k, (1, 3) with twiddle k + m */
-                    const float u2r = a2r * wAr - a2i * wAi, u2i = a2r * wAi + a2i * wAr;
-                    r2[v] = a0r - u2r;
-                    i2[v] = a0i - u2i;
-                    r0[v] = a0r + u2r;
-                    i0[v] = a0i + u2i;
-                    const float u3r = a3r * wBr - a3i * wBi, u3i = a3r * wBi + a3i * wBr;
-                    r3[v] = a1r - u3r;
-                    i3[v] = a1i - u3i;
-                    r1[v] = a1r + u3r;
-                    i1[v] = a1i + u3i;
-                }
-            }
-        }
-    }
-    if (len <= n) { /* an odd number of stages: the last, of length n, alone */
+    for (int len = 2; len <= n; len <<= 1) {
         const int half = len >> 1, step = n / len;
         for (int s = 0; s < n; s += len) {
             for (int k = 0; k < half; ++k) {
