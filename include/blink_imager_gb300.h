@@ -289,7 +289,10 @@ BGI_API int bgi_set_array_pointed(bgi_imager *im, int n_ant, const double *xyz_h
  * recorded into a CUDA graph, and the calls after it launch that graph on `stream` instead of
  * issuing each wave's kernels: the same work and results, one host launch per call.  Not under
  * stage timing or inside a stream capture of the caller's; the same holds for the host-buffer
- * calls below when their host buffers are page-locked. */
+ * calls below when their host buffers are page-locked.  A replayed call is ordered after the
+ * earlier work of `stream` only (not after the handle's own streams), so a caller who moves a
+ * handle's calls to another stream orders the two streams first, as the handle's rule that
+ * calls do not overlap already asks. */
 /* 1 when the handle holds the recorded graph of its last call (the next identical call
  * launches it), 0 otherwise; negative status on error.  bgi_set_replay(im, 0) turns the
  * recording off for the handle (every call issues its stream work; for one-off calls, whose
