@@ -97,3 +97,19 @@ def test_uvw_step_from_angles(lib):
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pointed_uvw.npz"))
     steps = imager.uvw_steps(g["rmat"], g["ha2000"], g["dec_aber"], g["lmst"], g["lmst2000"])
     np.testing.assert_allclose(steps, g["steps"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("lang,std", [("c", "c99"), ("c++", "c++11")])
+def test_header_compiles_alone(lang, std):
+    """The public header is plain C: it compiles on its own as C99 (pedantic) and as C++11, with
+    every warning on and none raised, so C, C++ and FFI binding generators can take it as is."""
+    import os
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no compiler")
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                       "blink_imager_gb300.h")
+    flags = ["-Wall", "-Wextra", "-Werror"] + (["-pedantic"] if lang == "c" else [])
+    r = subprocess.run([cc, f"-std={std}", *flags, "-fsyntax-only", "-x", lang, hdr], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
