@@ -364,7 +364,45 @@ static void fft_lines_f32(float *re, float *im, int n, const float *tw) {
             }
         }
     }
-    for (int len = 2; len <= n; len <<= 1) {
+    /* Two radix-2 stages (lengths 2m and 4m) per pass: each group of four elements s+k, s+k+m,
+     * s+k+2m, s+k+3m goes through both stages' butterflies in registers, with the radix-2 stages'
+     * own twiddle entries and operation order, so the results are the same bits in half the
+     * passes over the block.  (ivdep: the four rows of a group are at least 16 floats apart, so
+     * the lanes of the inner loop carry no dependence.) */
+    int len = 2;
+    for (; 2 * len <= n; len *= 4) {
+        const int m = len >> 1, step2 = n / len, step4 = n / (2 * len);
+        const int o1 = m * BGO_LINES, o2 = 2 * m * BGO_LINES, o3 = 3 * m * BGO_LINES;
+        for (int s = 0; s < n; s += 2 * len) {
+            for (int k = 0; k < m; ++k) {
+                const float w2r = tw[2 * k * step2], w2i = tw[2 * k * step2 + 1];
+                const float wAr = tw[2 * k * step4], wAi = tw[2 * k * step4 + 1];
+                const float wBr = tw[2 * (k + m) * step4], wBi = tw[2 * (k + m) * step4 + 1];
+                float *restrict R = re + (s + k) * BGO_LINES;
+                float *restrict I = im + (s + k) * BGO_LINES;
+#pragma GCC ivdep
+                for (int v = 0; v < BGO_LINES; ++v) {
+                    const float x0r = R[v], x0i = I[v], x1r = R[o1 + v], x1i = I[o1 + v];
+                    const float x2r = R[o2 + v], x2i = I[o2 + v], x3r = R[o3 + v], x3i = I[o3 + v];
+                    const float t1r = x1r * w2r - x1i * w2i, t1i = x1r * w2i + x1i * w2r;
+                    const float a1r = x0r - t1r, a1i = x0i - t1i, a0r = x0r + t1r, a0i = x0i + t1i;
+                    const float t3r = x3r * w2r - x3i * w2i, t3i = x3r * w2i + x3i * w2r;
+                    const float a3r = x2r - t3r, a3i = x2i - t3i, a2r = x2r + t3r, a2i = x2i + t3i;
+                    const float u2r = a2r * wAr - a2i * wAi, u2i = a2r * wAi + a2i * wAr;
+                    const float u3r = a3r * wBr - a3i * wBi, u3i = a3r * wBi + a3i * wBr;
+                    R[v] = a0r + u2r;
+                    I[v] = a0i + u2i;
+                    R[o2 + v] = a0r - u2r;
+                    I[o2 + v] = a0i - u2i;
+                    R[o1 + v] = a1r + u3r;
+                    I[o1 + v] = a1i + u3i;
+                    R[o3 + v] = a1r - u3r;
+                    I[o3 + v] = a1i - u3i;
+                }
+            }
+        }
+    }
+    if (len <= n) { /* an odd number of stages: the last, of length n, alone */
         const int half = len >> 1, step = n / len;
         for (int s = 0; s < n; s += len) {
             for (int k = 0; k < half; ++k) {

@@ -251,9 +251,10 @@ def test_cpu_runnable_plain_case_against_reference_build(oracle_lib):
 
 
 def test_fp32_fft_blocked_equals_scalar(oracle_lib):
-    """The CPU baseline's FP32 2D transform, blocked over 16 lines with a vectorisable inner loop,
-    gives the same bits as the one-line-at-a-time form (same butterflies, order and twiddles), for
-    batches below and above the thread count, and matches numpy to FP32 rounding."""
+    """The CPU baseline's FP32 2D transform, blocked over 16 lines with a vectorisable inner loop
+    and its radix-2 stages taken two at a time, gives the same bits as the one-line-at-a-time form
+    (same butterflies, order and twiddles), for even and odd stage counts, for batches below and
+    above the thread count, and matches numpy to FP32 rounding."""
     O = oracle_lib
     lib = O.library()
     rng = np.random.default_rng(5)
